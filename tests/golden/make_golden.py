@@ -1,0 +1,310 @@
+"""Generate golden vectors by running the reference implementation itself.
+
+Run in a container that has the reference checked out (default path below, or
+``CARC_REFERENCE``):  ``python tests/golden/make_golden.py``.  It writes
+``dense.npz``, ``tables.json``, ``trajectory.npz`` and ``numerics.npz`` next to
+this file.  The reference's randomness comes from numpy's global generator, so
+every case seeds it (``numpy.random.seed``) before calling into it.
+The GPU tests never run this script; they only read its outputs.
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+REF = os.environ.get("CARC_REFERENCE", "/root/reference")
+sys.path.insert(0, REF)
+sys.dont_write_bytecode = True
+
+from carcassonne.data import NDArrayData  # noqa: E402
+from carcassonne import sparse as rsparse  # noqa: E402
+from carcassonne.tensors._2d import dense as rdense  # noqa: E402
+from carcassonne.tensors._2d import sparse as rsp2  # noqa: E402
+from carcassonne.system import System  # noqa: E402
+from carcassonne.utils import relaxOver, computeCompressor, Multiplier, unitize  # noqa: E402
+from carcassonne.compression import computeProductCompressor  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def cn(rng, *shape):
+    return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex128)
+
+
+def D(a):
+    return NDArrayData(np.ascontiguousarray(a))
+
+
+def dense_cases():
+    rng = np.random.default_rng(1234)
+    out = {}
+    n = 0
+    for case in range(4):
+        dims = rng.integers(1, 4, size=12)
+        a, b, c, d, e, f, g, h, i, j, k, l = [int(x) for x in dims]
+        # stage 1: corner (a,b,c,d,e,f), side (d,e,f,g,h,i,j,k)
+        C = cn(rng, a, b, c, d, e, f)
+        S = cn(rng, d, e, f, g, h, i, j, k)
+        out[f"stage1_{case}_C"], out[f"stage1_{case}_S"] = C, S
+        out[f"stage1_{case}_out"] = rdense.formNormalizationStage1(D(C), D(S)).toArray().copy()
+        # absorb side into corner from the left: corner (a,b,c,d,e,f), side (g,h,i,a,b,c,j,k)
+        S2 = cn(rng, g, h, i, a, b, c, j, k)
+        out[f"absL_{case}_C"], out[f"absL_{case}_S"] = C, S2
+        out[f"absL_{case}_out"] = rdense.absorbDenseSideIntoCornerFromLeft(D(C), D(S2)).toArray().copy()
+        out[f"absR_{case}_C"], out[f"absR_{case}_S"] = C, S
+        out[f"absR_{case}_out"] = rdense.absorbDenseSideIntoCornerFromRight(D(C), D(S)).toArray().copy()
+        # stage 2: A (a,b,c,d), B (e,a,f,g)
+        A2 = cn(rng, a, b, c, d)
+        B2 = cn(rng, e, a, f, g)
+        out[f"stage2_{case}_A"], out[f"stage2_{case}_B"] = A2, B2
+        out[f"stage2_{case}_out"] = rdense.formNormalizationStage2(D(A2), D(B2)).toArray().copy()
+        # stage 3: s2_0 (x0,x1,k0,k1,l0,l1), s2_1 (x1,x0,k2,k3,l2,l3)
+        x0, x1 = a, b
+        k0, k1, k2, k3 = c, d, e, f
+        p = int(rng.integers(1, 4))
+        s20 = cn(rng, x0, x1, k0, k1, k0, k1)
+        s21 = cn(rng, x1, x0, k2, k3, k2, k3)
+        op = cn(rng, p, p)
+        v = cn(rng, k0, k1, k2, k3, p)
+        out[f"stage3_{case}_s20"], out[f"stage3_{case}_s21"] = s20, s21
+        out[f"stage3_{case}_op"], out[f"stage3_{case}_v"] = op, v
+        m = rdense.formDenseStage3(D(s20), D(s21), D(op))
+        out[f"stage3_{case}_Hv"] = m(D(v)).toArray().copy()
+        out[f"stage3_{case}_H"] = m.formMatrix().toArray().copy()
+        out[f"stage3_{case}_cost"] = np.array([m.cost_of_multiply, m.cost_of_formMatrix])
+        nm = rdense.formNormalizationStage3(D(s20), D(s21), NDArrayData.newIdentity(p))
+        out[f"stage3_{case}_Nv"] = nm(D(v)).toArray().copy()
+        out[f"stage3_{case}_N"] = nm.formMatrix().toArray().copy()
+        out[f"stage3_{case}_ncost"] = np.array([nm.cost_of_multiply, nm.cost_of_formMatrix])
+        # center into side, every direction
+        for direction in range(4):
+            g2 = int(rng.integers(1, 3))
+            side = cn(rng, a, b, c, d, e, f, g2, g2)
+            shp = [int(x) for x in rng.integers(1, 3, size=5)]
+            shp[direction] = g2
+            st = cn(rng, *shp)
+            o = cn(rng, shp[4], shp[4])
+            key = f"center_{case}_{direction}"
+            out[key + "_side"], out[key + "_S"], out[key + "_O"] = side, st, o
+            out[key + "_SS"] = rdense.absorbDenseCenterSSIntoSide(direction, D(side), D(st)).toArray().copy()
+            out[key + "_SOS"] = rdense.absorbDenseCenterSOSIntoSide(direction, D(side), D(st), D(o)).toArray().copy()
+        n += 1
+    np.savez_compressed(os.path.join(HERE, "dense.npz"), **out)
+
+
+# --- recording of the tag-pair schedule --------------------------------------
+_orig_contract = rsparse.contractSparseTensors
+_log = []
+
+
+def _recording_contract(dense_contractors, t1, t2):
+    keys1, keys2 = list(t1), list(t2)
+    rec = []
+    wrapped = {}
+    for key, handler in dense_contractors.items():
+        def wh(x, y, handler=handler):
+            r = handler(x, y)
+            if r is None or r[0] is None:
+                return r
+            tag, fn = r
+
+            def fn2(p, q, x=x, y=y, tag=tag, fn=fn):
+                rec.append([keys1.index(x), keys2.index(y), repr(tag)])
+                return fn(p, q)
+            return tag, fn2
+        wrapped[key] = wh
+    result = _orig_contract(wrapped, t1, t2)
+    _log.append(dict(tags1=[repr(k) for k in keys1], tags2=[repr(k) for k in keys2],
+                     entries=rec, result=[repr(k) for k in result]))
+    return result
+
+
+def _install_recorder():
+    rsp2.contractSparseTensors = _recording_contract
+
+
+def _stage3_terms(system):
+    """Term list of formExpectationStage3 recorded through the dense builders."""
+    s1 = [rsp2.formExpectationStage1(system.corners[i], system.sides[i]) for i in range(4)]
+    s2a = rsp2.formExpectationStage2(s1[0], s1[1])
+    s2b = rsp2.formExpectationStage2(s1[2], s1[3])
+    op = system.operator_center_tensor
+    rec = []
+    ids = {}
+    for which, t in ((0, s2a), (1, s2b), (2, op)):
+        for i, (k, v) in enumerate(t.items()):
+            ids[(which, id(v))] = i
+    orig_d, orig_n = rsp2.formDenseStage3, rsp2.formNormalizationStage3
+
+    def rd(a, b, c):
+        rec.append([ids[(0, id(a))], ids[(1, id(b))], ids[(2, id(c))], 0])
+        return orig_d(a, b, c)
+
+    def rn(a, b, c):
+        if (2, id(c)) in ids:
+            rec.append([ids[(0, id(a))], ids[(1, id(b))], ids[(2, id(c))], 1])
+        return orig_n(a, b, c)
+    rsp2.formDenseStage3, rsp2.formNormalizationStage3 = rd, rn
+    try:
+        H, N = rsp2.formExpectationStage3(s2a, s2b, op)
+    finally:
+        rsp2.formDenseStage3, rsp2.formNormalizationStage3 = orig_d, orig_n
+    return dict(s2_0=[repr(k) for k in s2a], s2_1=[repr(k) for k in s2b], op=[repr(k) for k in op],
+                terms=rec, cost_multiply=int(H.cost_of_multiply), cost_formMatrix=int(H.cost_of_formMatrix))
+
+
+def operators():
+    X, Y, Z = NDArrayData.X, NDArrayData.Y, NDArrayData.Z
+    return {
+        "ti": lambda: rsparse.makeSimpleSparseOperator(O=-3.0 * Z, OO_UD=(X, -1.0 * X), OO_LR=(X, -1.0 * X)),
+        "heis": lambda: rsparse.makeSparseOperator(OO_UDs=[(X, X), (Y, Y), (Z, Z)], OO_LRs=[(X, X), (Y, Y), (Z, Z)]),
+        "ising_ud": lambda: rsparse.makeSimpleSparseOperator(O=-1.0 * Z, OO_UD=(X, -0.5 * X)),
+    }
+
+
+def bond_system(op, D_, seed):
+    """Unit corners and identity bond boundaries (a positive-definite norm
+    environment) of bond dimension D_ around a random center."""
+    rng = np.random.default_rng(seed)
+    d = next(iter(op.values())).shape[0]
+    corners = tuple({rsparse.Identity(): NDArrayData.newTrivial((1,) * 6, dtype=np.complex128)} for _ in range(4))
+    eye = np.eye(D_, dtype=np.complex128).reshape((1,) * 6 + (D_, D_))
+    sides = tuple({rsparse.Identity(): NDArrayData(eye.copy())} for _ in range(4))
+    st = rng.standard_normal((D_,) * 4 + (d,)).astype(np.complex128)
+    st /= np.linalg.norm(st)
+    return System(corners, sides, NDArrayData(st), op)
+
+
+def tables_and_trajectories():
+    _install_recorder()
+    tables = {}
+    traj = {}
+    schedules = {
+        "ti": (2, [0, 1, 2, 3, 0, 1], 7),
+        "heis": (2, [0, 2, 1, 3, 0], 11),
+        "ising_ud": (1, [0, 2, 1, 3, 1, 3, 0, 2], 5),
+    }
+    for name, mk in operators().items():
+        D_, steps, seed = schedules[name]
+        # distinct data objects per tag: the stage-3 recorder identifies data by id()
+        op = {k: NDArrayData(v.toArray().copy()) for k, v in mk().items()}
+        system = bond_system(op, D_, seed)
+        st = system.state_center_data.toArray().copy()
+        traj[f"{name}_state0"] = st
+        traj[f"{name}_op_tags"] = np.array([repr(k) for k in op])
+        for ki, (k, v) in enumerate(op.items()):
+            traj[f"{name}_op_{ki}"] = v.toArray().astype(np.complex128)
+        records = []
+        for step, direction in enumerate(steps):
+            _log.clear()
+            Hm, Nm = system.formExpectationAndNormalizationMultipliers()
+            stage_log = list(_log)
+            terms = _stage3_terms(system)
+            Hd = Hm.formMatrix().toArray().copy()
+            Nd = Nm.formMatrix().toArray().copy()
+            import scipy.linalg as sla
+            w, v = sla.eigh(Hd, Nd)
+            e, nrm = system.computeExpectationAndNormalization()
+            traj[f"{name}_{step}_H"] = Hd
+            traj[f"{name}_{step}_N"] = Nd
+            traj[f"{name}_{step}_E"] = np.array([w[0], e, nrm])
+            for i in range(4):
+                for kj, (k, v_) in enumerate(system.corners[i].items()):
+                    traj[f"{name}_{step}_corner{i}_{kj}"] = v_.toArray().copy().copy()
+                for kj, (k, v_) in enumerate(system.sides[i].items()):
+                    traj[f"{name}_{step}_side{i}_{kj}"] = v_.toArray().copy().copy()
+            traj[f"{name}_{step}_state"] = system.state_center_data.toArray().copy()
+            rec = dict(direction=direction,
+                       corners=[[repr(k) for k in c] for c in system.corners],
+                       sides=[[repr(k) for k in s] for s in system.sides],
+                       stage_calls=stage_log, stage3=terms)
+            # relaxOver from the current center
+            np.random.seed(100 + step)
+            x = relaxOver(system.state_center_data, Hm, Nm, maximum_number_of_multiplications=100)
+            xr = x.toArray().ravel()
+            rq = np.vdot(xr, Hd @ xr) / np.vdot(xr, Nd @ xr)
+            traj[f"{name}_{step}_relax"] = np.array([rq])
+            # minimize with the dense solver, then absorb towards direction
+            system.minimizeExpectationUsingFullEigensolver()
+            traj[f"{name}_{step}_minstate"] = system.state_center_data.toArray().copy()
+            _log.clear()
+            system.contractTowards(direction)
+            rec["absorb_calls"] = list(_log)
+            traj[f"{name}_{step}_after_state"] = system.state_center_data.toArray().copy()
+            records.append(rec)
+        tables[name] = dict(D=D_, steps=steps, seed=seed, records=records)
+    rsp2.contractSparseTensors = _orig_contract
+    with open(os.path.join(HERE, "tables.json"), "w") as f:
+        json.dump(tables, f, indent=0, separators=(",", ":"))
+    np.savez_compressed(os.path.join(HERE, "trajectory.npz"), **traj)
+
+
+def numerics():
+    rng = np.random.default_rng(77)
+    out = {}
+    # normalizeAxis
+    for case, shape in enumerate([(2, 3, 2, 3, 2), (3, 3, 3, 3, 2), (4, 2, 5), (6, 1, 2)]):
+        t = cn(rng, *shape)
+        for axis in range(len(shape)):
+            if np.prod(shape) // shape[axis] < shape[axis]:
+                continue
+            iso, nz, dz = NDArrayData(t).normalizeAxis(axis)
+            key = f"nax_{case}_{axis}"
+            out[key + "_in"] = t
+            out[key + "_iso"] = iso.toArray().copy()
+            out[key + "_norm"] = nz.toArray().copy()
+            out[key + "_denorm"] = dz.toArray().copy()
+            a, b = NDArrayData(t).normalizeAxis(axis, True)
+            out[key + "_sq_a"] = a.toArray().copy()
+            out[key + "_sq_b"] = b.toArray().copy()
+    # unitize
+    for case in range(3):
+        m = cn(rng, 7, 3 + case)
+        out[f"unitize_{case}_in"] = m
+        out[f"unitize_{case}_out"] = unitize(m)
+    # computeCompressor (eigh branch)
+    for case, (old, new) in enumerate([(6, 3), (5, 5), (8, 4)]):
+        a = cn(rng, 9, old)
+        g = a.conj().T @ a
+        c, ic = computeCompressor(old, new, Multiplier((old, old), lambda v: g @ v, 0, lambda: g, 0), np.complex128)
+        out[f"cc_{case}_in"] = g
+        out[f"cc_{case}_c"] = c
+        out[f"cc_{case}_meta"] = np.array([old, new])
+        c2, ic2 = computeCompressor(old, new, Multiplier((old, old), lambda v: g @ v, 0, lambda: g, 0), np.complex128, True)
+        out[f"cc_{case}_cn"] = c2
+        out[f"cc_{case}_icn"] = ic2
+    # computeProductCompressor on an exactly compressible pair (tests/test_compression.py:11-30)
+    for case, (new, extra, l, r, opd) in enumerate([(2, 2, 3, 4, 2), (3, 1, 2, 2, 1)]):
+        old = new + extra
+        Lc = cn(rng, l, new, new, opd)
+        Lc = Lc + Lc.transpose(0, 2, 1, 3).conj()
+        Lf = np.zeros((l, old, old, opd), np.complex128)
+        Lf[:, :new, :new, :] = Lc
+        Rc = cn(rng, new, new, opd, r)
+        Rc = Rc + Rc.transpose(1, 0, 2, 3).conj()
+        Rf = np.zeros((old, old, opd, r), np.complex128)
+        Rf[:new, :new] = Rc
+        np.random.seed(5 + case)
+        P = computeProductCompressor(NDArrayData(Lf), NDArrayData(Rf), new).toArray().copy()
+        out[f"pc_{case}_L"], out[f"pc_{case}_R"], out[f"pc_{case}_P"] = Lf, Rf, P
+        out[f"pc_{case}_exact"] = np.tensordot(Lc, Rc, ((1, 2, 3), (0, 1, 2)))
+    # relaxOver on small Hermitian pencils (tests/test_utils.py:857-878)
+    for case, n in enumerate([4, 7, 10]):
+        h = cn(rng, n, n)
+        h = h + h.conj().T
+        a = cn(rng, n, n)
+        nm = a.conj().T @ a + n * np.eye(n)
+        v0 = cn(rng, n)
+        x = relaxOver(NDArrayData(v0.copy()), Multiplier.fromMatrix(NDArrayData(h)), Multiplier.fromMatrix(NDArrayData(nm)))
+        out[f"relax_{case}_H"], out[f"relax_{case}_N"], out[f"relax_{case}_v0"] = h, nm, v0
+        out[f"relax_{case}_x"] = x.toArray().copy()
+    np.savez_compressed(os.path.join(HERE, "numerics.npz"), **out)
+
+
+if __name__ == "__main__":
+    dense_cases()
+    tables_and_trajectories()
+    numerics()
+    for fn in ("dense.npz", "tables.json", "trajectory.npz", "numerics.npz"):
+        print(fn, os.path.getsize(os.path.join(HERE, fn)))
