@@ -1,0 +1,739 @@
+// Lowest eigenpair of the generalized Hermitian-definite problem H x = l N x
+// on the GPU (the center-site optimisation of System.minimizeExpectation,
+// system/_2d.py:489-502):
+//   N = L L^H (blocked Cholesky), C = L^{-1} H L^{-H},
+//   Lanczos with full reorthogonalisation (two classical Gram-Schmidt passes
+//   with warp-shuffle dot products) on C, restarted from the Ritz vector,
+//   the small tridiagonal problem solved on the device by Sturm bisection and
+//   inverse iteration, and x = L^{-H} u.
+// The host loop syncs the stream only at convergence checkpoints.
+#include "common.cuh"
+#include "contract.cuh"
+#include "linalg.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace carc {
+
+namespace {
+
+inline int64_t a256(int64_t b) { return (b + 255) / 256 * 256; }
+
+// y = A x, A n x n row-major; one warp per row
+__global__ void gemv_kernel(int n, const double2* __restrict__ A, const double2* __restrict__ x, double2* __restrict__ y) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
+    const double2* a = A + (int64_t)row * n;
+    double2 s = make_double2(0.0, 0.0);
+    for (int j = lane; j < n; j += 32) cfma(s, a[j], x[j]);
+    s = warp_sum2(s);
+    if (lane == 0) y[row] = s;
+  }
+}
+
+// h[r] = sum_i conj(Q[r][i]) w[i] for r < rows; one warp per row
+__global__ void proj_kernel(int n, int rows, const double2* __restrict__ Q, const double2* __restrict__ w,
+                            double2* __restrict__ h) {
+  const int lane = threadIdx.x & 31;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += warps) {
+    const double2* q = Q + (int64_t)r * n;
+    double2 s = make_double2(0.0, 0.0);
+    for (int j = lane; j < n; j += 32) s = cadd(s, cmulc(q[j], w[j]));
+    s = warp_sum2(s);
+    if (lane == 0) h[r] = s;
+  }
+}
+
+// w[i] += sign * sum_r h[r] Q[r][i]
+__global__ void combine_kernel(int n, int rows, const double2* __restrict__ Q, const double2* __restrict__ h,
+                               double sign, double2* __restrict__ w, int overwrite) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int r = 0; r < rows; ++r) cfma(s, h[r], Q[(int64_t)r * n + i]);
+    w[i] = overwrite ? cscale(s, sign) : cadd(w[i], cscale(s, sign));
+  }
+}
+
+// w -= alpha_j q_j + beta_{j-1} q_{j-1}; alpha_j = Re(dot) read from the device
+__global__ void lanczos_axpy_kernel(int n, int j, const double2* __restrict__ dotv, double* __restrict__ alpha,
+                                    const double* __restrict__ beta, const double2* __restrict__ qj,
+                                    const double2* __restrict__ qjm1, double2* __restrict__ w) {
+  const double a = dotv->x;
+  const double b = j > 0 ? beta[j - 1] : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) alpha[j] = a;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 v = csub(w[i], cscale(qj[i], a));
+    if (j > 0) v = csub(v, cscale(qjm1[i], b));
+    w[i] = v;
+  }
+}
+
+// beta_j = ||w||, q_{j+1} = w / beta_j  (breakdown flag when beta is negligible)
+__global__ void lanczos_next_kernel(int n, int j, const double2* __restrict__ nrm2, double* __restrict__ beta,
+                                    const double2* __restrict__ w, double2* __restrict__ qn, double scale_ref,
+                                    int* __restrict__ breakdown) {
+  const double b = sqrt(fmax(nrm2->x, 0.0));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    beta[j] = b;
+    if (b <= 1e-13 * scale_ref) *breakdown = 1;
+  }
+  const double inv = b > 0 ? 1.0 / b : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) qn[i] = cscale(w[i], inv);
+}
+
+__global__ void scale_by_norm_kernel(int n, const double2* __restrict__ nrm2, double2* __restrict__ v) {
+  const double b = sqrt(fmax(nrm2->x, 0.0));
+  const double inv = b > 0 ? 1.0 / b : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = cscale(v[i], inv);
+}
+
+// Sturm count of eigenvalues of the tridiagonal (alpha, beta) below x
+__device__ int sturm_count(int m, const double* alpha, const double* beta, double x) {
+  int c = 0;
+  double d = 1.0;
+  for (int i = 0; i < m; ++i) {
+    double b2 = i > 0 ? beta[i - 1] * beta[i - 1] : 0.0;
+    d = alpha[i] - x - (i > 0 ? b2 / d : 0.0);
+    if (d == 0.0) d = -1e-300;
+    if (d < 0) ++c;
+  }
+  return c;
+}
+
+// Lowest eigenpair of the m x m tridiagonal matrix; out = (lambda, residual
+// estimate |beta_m s_m|), s = eigenvector (m).  Single thread; m <= MAXM.
+constexpr int MAXM = 512;
+
+__global__ void tridiag_lowest_kernel(int m, const double* __restrict__ alpha, const double* __restrict__ beta,
+                                      double* __restrict__ out, double* __restrict__ s, double* __restrict__ scratch) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double lo = 1e300, hi = -1e300;
+  for (int i = 0; i < m; ++i) {
+    double r = (i > 0 ? fabs(beta[i - 1]) : 0.0) + (i + 1 < m ? fabs(beta[i]) : 0.0);
+    lo = fmin(lo, alpha[i] - r);
+    hi = fmax(hi, alpha[i] + r);
+  }
+  double span = fmax(hi - lo, 1e-300);
+  for (int it = 0; it < 200; ++it) {
+    double mid = 0.5 * (lo + hi);
+    if (sturm_count(m, alpha, beta, mid) >= 1) hi = mid; else lo = mid;
+    if (hi - lo <= 1e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300 * span) break;
+  }
+  const double lam = 0.5 * (lo + hi);
+  // inverse iteration with partial pivoting on T - (lam - delta) I
+  double* dl = scratch;          // sub
+  double* dd = scratch + MAXM;   // diag
+  double* du = scratch + 2 * MAXM;  // super
+  double* du2 = scratch + 3 * MAXM;  // second super (fill-in)
+  double* x = s;
+  const double shift = lam - 1e-12 * span;
+  for (int i = 0; i < m; ++i) x[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (i % 7));
+  int piv[MAXM];
+  for (int iter = 0; iter < 3; ++iter) {
+    for (int i = 0; i < m; ++i) {
+      dd[i] = alpha[i] - shift;
+      dl[i] = i + 1 < m ? beta[i] : 0.0;
+      du[i] = i + 1 < m ? beta[i] : 0.0;
+      du2[i] = 0.0;
+    }
+    // LU with partial pivoting (LAPACK gttrf pattern)
+    for (int i = 0; i + 1 < m; ++i) {
+      if (fabs(dd[i]) >= fabs(dl[i])) {
+        piv[i] = 0;
+        double f = dd[i] != 0.0 ? dl[i] / dd[i] : 0.0;
+        dl[i] = f;
+        dd[i + 1] -= f * du[i];
+      } else {
+        piv[i] = 1;
+        double f = dd[i] / dl[i];
+        dd[i] = dl[i];
+        dl[i] = f;
+        double t = du[i];
+        du[i] = dd[i + 1];
+        dd[i + 1] = t - f * dd[i + 1];
+        if (i + 2 < m) {
+          du2[i] = du[i + 1];
+          du[i + 1] = -f * du[i + 1];
+        }
+      }
+    }
+    // solve L U y = x
+    for (int i = 0; i + 1 < m; ++i) {
+      if (piv[i] == 0) {
+        x[i + 1] -= dl[i] * x[i];
+      } else {
+        double t = x[i];
+        x[i] = x[i + 1];
+        x[i + 1] = t - dl[i] * x[i + 1];
+      }
+    }
+    for (int i = m - 1; i >= 0; --i) {
+      double v = x[i];
+      if (i + 1 < m) v -= du[i] * x[i + 1];
+      if (i + 2 < m) v -= du2[i] * x[i + 2];
+      double d = dd[i] != 0.0 ? dd[i] : 1e-300;
+      x[i] = v / d;
+    }
+    double nrm = 0.0;
+    for (int i = 0; i < m; ++i) nrm += x[i] * x[i];
+    nrm = sqrt(nrm);
+    for (int i = 0; i < m; ++i) x[i] /= nrm;
+  }
+  out[0] = lam;
+  out[1] = fabs(beta[m - 1] * x[m - 1]);
+}
+
+// copy real s (m) into complex h (m)
+__global__ void real_to_complex_kernel(int m, const double* __restrict__ s, double2* __restrict__ h) {
+  for (int i = threadIdx.x; i < m; i += blockDim.x) h[i] = make_double2(s[i], 0.0);
+}
+
+inline int blocks_for(int64_t n, int threads = 256) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, threads), 4 * 152));
+}
+
+struct LanczosWs {
+  double2* Q;
+  double2* w;
+  double2* h;
+  double2* dotv;
+  double2* nrm;
+  double* alpha;
+  double* beta;
+  double* tri_out;
+  double* s;
+  double* scratch;
+  int* breakdown;
+  void* dot_ws;
+  int64_t dot_ws_bytes;
+};
+
+int64_t lanczos_ws_layout(int n, int mk, LanczosWs* L, void* base) {
+  char* p = static_cast<char*>(base);
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) {
+    void* r = p ? p + off : nullptr;
+    off += a256(bytes);
+    return r;
+  };
+  LanczosWs t;
+  t.Q = (double2*)take((int64_t)(mk + 1) * n * 16);
+  t.w = (double2*)take((int64_t)n * 16);
+  t.h = (double2*)take((int64_t)(mk + 1) * 16);
+  t.dotv = (double2*)take(16);
+  t.nrm = (double2*)take(16);
+  t.alpha = (double*)take((int64_t)(mk + 1) * 8);
+  t.beta = (double*)take((int64_t)(mk + 1) * 8);
+  t.tri_out = (double*)take(4 * 8);
+  t.s = (double*)take((int64_t)MAXM * 8);
+  t.scratch = (double*)take((int64_t)4 * MAXM * 8);
+  t.breakdown = (int*)take(16);
+  t.dot_ws_bytes = dot_workspace_size(n);
+  t.dot_ws = take(t.dot_ws_bytes);
+  if (L) *L = t;
+  return off;
+}
+
+}  // namespace
+
+int64_t lanczos_workspace_size(int n, int max_krylov) {
+  int mk = std::max(1, std::min(max_krylov, std::min(n, MAXM)));
+  return lanczos_ws_layout(n, mk, nullptr, nullptr);
+}
+
+int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigenvalue, int max_krylov,
+                   int max_restarts, double tol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream) {
+  if (n < 1) return fail(CARC_BAD_SHAPE, "lanczos: n = %d", n);
+  const int mk = std::max(1, std::min(max_krylov, std::min(n, MAXM)));
+  if (ws_bytes < lanczos_workspace_size(n, max_krylov)) return fail(CARC_BAD_ARG, "lanczos: workspace too small");
+  LanczosWs W;
+  lanczos_ws_layout(n, mk, &W, ws);
+  const double2* C = static_cast<const double2*>(Cv);
+  const int gb = blocks_for((int64_t)n * 32);
+  const int eb = blocks_for(n);
+  // start vector
+  CARC_CHECK_CUDA(cudaMemcpyAsync(W.Q, u0, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+  CARC_RETURN_IF(dot_launch(n, W.Q, W.Q, 1, W.nrm, W.dot_ws, W.dot_ws_bytes, stream));
+  scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.nrm, W.Q);
+  CARC_CHECK_LAUNCH();
+  // scale reference for the breakdown test: |C|_max row sum estimate via |C q0|
+  double lam = 0.0, res = 0.0;
+  int total = 0;
+  bool converged = false;
+  for (int restart = 0; restart <= max_restarts && !converged; ++restart) {
+    CARC_CHECK_CUDA(cudaMemsetAsync(W.breakdown, 0, sizeof(int), stream));
+    int m = 0;
+    double scale_ref = 1.0;
+    {
+      // scale of C from |C q0|
+      gemv_kernel<<<gb, 256, 0, stream>>>(n, C, W.Q, W.w);
+      CARC_CHECK_LAUNCH();
+      CARC_RETURN_IF(dot_launch(n, W.w, W.w, 1, W.nrm, W.dot_ws, W.dot_ws_bytes, stream));
+      double2 hn;
+      CARC_CHECK_CUDA(cudaMemcpyAsync(&hn, W.nrm, 16, cudaMemcpyDeviceToHost, stream));
+      CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+      scale_ref = std::max(sqrt(std::max(hn.x, 0.0)), 1e-300);
+    }
+    for (int j = 0; j < mk; ++j) {
+      double2* qj = W.Q + (int64_t)j * n;
+      double2* qn = W.Q + (int64_t)(j + 1) * n;
+      gemv_kernel<<<gb, 256, 0, stream>>>(n, C, qj, W.w);
+      CARC_CHECK_LAUNCH();
+      CARC_RETURN_IF(dot_launch(n, qj, W.w, 1, W.dotv, W.dot_ws, W.dot_ws_bytes, stream));
+      lanczos_axpy_kernel<<<eb, 256, 0, stream>>>(n, j, W.dotv, W.alpha, W.beta, qj,
+                                                  j > 0 ? W.Q + (int64_t)(j - 1) * n : qj, W.w);
+      CARC_CHECK_LAUNCH();
+      for (int pass = 0; pass < 2; ++pass) {
+        proj_kernel<<<blocks_for((int64_t)(j + 1) * 32), 256, 0, stream>>>(n, j + 1, W.Q, W.w, W.h);
+        CARC_CHECK_LAUNCH();
+        combine_kernel<<<eb, 256, 0, stream>>>(n, j + 1, W.Q, W.h, -1.0, W.w, 0);
+        CARC_CHECK_LAUNCH();
+      }
+      CARC_RETURN_IF(dot_launch(n, W.w, W.w, 1, W.nrm, W.dot_ws, W.dot_ws_bytes, stream));
+      lanczos_next_kernel<<<eb, 256, 0, stream>>>(n, j, W.nrm, W.beta, W.w, qn, scale_ref, W.breakdown);
+      CARC_CHECK_LAUNCH();
+      m = j + 1;
+      ++total;
+      const bool last = (j + 1 == mk);
+      if ((m % 8) == 0 || last || m == n) {
+        tridiag_lowest_kernel<<<1, 32, 0, stream>>>(m, W.alpha, W.beta, W.tri_out, W.s, W.scratch);
+        CARC_CHECK_LAUNCH();
+        double hv[2];
+        int bd = 0;
+        CARC_CHECK_CUDA(cudaMemcpyAsync(hv, W.tri_out, 16, cudaMemcpyDeviceToHost, stream));
+        CARC_CHECK_CUDA(cudaMemcpyAsync(&bd, W.breakdown, sizeof(int), cudaMemcpyDeviceToHost, stream));
+        CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+        lam = hv[0];
+        res = hv[1];
+        if (bd || res <= tol * std::max(fabs(lam), 1e-300) || m == n) {
+          converged = true;
+          break;
+        }
+      }
+    }
+    // Ritz vector u = Q^T s (becomes the restart vector)
+    real_to_complex_kernel<<<1, 256, 0, stream>>>(m, W.s, W.h);
+    CARC_CHECK_LAUNCH();
+    combine_kernel<<<eb, 256, 0, stream>>>(n, m, W.Q, W.h, 1.0, W.w, 1);
+    CARC_CHECK_LAUNCH();
+    CARC_RETURN_IF(dot_launch(n, W.w, W.w, 1, W.nrm, W.dot_ws, W.dot_ws_bytes, stream));
+    scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.nrm, W.w);
+    CARC_CHECK_LAUNCH();
+    CARC_CHECK_CUDA(cudaMemcpyAsync(W.Q, W.w, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+  }
+  CARC_CHECK_CUDA(cudaMemcpyAsync(u, W.w, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+  if (eigenvalue) *eigenvalue = lam;
+  if (iterations) *iterations = total;
+  if (!converged)
+    return fail(CARC_NOT_CONVERGED, "lanczos: residual %.3e after %d iterations (tolerance %.1e)", res, total, tol);
+  return CARC_OK;
+}
+
+int64_t hegv_workspace_size(int n, int max_krylov) {
+  int64_t mat = a256((int64_t)n * n * 16);
+  carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
+  int64_t g = std::max<int64_t>(gett_workspace_size(d, 1), 0);
+  int64_t sub = std::max({potrf_workspace_size(n), trtri_workspace_size(n), a256(g),
+                          lanczos_workspace_size(n, max_krylov)});
+  return 4 * mat + 2 * a256((int64_t)n * 16) + a256(64) + sub;
+}
+
+int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, double* eigenvalue, int max_krylov,
+                int max_restarts, double tol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream) {
+  if (n < 1) return fail(CARC_BAD_SHAPE, "hegv: n = %d", n);
+  if (ws_bytes < hegv_workspace_size(n, max_krylov)) return fail(CARC_BAD_ARG, "hegv: workspace too small");
+  char* p = static_cast<char*>(ws);
+  int64_t mat = a256((int64_t)n * n * 16);
+  double2* Lm = (double2*)p;
+  double2* Li = (double2*)(p + mat);
+  double2* T1 = (double2*)(p + 2 * mat);
+  double2* Cm = (double2*)(p + 3 * mat);
+  double2* u0 = (double2*)(p + 4 * mat);
+  double2* u = (double2*)(p + 4 * mat + a256((int64_t)n * 16));
+  int* status = (int*)(p + 4 * mat + 2 * a256((int64_t)n * 16));
+  void* sub = p + 4 * mat + 2 * a256((int64_t)n * 16) + a256(64);
+  int64_t sub_bytes = ws_bytes - (4 * mat + 2 * a256((int64_t)n * 16) + a256(64));
+
+  CARC_CHECK_CUDA(cudaMemcpyAsync(Lm, Nm, (int64_t)n * n * 16, cudaMemcpyDeviceToDevice, stream));
+  CARC_RETURN_IF(potrf(n, Lm, status, sub, sub_bytes, stream));
+  int hstat = 0;
+  CARC_CHECK_CUDA(cudaMemcpyAsync(&hstat, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+  if (hstat != CARC_OK) return fail(CARC_NOT_POSDEF, "hegv: the normalization matrix is not positive definite");
+  CARC_RETURN_IF(trtri_lower(n, Lm, Li, sub, sub_bytes, stream));
+  // T1 = Linv H ; C = T1 Linv^H
+  {
+    carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
+    const void* pa[1] = {Li};
+    const void* pb[1] = {H};
+    void* pc[1] = {T1};
+    int32_t e[3] = {0, 0, 0};
+    CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+    carc_contract_desc d2 = DescBuilder().m(n, n, n).n(n, n, 1).k(n, 1, 1).d;
+    d2.conj_b = 1;
+    const void* pa2[1] = {T1};
+    const void* pb2[1] = {Li};
+    void* pc2[1] = {Cm};
+    CARC_RETURN_IF(gett_launch(d2, pa2, 1, pb2, 1, pc2, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+  }
+  // start vector u0 = L^H x0 (or a fixed vector)
+  if (x0) {
+    carc_contract_desc d = DescBuilder().m(n, 1, 1).k(n, n, 1).d;  // u0[j] = sum_i conj(L[i][j]) x0[i]
+    d.conj_a = 1;
+    const void* pa[1] = {Lm};
+    const void* pb[1] = {x0};
+    void* pc[1] = {u0};
+    int32_t e[3] = {0, 0, 0};
+    CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+  } else {
+    CARC_RETURN_IF(fill_launch(n, make_double2(1.0, 0.0), u0, stream));
+  }
+  int st = lanczos_lowest(n, Cm, u0, u, eigenvalue, max_krylov, max_restarts, tol, iterations, sub, sub_bytes, stream);
+  if (st != CARC_OK && st != CARC_NOT_CONVERGED) return st;
+  // x = Linv^H u : x[j] = sum_i conj(Li[i][j]) u[i]
+  {
+    carc_contract_desc d = DescBuilder().m(n, 1, 1).k(n, n, 1).d;
+    d.conj_a = 1;
+    const void* pa[1] = {Li};
+    const void* pb[1] = {u};
+    void* pc[1] = {x};
+    int32_t e[3] = {0, 0, 0};
+    CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+  }
+  return st;
+}
+
+// ---------------------------------------------------------------------------
+// relaxOver (utils.py:805-878) on the GPU: restarted Krylov / Rayleigh-Ritz on
+// M = N^{-1} H with single-pass classical Gram-Schmidt, the k x k projected
+// (non-Hermitian) eigenproblem solved on the device, and the reference's
+// stopping rule (|change of the lowest Ritz value| <= tol, complete space, or
+// the multiplication budget).  M is formed once: M = L^{-H} L^{-1} H.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int SMALLK = 8;
+
+__device__ double2 cdiv(double2 a, double2 b) {
+  double den = cabs2(b);
+  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+
+__device__ double2 csqrt_d(double2 z) {
+  double r = sqrt(sqrt(cabs2(z)));
+  double th = 0.5 * atan2(z.y, z.x);
+  return make_double2(r * cos(th), r * sin(th));
+}
+
+// Eigenvalues of a small complex matrix by shifted QR iterations (full
+// matrix, Gram-Schmidt QR, Wilkinson shifts, deflation from the bottom);
+// picks the eigenvalue of minimum real part and its eigenvector of the
+// original matrix by pivoted elimination.  Single thread.
+__global__ void small_eig_min_real_kernel(int k, const double2* __restrict__ A0, double2* __restrict__ lam_out,
+                                          double2* __restrict__ vec_out, int* __restrict__ status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double2 A[SMALLK][SMALLK], Q[SMALLK][SMALLK], R[SMALLK][SMALLK];
+  double2 ev[SMALLK];
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < k; ++j) A[i][j] = A0[i * k + j];
+  double scale = 0.0;
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < k; ++j) scale = fmax(scale, sqrt(cabs2(A[i][j])));
+  if (scale == 0.0) scale = 1.0;
+  int m = k;
+  int guard = 0;
+  while (m > 0 && guard < 500 * SMALLK) {
+    ++guard;
+    if (m == 1) {
+      ev[0] = A[0][0];
+      m = 0;
+      break;
+    }
+    // deflation test on the last row
+    double off = 0.0;
+    for (int j = 0; j < m - 1; ++j) off = fmax(off, sqrt(cabs2(A[m - 1][j])));
+    if (off <= 1e-15 * scale) {
+      ev[m - 1] = A[m - 1][m - 1];
+      --m;
+      continue;
+    }
+    // Wilkinson shift from the trailing 2x2 block
+    double2 a = A[m - 2][m - 2], b = A[m - 2][m - 1], c = A[m - 1][m - 2], d = A[m - 1][m - 1];
+    double2 tr = cadd(a, d), det = csub(cmul(a, d), cmul(b, c));
+    double2 disc = csqrt_d(csub(cscale(cmul(tr, tr), 0.25), det));
+    double2 h = cscale(tr, 0.5);
+    double2 l1 = cadd(h, disc), l2 = csub(h, disc);
+    double2 mu = cabs2(csub(l1, d)) < cabs2(csub(l2, d)) ? l1 : l2;
+    if (guard % 37 == 0) mu = cadd(mu, make_double2(1e-3 * scale, 0.0));  // exceptional shift
+    for (int i = 0; i < m; ++i) A[i][i] = csub(A[i][i], mu);
+    // QR by modified Gram-Schmidt on the columns of the active block
+    for (int j = 0; j < m; ++j) {
+      for (int i = 0; i < m; ++i) Q[i][j] = A[i][j];
+      for (int p = 0; p < j; ++p) {
+        double2 r = make_double2(0.0, 0.0);
+        for (int i = 0; i < m; ++i) r = cadd(r, cmulc(Q[i][p], Q[i][j]));
+        R[p][j] = r;
+        for (int i = 0; i < m; ++i) Q[i][j] = csub(Q[i][j], cmul(r, Q[i][p]));
+      }
+      double nr = 0.0;
+      for (int i = 0; i < m; ++i) nr += cabs2(Q[i][j]);
+      nr = sqrt(nr);
+      R[j][j] = make_double2(nr, 0.0);
+      for (int i = 0; i < m; ++i) Q[i][j] = nr > 0 ? cscale(Q[i][j], 1.0 / nr) : make_double2(i == j ? 1.0 : 0.0, 0.0);
+      for (int p = j + 1; p < m; ++p) R[p][j] = make_double2(0.0, 0.0);
+    }
+    // A = R Q + mu I (the rest of the matrix keeps its already-deflated rows)
+    double2 RQ[SMALLK][SMALLK];
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int p = i; p < m; ++p) s = cadd(s, cmul(R[i][p], Q[p][j]));
+        RQ[i][j] = s;
+      }
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) A[i][j] = i == j ? cadd(RQ[i][j], mu) : RQ[i][j];
+  }
+  if (m > 0) {
+    *status = CARC_NOT_CONVERGED;
+    for (int i = 0; i < m; ++i) ev[i] = A[i][i];
+  }
+  int best = 0;
+  for (int i = 1; i < k; ++i)
+    if (ev[i].x < ev[best].x) best = i;
+  const double2 lam = ev[best];
+  // null vector of (A0 - lam I) by Gaussian elimination with full pivoting
+  double2 B[SMALLK][SMALLK];
+  int colp[SMALLK];
+  for (int i = 0; i < k; ++i) {
+    colp[i] = i;
+    for (int j = 0; j < k; ++j) B[i][j] = i == j ? csub(A0[i * k + j], lam) : A0[i * k + j];
+  }
+  for (int p = 0; p < k - 1; ++p) {
+    int bi = p, bj = p;
+    double bv = -1.0;
+    for (int i = p; i < k; ++i)
+      for (int j = p; j < k; ++j)
+        if (cabs2(B[i][j]) > bv) {
+          bv = cabs2(B[i][j]);
+          bi = i;
+          bj = j;
+        }
+    for (int j = 0; j < k; ++j) {
+      double2 t = B[p][j];
+      B[p][j] = B[bi][j];
+      B[bi][j] = t;
+    }
+    for (int i = 0; i < k; ++i) {
+      double2 t = B[i][p];
+      B[i][p] = B[i][bj];
+      B[i][bj] = t;
+    }
+    int t = colp[p];
+    colp[p] = colp[bj];
+    colp[bj] = t;
+    if (bv <= 0.0) continue;
+    for (int i = p + 1; i < k; ++i) {
+      double2 f = cdiv(B[i][p], B[p][p]);
+      for (int j = p; j < k; ++j) B[i][j] = csub(B[i][j], cmul(f, B[p][j]));
+    }
+  }
+  double2 y[SMALLK];
+  y[k - 1] = make_double2(1.0, 0.0);
+  for (int i = k - 2; i >= 0; --i) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int j = i + 1; j < k; ++j) s = cadd(s, cmul(B[i][j], y[j]));
+    y[i] = cabs2(B[i][i]) > 0 ? cscale(cdiv(s, B[i][i]), -1.0) : make_double2(0.0, 0.0);
+  }
+  double nr = 0.0;
+  for (int i = 0; i < k; ++i) nr += cabs2(y[i]);
+  nr = sqrt(nr);
+  for (int i = 0; i < k; ++i) vec_out[colp[i]] = cscale(y[i], 1.0 / nr);
+  *lam_out = lam;
+}
+
+struct RelaxWs {
+  double2 *M, *K, *MK, *h, *small, *lam, *vec, *x, *tmp, *scal;
+  int* status;
+  void* dot_ws;
+  int64_t dot_ws_bytes;
+};
+
+int64_t relax_layout(int n, int k, RelaxWs* R, void* base) {
+  char* p = static_cast<char*>(base);
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) {
+    void* r = p ? p + off : nullptr;
+    off += a256(bytes);
+    return r;
+  };
+  RelaxWs t;
+  t.M = (double2*)take((int64_t)n * n * 16);
+  t.K = (double2*)take((int64_t)k * n * 16);
+  t.MK = (double2*)take((int64_t)k * n * 16);
+  t.h = (double2*)take((int64_t)k * 16);
+  t.small = (double2*)take((int64_t)k * k * 16);
+  t.lam = (double2*)take(16);
+  t.vec = (double2*)take((int64_t)k * 16);
+  t.x = (double2*)take((int64_t)n * 16);
+  t.tmp = (double2*)take((int64_t)n * 16);
+  t.scal = (double2*)take(4 * 16);
+  t.status = (int*)take(16);
+  t.dot_ws_bytes = dot_workspace_size(n);
+  t.dot_ws = take(t.dot_ws_bytes);
+  if (R) *R = t;
+  return off;
+}
+
+__global__ void copy_column_kernel(int k, const double2* __restrict__ h, double2* __restrict__ small, int col) {
+  for (int i = threadIdx.x; i < k; i += blockDim.x) small[i * k + col] = h[i];
+}
+
+}  // namespace
+
+int64_t relax_workspace_size(int n, int k) {
+  int64_t mat = a256((int64_t)n * n * 16);
+  carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
+  int64_t g = std::max<int64_t>(gett_workspace_size(d, 1), 0);
+  return relax_layout(n, k, nullptr, nullptr) + 3 * mat + a256(64) +
+         std::max({potrf_workspace_size(n), trtri_workspace_size(n), a256(g)});
+}
+
+int relax_over(int n, const void* Hv, const void* Nv, const void* x0, void* x_out, int k, int max_mults, double tol,
+               double2* eigenvalue, int* mults_out, double2* values_out, void* ws, int64_t ws_bytes,
+               cudaStream_t stream) {
+  if (n < 1 || k < 1 || k > SMALLK) return fail(CARC_BAD_ARG, "relaxOver: n=%d, krylov dimension %d (1..%d)", n, k, SMALLK);
+  if (ws_bytes < relax_workspace_size(n, k)) return fail(CARC_BAD_ARG, "relaxOver: workspace too small");
+  RelaxWs W;
+  int64_t used = relax_layout(n, k, &W, ws);
+  char* p = static_cast<char*>(ws) + used;
+  int64_t mat = a256((int64_t)n * n * 16);
+  double2* Lm = (double2*)p;
+  double2* Li = (double2*)(p + mat);
+  double2* T1 = (double2*)(p + 2 * mat);
+  int* st = (int*)(p + 3 * mat);
+  void* sub = p + 3 * mat + a256(64);
+  int64_t sub_bytes = ws_bytes - used - 3 * mat - a256(64);
+  const int eb = blocks_for(n);
+  const int gb = blocks_for((int64_t)n * 32);
+  int32_t e[3] = {0, 0, 0};
+  // M = N^{-1} H  (or H when N is absent)
+  if (Nv) {
+    CARC_CHECK_CUDA(cudaMemcpyAsync(Lm, Nv, (int64_t)n * n * 16, cudaMemcpyDeviceToDevice, stream));
+    CARC_RETURN_IF(potrf(n, Lm, st, sub, sub_bytes, stream));
+    int hs = 0;
+    CARC_CHECK_CUDA(cudaMemcpyAsync(&hs, st, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+    if (hs != CARC_OK) return fail(CARC_NOT_POSDEF, "relaxOver: the normalization matrix is not positive definite");
+    CARC_RETURN_IF(trtri_lower(n, Lm, Li, sub, sub_bytes, stream));
+    carc_contract_desc d1 = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;  // T1 = Li H
+    const void* a1[1] = {Li};
+    const void* b1[1] = {Hv};
+    void* c1[1] = {T1};
+    CARC_RETURN_IF(gett_launch(d1, a1, 1, b1, 1, c1, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+    carc_contract_desc d2 = DescBuilder().m(n, 1, n).n(n, 1, 1).k(n, n, n).d;  // M[i][j] = sum_r conj(Li[r][i]) T1[r][j]
+    d2.conj_a = 1;
+    const void* a2[1] = {Li};
+    const void* b2[1] = {T1};
+    void* c2[1] = {W.M};
+    CARC_RETURN_IF(gett_launch(d2, a2, 1, b2, 1, c2, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+  } else {
+    CARC_CHECK_CUDA(cudaMemcpyAsync(W.M, Hv, (int64_t)n * n * 16, cudaMemcpyDeviceToDevice, stream));
+  }
+  CARC_CHECK_CUDA(cudaMemsetAsync(W.status, 0, sizeof(int), stream));
+  // x = x0 / |x0| ; initial value x^H M x
+  CARC_CHECK_CUDA(cudaMemcpyAsync(W.x, x0, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+  CARC_RETURN_IF(dot_launch(n, W.x, W.x, 1, W.scal, W.dot_ws, W.dot_ws_bytes, stream));
+  scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.scal, W.x);
+  CARC_CHECK_LAUNCH();
+  gemv_kernel<<<gb, 256, 0, stream>>>(n, W.M, W.x, W.tmp);
+  CARC_CHECK_LAUNCH();
+  CARC_RETURN_IF(dot_launch(n, W.x, W.tmp, 1, W.scal + 1, W.dot_ws, W.dot_ws_bytes, stream));
+  double2 initial_value;
+  CARC_CHECK_CUDA(cudaMemcpyAsync(&initial_value, W.scal + 1, 16, cudaMemcpyDeviceToHost, stream));
+  int mults = 0;
+  bool have_last = false;
+  double2 last = make_double2(0, 0);
+  bool complete = (k == n);
+  const int max_restarts = 100000;
+  for (int restart = 0; restart < max_restarts; ++restart) {
+    int kk = k;
+    CARC_CHECK_CUDA(cudaMemcpyAsync(W.K, W.x, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+    for (int i = 0; i < k; ++i) {
+      gemv_kernel<<<gb, 256, 0, stream>>>(n, W.M, W.K + (int64_t)i * n, W.MK + (int64_t)i * n);
+      CARC_CHECK_LAUNCH();
+      if (i < k - 1) {
+        // K[i+1] = MK[i] - (K[:i+1]^H MK[i]) K[:i+1]   (single classical Gram-Schmidt pass, utils.py:852)
+        proj_kernel<<<blocks_for((int64_t)(i + 1) * 32), 256, 0, stream>>>(n, i + 1, W.K, W.MK + (int64_t)i * n, W.h);
+        CARC_CHECK_LAUNCH();
+        CARC_CHECK_CUDA(cudaMemcpyAsync(W.K + (int64_t)(i + 1) * n, W.MK + (int64_t)i * n, (int64_t)n * 16,
+                                        cudaMemcpyDeviceToDevice, stream));
+        combine_kernel<<<eb, 256, 0, stream>>>(n, i + 1, W.K, W.h, -1.0, W.K + (int64_t)(i + 1) * n, 0);
+        CARC_CHECK_LAUNCH();
+        CARC_RETURN_IF(dot_launch(n, W.K + (int64_t)(i + 1) * n, W.K + (int64_t)(i + 1) * n, 1, W.scal + 2,
+                                  W.dot_ws, W.dot_ws_bytes, stream));
+        double2 nr2;
+        CARC_CHECK_CUDA(cudaMemcpyAsync(&nr2, W.scal + 2, 16, cudaMemcpyDeviceToHost, stream));
+        CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+        if (sqrt(std::max(nr2.x, 0.0)) <= 1e-14) {
+          complete = true;
+          kk = i + 1;
+          break;
+        }
+        scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.scal + 2, W.K + (int64_t)(i + 1) * n);
+        CARC_CHECK_LAUNCH();
+      }
+    }
+    mults += k;
+    // small[a][b] = K[a]^H MK[b]
+    for (int b = 0; b < kk; ++b) {
+      proj_kernel<<<blocks_for((int64_t)kk * 32), 256, 0, stream>>>(n, kk, W.K, W.MK + (int64_t)b * n, W.h);
+      CARC_CHECK_LAUNCH();
+      copy_column_kernel<<<1, 32, 0, stream>>>(kk, W.h, W.small, b);
+      CARC_CHECK_LAUNCH();
+    }
+    small_eig_min_real_kernel<<<1, 1, 0, stream>>>(kk, W.small, W.lam, W.vec, W.status);
+    CARC_CHECK_LAUNCH();
+    double2 lam;
+    int sst = 0;
+    CARC_CHECK_CUDA(cudaMemcpyAsync(&lam, W.lam, 16, cudaMemcpyDeviceToHost, stream));
+    CARC_CHECK_CUDA(cudaMemcpyAsync(&sst, W.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+    if (sst != 0) return fail(CARC_NOT_CONVERGED, "relaxOver: projected eigenproblem did not converge");
+    // x = vec . K, normalized
+    combine_kernel<<<eb, 256, 0, stream>>>(n, kk, W.K, W.vec, 1.0, W.x, 1);
+    CARC_CHECK_LAUNCH();
+    CARC_RETURN_IF(dot_launch(n, W.x, W.x, 1, W.scal, W.dot_ws, W.dot_ws_bytes, stream));
+    scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.scal, W.x);
+    CARC_CHECK_LAUNCH();
+    const bool changed_little = have_last && sqrt(cabs2(csub(last, lam))) <= tol;
+    if (complete || changed_little || (max_mults > 0 && mults >= max_mults)) {
+      gemv_kernel<<<gb, 256, 0, stream>>>(n, W.M, W.x, W.tmp);
+      CARC_CHECK_LAUNCH();
+      CARC_RETURN_IF(dot_launch(n, W.x, W.tmp, 1, W.scal + 1, W.dot_ws, W.dot_ws_bytes, stream));
+      double2 final_value;
+      CARC_CHECK_CUDA(cudaMemcpyAsync(&final_value, W.scal + 1, 16, cudaMemcpyDeviceToHost, stream));
+      CARC_CHECK_CUDA(cudaMemcpyAsync(x_out, W.x, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+      CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+      if (eigenvalue) *eigenvalue = lam;
+      if (mults_out) *mults_out = mults;
+      if (values_out) {
+        values_out[0] = initial_value;
+        values_out[1] = final_value;
+      }
+      // RelaxFailed test of utils.py:871-872 (real part of the complex ratio, as numpy compares)
+      double2 diff = csub(final_value, initial_value);
+      double den = sqrt(cabs2(final_value)) + sqrt(cabs2(initial_value));
+      if (den > 0 && diff.x / den > 1 + 1e-7) return fail(CARC_RELAX_FAILED, "relaxOver: value rose");
+      return CARC_OK;
+    }
+    last = lam;
+    have_last = true;
+  }
+  return fail(CARC_NOT_CONVERGED, "relaxOver: restart budget spent");
+}
+
+}  // namespace carc

@@ -1,0 +1,87 @@
+"""Seeded synthetic center-site problems with the shapes of the benchmark configs.
+
+The tag structure of a grown boundary is obtained by running the product's
+own schedules on tags alone (no data), e.g. one absorption round 0,1,2,3 of
+the transverse-field Ising operator gives corners with 4 tags and sides with
+5 tags, i.e. 9 stage-3 terms.  Tensor entries are i.i.d. N(0,1) from
+``numpy.random.default_rng(seed)``, each tensor scaled to unit Frobenius norm.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .sparse import (Identity, OneSiteOperator, TwoSiteOperator, compileSparseSchedule)
+from .utils import L, R
+
+X = np.array([[0, 1], [1, 0]], np.complex128)
+Y = np.array([[0, -1j], [1j, 0]], np.complex128)
+Z = np.array([[1, 0], [0, -1]], np.complex128)
+
+
+def ti_operator_arrays(h=3.0, J=1.0):
+    """Transverse-field Ising center: O=-h Z, OO_UD=OO_LR=(X, -J X)
+    (the convention of makeSimpleSparseOperator, sparse.py:288-294)."""
+    return [
+        (OneSiteOperator(None), -h * Z),
+        (TwoSiteOperator(0, 3, 0), X.copy()),
+        (TwoSiteOperator(0, 1, 0), -J * X),
+        (TwoSiteOperator(0, 0, 0), X.copy()),
+        (TwoSiteOperator(0, 2, 0), -J * X),
+        (Identity(), np.eye(2, dtype=np.complex128)),
+    ]
+
+
+def heisenberg_operator_arrays(J=1.0):
+    """XXX antiferromagnet with spin-1/2 factor 1/4: makeSparseOperator(OO_UDs=[(X,X),(Y,Y),(Z,Z)]*J/4, same LR)."""
+    out = []
+    pairs = [(X, X), (Y, Y), (Z, Z)]
+    for i, (a, b) in enumerate(pairs):
+        out.append((TwoSiteOperator(i, 3, 0), a.copy()))
+        out.append((TwoSiteOperator(i, 1, 0), 0.25 * J * b))
+    for i, (a, b) in enumerate(pairs):
+        out.append((TwoSiteOperator(i, 0, 0), a.copy()))
+        out.append((TwoSiteOperator(i, 2, 0), 0.25 * J * b))
+    out.append((Identity(), np.eye(2, dtype=np.complex128)))
+    return out
+
+
+def simulate_tags(op_tags, directions):
+    """Tag lists of corners and sides after absorbing towards each direction."""
+    from .tensors._2d import sparse as tsp
+    corners = [[Identity()] for _ in range(4)]
+    sides = [[Identity()] for _ in range(4)]
+    for d in directions:
+        corners[d] = compileSparseSchedule(tsp.RULES["absL"](), corners[d], sides[L(d)]).result_tags
+        sides[d] = compileSparseSchedule(tsp._center_rules(d), sides[d], list(op_tags)).result_tags
+        corners[R(d)] = compileSparseSchedule(tsp.RULES["absR"](), corners[R(d)], sides[R(d)]).result_tags
+    return corners, sides
+
+
+def random_unit(rng, shape, complex_=False):
+    a = rng.standard_normal(shape)
+    if complex_:
+        a = a + 1j * rng.standard_normal(shape)
+    a = a.astype(np.complex128)
+    return a / np.linalg.norm(a)
+
+
+def matvec_problem_arrays(D=4, c_ket=8, c_bra=4, seed=1, op_arrays=None, rounds=1):
+    """Host arrays of the stage-3 microbenchmark: corners (c,c',1,c,c',1) and
+    sides (c,c',1,c,c',1,D,D) per tag, chi = c*c' merged boundary dimension."""
+    rng = np.random.default_rng(seed)
+    op_arrays = ti_operator_arrays() if op_arrays is None else op_arrays
+    op_tags = [t for t, _ in op_arrays]
+    corners_t, sides_t = simulate_tags(op_tags, list(range(4)) * rounds)
+    cshape = (c_ket, c_bra, 1, c_ket, c_bra, 1)
+    sshape = cshape + (D, D)
+    corners = [[(t, random_unit(rng, cshape)) for t in ct] for ct in corners_t]
+    sides = [[(t, random_unit(rng, sshape)) for t in st] for st in sides_t]
+    return corners, sides, op_arrays
+
+
+def to_device(corners, sides, op_arrays):
+    from .data import TorchData
+    c = [{t: TorchData(a) for t, a in lst} for lst in corners]
+    s = [{t: TorchData(a) for t, a in lst} for lst in sides]
+    o = {t: TorchData(a) for t, a in op_arrays}
+    return c, s, o

@@ -1,0 +1,230 @@
+/*
+ * carcassonne_gb300 -- C ABI of the GB300 (sm_103a) center-site path.
+ *
+ * Every entry point takes plain device pointers and sizes, returns an int
+ * status (CARC_OK on success), never throws, and enqueues its work on the
+ * given cudaStream_t (passed as void*).  Device buffers belong to the caller;
+ * the library never frees them.  The message of the last failure on the
+ * calling thread is returned by carc_last_error_string().
+ *
+ * Complex data is complex128 stored as interleaved (re, im) doubles, the
+ * layout of numpy/torch complex128 tensors, in C (row-major) order.
+ *
+ * Each declaration names the reference interface (gcross/Carcassonne, path
+ * within that project) whose arithmetic it carries out.
+ */
+#ifndef CARCASSONNE_GB300_H
+#define CARCASSONNE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum carc_status_code {
+  CARC_OK = 0,
+  CARC_BAD_SHAPE = 1,      /* DimensionMismatchError / UnexpectedTensorRankError (utils.py:13-41) */
+  CARC_BAD_ARG = 2,        /* ValueError */
+  CARC_CUDA_ERROR = 3,
+  CARC_NOT_CONVERGED = 4,  /* iteration budget spent (gmres info != 0 in compression.py:43) */
+  CARC_NAN = 5,            /* checkForNaNsIn / assertHasNoNaNs (utils.py:250-253) */
+  CARC_NOT_POSDEF = 6,     /* normalization matrix not positive definite */
+  CARC_TOO_LARGE = 7,      /* request exceeds a documented fixed limit */
+  CARC_RELAX_FAILED = 8    /* RelaxFailed: the Rayleigh value rose (utils.py:871-872) */
+};
+
+#define CARC_MAX_SUBDIMS 6   /* index groups per contraction operand side */
+#define CARC_MAX_SLOTS 64    /* tags per sparse boundary in one grouped call */
+#define CARC_MAX_ENTRIES 512 /* tag pairs in one grouped call */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* carc_last_error_string(void);
+/* Library version (major*10000 + minor*100 + patch). */
+int carc_version(void);
+/* Kernels launched by this library so far, over all threads (a monotone
+ * counter for instrumentation; no counterpart in the reference). */
+int64_t carc_launch_counter(void);
+
+/*
+ * A strided complex contraction  C[m; n] (+)= alpha * sum_k op(A)[m; k] op(B)[k; n]
+ * where m, n and k are multi-indices (outermost first) with arbitrary
+ * element strides into A, B and C.  nm/nn/nk may be 0 (then that extent is 1).
+ * conj_a / conj_b conjugate the operand on load.
+ */
+typedef struct carc_contract_desc {
+  int32_t nm, nn, nk;
+  int32_t conj_a, conj_b;
+  int64_t m_ext[CARC_MAX_SUBDIMS];
+  int64_t n_ext[CARC_MAX_SUBDIMS];
+  int64_t k_ext[CARC_MAX_SUBDIMS];
+  int64_t a_m[CARC_MAX_SUBDIMS];
+  int64_t a_k[CARC_MAX_SUBDIMS];
+  int64_t b_n[CARC_MAX_SUBDIMS];
+  int64_t b_k[CARC_MAX_SUBDIMS];
+  int64_t c_m[CARC_MAX_SUBDIMS];
+  int64_t c_n[CARC_MAX_SUBDIMS];
+} carc_contract_desc;
+
+/*
+ * Grouped contraction over a tag-pair table: for every output slot c,
+ * C[c] = alpha * sum over entries e with entries[3e+2]==c, in table order, of
+ * A[entries[3e]] . B[entries[3e+1]]   (+ the old C[c] when accumulate != 0).
+ * a_ptrs/b_ptrs/c_ptrs and entries are HOST arrays (device pointers inside).
+ * Replaces: sparse.contractSparseTensors (sparse.py:223-240) driving the dense
+ * contractors, and NDArrayData.contractWith (data/__init__.py:157-159).
+ * workspace: device scratch of carc_zcontract_workspace_size() bytes (may be
+ * NULL when that size is 0).
+ */
+int carc_zcontract_grouped(const carc_contract_desc* desc,
+                           const void* const* a_ptrs, int32_t n_a,
+                           const void* const* b_ptrs, int32_t n_b,
+                           void* const* c_ptrs, int32_t n_c,
+                           const int32_t* entries, int32_t n_entries,
+                           double alpha_re, double alpha_im, int32_t accumulate,
+                           void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zcontract_workspace_size(const carc_contract_desc* desc, int32_t n_c);
+
+/*
+ * out = permutation/reshape of in: out is C-contiguous with shape out_shape;
+ * element out[i0..i_{n-1}] = in[sum_j i_j * in_strides[j]] (conjugated if conj).
+ * Replaces NDArrayData.join / transpose / conj (data/__init__.py:247-256, :151-153).
+ */
+int carc_zpermute(const void* in, void* out, int32_t ndim, const int64_t* out_shape,
+                  const int64_t* in_strides, int32_t conj, void* stream);
+
+/* out = a*x + b*y over n complex elements (x or y may be NULL when its
+ * coefficient is 0).  Replaces NDArrayData.__add__/__sub__/__iadd__/__mul__(scalar)
+ * (data/__init__.py:91-140). */
+int carc_zaxpby(int64_t n, double a_re, double a_im, const void* x,
+                double b_re, double b_im, const void* y, void* out, void* stream);
+/* out = x * y (elementwise).  Replaces NDArrayData.__mul__/__imul__ with data. */
+int carc_zmul(int64_t n, const void* x, const void* y, void* out, void* stream);
+/* out[i] = value. */
+int carc_zfill(int64_t n, double re, double im, void* out, void* stream);
+/* out (device complex128 scalar) = sum_i op(x_i) y_i, op = conj if conj_x.
+ * Warp-shuffle tree reduction in a fixed order (deterministic).
+ * Replaces contractWith over all axes (system/_2d.py:429-430) and norm(). */
+int carc_zdot(int64_t n, const void* x, const void* y, int32_t conj_x, void* out,
+              void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zdot_workspace_size(int64_t n);
+/* *flag (device int32) = 1 if any element of x is NaN, else 0.  Replaces hasNaN
+ * (data/__init__.py:209-211). */
+int carc_zhasnan(int64_t n, const void* x, void* flag, void* stream);
+
+/*
+ * Stage-3 operator application (the center-site matvec) in FP64:
+ *   y[v] = sum_t S2_0[i0_t] (x) S2_1[i1_t] (x) O[io_t] . x[v]     (+ y if accumulate)
+ * S2_0 tags have shape s0_shape = (x0,x1,k0,k1,l0,l1), S2_1 tags have
+ * s1_shape = (x1,x0,k2,k3,l2,l3); the operator tags are (d,d); io_t < 0 means
+ * the identity (formNormalizationStage3).  x and y hold nvec centers of shape
+ * (k0,k1,k2,k3,d) / (l0,l1,l2,l3,d), contiguous one after the other.
+ * terms: HOST int32 [n_terms][3] = (i0, i1, io).
+ * Replaces formDenseStage3 multiply (tensors/_2d/dense.py:145-174),
+ * formNormalizationStage3 multiply (:114-144) and the term sum of
+ * formExpectationStage3 (tensors/_2d/sparse.py:129-133).
+ */
+int carc_stage3_matvec_f64(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                           const void* const* s0_ptrs, int32_t n0,
+                           const void* const* s1_ptrs, int32_t n1,
+                           const void* const* op_ptrs, int32_t nop,
+                           const int32_t* terms, int32_t n_terms,
+                           const void* x, void* y, int32_t nvec, int32_t accumulate,
+                           void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_stage3_matvec_f64_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape,
+                                              int64_t d, int32_t n_terms, int32_t nvec);
+
+/*
+ * Dense stage-3 matrix H[(l,p),(k,q)] = sum_t G_t[l,k] O_t[p,q] with
+ * G_t = sum_x S2_0[i0_t] S2_1[i1_t] (formDenseStage3_formMatrix,
+ * tensors/_2d/dense.py:175-195; formNormalizationSubmatrix :204-225 when d=1
+ * and all io_t < 0; formExpectationMatrix tensors/_2d/sparse.py:144-148).
+ * H is (N,N) row-major, N = l0*l1*l2*l3*d, overwritten (or accumulated).
+ */
+int carc_stage3_form_matrix_f64(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                                const void* const* s0_ptrs, int32_t n0,
+                                const void* const* s1_ptrs, int32_t n1,
+                                const void* const* op_ptrs, int32_t nop,
+                                const int32_t* terms, int32_t n_terms,
+                                void* H, int32_t accumulate,
+                                void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_stage3_form_matrix_f64_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape,
+                                                   int64_t d, int32_t n_terms);
+
+/*
+ * Batched one-sided Jacobi SVD, FP64 complex: A (batch x m x n, m >= n,
+ * row-major) = U diag(S) Vh with U (m x n), S (n, descending), Vh (n x n).
+ * *status (device int32) = CARC_NOT_CONVERGED if a sweep budget ran out.
+ * Replaces NDArrayData.svd (data/__init__.py:344-346, scipy.linalg.svd).
+ */
+int carc_zgesvd_jacobi(int32_t m, int32_t n, int32_t batch, const void* A, void* U, void* S, void* Vh,
+                       void* status, void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zgesvd_jacobi_workspace_size(int32_t m, int32_t n, int32_t batch);
+
+/*
+ * The normalizer / denormalizer of NDArrayData.normalizeAxis
+ * (data/__init__.py:282-301) from S (n) and Vh (n x n):
+ *   sqrt_svals == 0: out_a = Vh^T (Vh * SI)^*,  out_b = Vh^H (Vh * S)
+ *   sqrt_svals != 0: out_a = (Vh * sqrt(SI))^*, out_b = Vh * sqrt(S)
+ * with SI = 1/S where |S| > dont_recip_under (always when it is <= 0).
+ */
+int carc_normalize_axis_finish(int32_t n, const void* S, const void* Vh, double dont_recip_under,
+                               int32_t sqrt_svals, void* out_a, void* out_b, void* stream);
+
+/*
+ * Batched Hermitian eigensolver (parallel cyclic Jacobi), n <= 512:
+ * A = V diag(W) V^H, W ascending.  Replaces scipy.linalg.eigh in
+ * computeCompressor (utils.py:268-302).
+ */
+int carc_zheev_jacobi(int32_t n, int32_t batch, const void* A, void* W, void* V, void* status,
+                      void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zheev_jacobi_workspace_size(int32_t n, int32_t batch);
+
+/* In-place blocked Cholesky A = L L^H (lower; strict upper zeroed);
+ * *status = CARC_NOT_POSDEF when a pivot is not positive.  Replaces the LU
+ * factorisation of the normalization matrix in relaxOver (utils.py:816-817). */
+int carc_zpotrf(int32_t n, void* A, void* status, void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zpotrf_workspace_size(int32_t n);
+/* X = L^{-1} for lower-triangular L (blocked forward substitution). */
+int carc_ztrtri_lower(int32_t n, const void* L, void* X, void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_ztrtri_lower_workspace_size(int32_t n);
+
+/*
+ * Lowest eigenpair of H x = l N x (H Hermitian, N Hermitian positive
+ * definite, both n x n): Cholesky of N, C = L^-1 H L^-H, restarted Lanczos
+ * with full reorthogonalisation from u0 = L^H x0 (x0 may be NULL), stopping
+ * when |beta_m s_m| <= tol |l|; x is N-normalized (x^H N x = 1).
+ * *eigenvalue and *iterations are HOST pointers.  The call synchronizes the
+ * stream at its convergence checkpoints.  Replaces
+ * minimizeExpectationUsingFullEigensolver (system/_2d.py:498-502) and the
+ * solve of minimizeExpectation (:489-497).
+ */
+int carc_zhegv_lowest(int32_t n, const void* H, const void* N, const void* x0, void* x, double* eigenvalue,
+                      int32_t max_krylov, int32_t max_restarts, double tol, int32_t* iterations,
+                      void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zhegv_lowest_workspace_size(int32_t n, int32_t max_krylov);
+/* The Lanczos part alone, for a dense Hermitian C. */
+int carc_zheev_lowest_lanczos(int32_t n, const void* C, const void* u0, void* u, double* eigenvalue,
+                              int32_t max_krylov, int32_t max_restarts, double tol, int32_t* iterations,
+                              void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zheev_lowest_lanczos_workspace_size(int32_t n, int32_t max_krylov);
+
+/*
+ * relaxOver (utils.py:805-878): restarted Krylov / Rayleigh-Ritz on
+ * M = N^{-1} H (N may be NULL for the standard problem) with dimension k
+ * (1..8), stopping when the lowest Ritz value moves by <= tol, the space is
+ * complete, or max_mults multiplications were spent (<= 0: no budget).
+ * x0/x are device vectors of n; *eigenvalue (the last Ritz value),
+ * *mults and values[2] = (initial, final Rayleigh values) are HOST outputs.
+ * Returns CARC_RELAX_FAILED where the reference raises RelaxFailed.
+ */
+int carc_relax_over(int32_t n, const void* H, const void* N, const void* x0, void* x, int32_t k,
+                    int32_t max_mults, double tol, double* eigenvalue, int32_t* mults, double* values,
+                    void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_relax_over_workspace_size(int32_t n, int32_t k);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CARCASSONNE_GB300_H */
