@@ -124,13 +124,20 @@ __global__ void tridiag_lowest_kernel(int m, const double* __restrict__ alpha, c
     if (hi - lo <= 1e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300 * span) break;
   }
   const double lam = 0.5 * (lo + hi);
+  if (m == 1) {
+    s[0] = 1.0;
+    out[0] = alpha[0];
+    out[1] = fabs(beta[0]);
+    return;
+  }
+  const double scale = fmax(fmax(fabs(lo), fabs(hi)), span);
   // inverse iteration with partial pivoting on T - (lam - delta) I
   double* dl = scratch;          // sub
   double* dd = scratch + MAXM;   // diag
   double* du = scratch + 2 * MAXM;  // super
   double* du2 = scratch + 3 * MAXM;  // second super (fill-in)
   double* x = s;
-  const double shift = lam - 1e-12 * span;
+  const double shift = lam - 1e-10 * scale;
   for (int i = 0; i < m; ++i) x[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (i % 7));
   int piv[MAXM];
   for (int iter = 0; iter < 3; ++iter) {
@@ -175,11 +182,20 @@ __global__ void tridiag_lowest_kernel(int m, const double* __restrict__ alpha, c
       double v = x[i];
       if (i + 1 < m) v -= du[i] * x[i + 1];
       if (i + 2 < m) v -= du2[i] * x[i + 2];
-      double d = dd[i] != 0.0 ? dd[i] : 1e-300;
+      double d = dd[i] != 0.0 ? dd[i] : 1e-300 * scale;
       x[i] = v / d;
     }
+    double mx = 0.0;
+    for (int i = 0; i < m; ++i) mx = fmax(mx, fabs(x[i]));
+    if (!(mx > 0.0) || isinf(mx)) {
+      for (int i = 0; i < m; ++i) x[i] = (i == 0) ? 1.0 : 0.0;
+      mx = 1.0;
+    }
     double nrm = 0.0;
-    for (int i = 0; i < m; ++i) nrm += x[i] * x[i];
+    for (int i = 0; i < m; ++i) {
+      x[i] /= mx;
+      nrm += x[i] * x[i];
+    }
     nrm = sqrt(nrm);
     for (int i = 0; i < m; ++i) x[i] /= nrm;
   }

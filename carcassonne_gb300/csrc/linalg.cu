@@ -126,7 +126,7 @@ __global__ void svd_finish_kernel(int m, int n, const double2* __restrict__ Wall
       int best = a;
       for (int b = a + 1; b < n; ++b)
         if (S[perm[b]] > S[perm[best]]) best = b;
-      int t = perm[a];
+      int t = perm[best];
       for (int b = best; b > a; --b) perm[b] = perm[b - 1];
       perm[a] = t;
     }
@@ -286,7 +286,7 @@ __global__ void heev_finish_kernel(int n, const double2* __restrict__ Aall, cons
       int best = a;
       for (int b = a + 1; b < n; ++b)
         if (A[perm[b] * n + perm[b]].x < A[perm[best] * n + perm[best]].x) best = b;
-      int t = perm[a];
+      int t = perm[best];
       for (int b = best; b > a; --b) perm[b] = perm[b - 1];
       perm[a] = t;
     }

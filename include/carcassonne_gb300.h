@@ -134,6 +134,7 @@ int carc_stage3_matvec_f64(const int64_t* s0_shape, const int64_t* s1_shape, int
 int64_t carc_stage3_matvec_f64_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape,
                                               int64_t d, int32_t n_terms, int32_t nvec);
 
+
 /*
  * Dense stage-3 matrix H[(l,p),(k,q)] = sum_t G_t[l,k] O_t[p,q] with
  * G_t = sum_x S2_0[i0_t] S2_1[i1_t] (formDenseStage3_formMatrix,

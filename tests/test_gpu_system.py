@@ -1,0 +1,243 @@
+"""GPU System: the reference's known-answer tests (tests/test_system.py),
+trajectory parity against the golden run of the reference, and invariance
+of expectations under gauge changes and compression."""
+import json
+import os
+import random
+
+import numpy as np
+import pytest
+import torch
+
+from tests.product_tags import parse
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def env():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from carcassonne_gb300.data import TorchData
+    from carcassonne_gb300.system import System, sideFromCorner
+    from carcassonne_gb300 import sparse
+    return TorchData, System, sideFromCorner, sparse
+
+
+def rel(a, b):
+    a = a.toArray() if hasattr(a, "toArray") else np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+# -- known answers (tests/test_system.py:308-440) ---------------------------
+@pytest.mark.parametrize("seed", range(4))
+def test_silly_field_random_walk(env, seed):
+    TorchData, System, _, _ = env
+    rnd = random.Random(seed)
+    system = System.newTrivialWithSimpleSparseOperator(O=TorchData.newIdentity(1))
+    width = height = 1
+    for _ in range(rnd.randint(0, 7)):
+        direction = rnd.randint(0, 3)
+        system.contractTowards(direction)
+        if direction in (0, 2):
+            width += 1
+        else:
+            height += 1
+    assert abs(system.computeExpectation() - width * height) < 1e-12
+    assert abs(system.computeNormalization() - 1) < 1e-12
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_magnetic_field_random_walk(env, seed):
+    TorchData, System, _, _ = env
+    rnd = random.Random(100 + seed)
+    system = System.newTrivialWithSimpleSparseOperator(O=TorchData.Z)
+    states = (TorchData(np.array([[[[[1, 0]]]]], np.complex128)), TorchData(np.array([[[[[0, 1]]]]], np.complex128)))
+    spins = (1, -1)
+    UL = U = UR = Lf = Rf = DL = Dn = DR = 0
+    for _ in range(rnd.randint(1, 8)):
+        direction, spin = rnd.randint(0, 3), rnd.randint(0, 1)
+        system.setStateCenter(states[spin])
+        system.contractTowards(direction)
+        if direction == 0:
+            Rf += spins[spin]; UR += U; DR += Dn
+        elif direction == 1:
+            U += spins[spin]; UL += Lf; UR += Rf
+        elif direction == 2:
+            Lf += spins[spin]; UL += U; DR += Dn
+        else:
+            Dn += spins[spin]; DL += Lf; DR += Rf
+    final = rnd.randint(0, 1)
+    N = UL + U + UR + Lf + Rf + spins[final] + DL + Dn + DR
+    system.setStateCenter(states[final])
+    assert abs(system.computeExpectation() - N) < 1e-12
+    assert abs(system.computeNormalization() - 1) < 1e-12
+    y = system.formExpectationMultiplier()(states[final]).toArray()
+    assert np.abs(y - N * states[final].toArray()).max() < 1e-12
+
+
+def test_form_expectation_matrix_equals_multiplier(env):
+    TorchData, System, _, _ = env
+    random.seed(7)
+    np.random.seed(7)
+    system = System.newRandom()
+    for direction in [0, 1, 3, 2, 0]:
+        system.contractTowards(direction)
+    m = system.formExpectationMultiplier()
+    M = system.formExpectationMatrix().toArray()
+    v = TorchData.newRandom(*system.state_center_data.shape)
+    assert rel(m(v).toArray().ravel(), M @ v.toArray().ravel()) < 1e-11
+    n = system.formNormalizationMultiplier()
+    assert rel(n(v).toArray().ravel(), system.formNormalizationMatrix().toArray() @ v.toArray().ravel()) < 1e-11
+
+
+# -- trajectory parity with the reference's own run -----------------------
+def _system_at(env, traj, rec, name, step):
+    TorchData, System, _, _ = env
+    corners = [{parse(t): TorchData(traj[f"{name}_{step}_corner{i}_{j}"]) for j, t in enumerate(rec["corners"][i])}
+               for i in range(4)]
+    sides = [{parse(t): TorchData(traj[f"{name}_{step}_side{i}_{j}"]) for j, t in enumerate(rec["sides"][i])}
+             for i in range(4)]
+    op_tags = [parse(str(t)) for t in traj[f"{name}_op_tags"]]
+    op = {t: TorchData(traj[f"{name}_op_{k}"]) for k, t in enumerate(op_tags)}
+    return System(corners, sides, TorchData(traj[f"{name}_{step}_state"]), op)
+
+
+@pytest.mark.parametrize("name", ["ti", "heis", "ising_ud"])
+def test_trajectory_energies_and_absorption(env, name):
+    with open(os.path.join(GOLD, "tables.json")) as f:
+        tables = json.load(f)
+    traj = np.load(os.path.join(GOLD, "trajectory.npz"))
+    steps = tables[name]["steps"]
+    for step, direction in enumerate(steps):
+        rec = tables[name]["records"][step]
+        system = _system_at(env, traj, rec, name, step)
+        e_ref, expect_ref, norm_ref = traj[f"{name}_{step}_E"]
+        e, n = system.computeExpectationAndNormalization()
+        assert abs(e - expect_ref) <= 1e-10 * max(1, abs(expect_ref))
+        assert abs(n - norm_ref) <= 1e-10 * max(1, abs(norm_ref))
+        # ground-state energy: 1e-8 relative is the target; FP64 reaches ~1e-12
+        system.minimizeExpectation()
+        lam = system.last_solve["eigenvalue"]
+        assert abs(lam - e_ref.real) <= 1e-10 * max(1.0, abs(e_ref.real)), (step, lam, e_ref)
+        e_min = system.computeExpectation()
+        assert abs(e_min - e_ref.real) <= 1e-10 * max(1.0, abs(e_ref.real))
+        # absorb the reference's minimized center through the GPU gauge (Jacobi SVD)
+        if step + 1 < len(steps):
+            TorchData = env[0]
+            system.setStateCenter(TorchData(traj[f"{name}_{step}_minstate"]))
+            system.contractTowards(direction)
+            assert rel(system.state_center_data, traj[f"{name}_{step}_after_state"]) < 1e-9
+            nxt = tables[name]["records"][step + 1]
+            for i in range(4):
+                assert [repr(t) for t in system.corners[i]] == nxt["corners"][i]
+                assert [repr(t) for t in system.sides[i]] == nxt["sides"][i]
+                for j, t in enumerate(nxt["corners"][i]):
+                    assert rel(system.corners[i][parse(t)], traj[f"{name}_{step + 1}_corner{i}_{j}"]) < 1e-9
+                for j, t in enumerate(nxt["sides"][i]):
+                    assert rel(system.sides[i][parse(t)], traj[f"{name}_{step + 1}_side{i}_{j}"]) < 1e-9
+
+
+def test_relax_solver_reaches_reference_energy(env):
+    with open(os.path.join(GOLD, "tables.json")) as f:
+        tables = json.load(f)
+    traj = np.load(os.path.join(GOLD, "trajectory.npz"))
+    name = "ti"
+    for step in range(len(tables[name]["steps"])):
+        system = _system_at(env, traj, tables[name]["records"][step], name, step)
+        system.solver = "relax"
+        system.minimizeExpectation()
+        ref_relax = traj[f"{name}_{step}_relax"][0].real
+        e = system.computeExpectation().real
+        # same algorithm and stopping rule as the reference's relaxOver
+        assert abs(e - ref_relax) <= 1e-7 * max(1.0, abs(ref_relax)), (step, e, ref_relax)
+
+
+# -- invariances (tests/test_system.py:41-178, :277-306) -------------------
+@pytest.mark.parametrize("corner_id,direction", [(0, 0), (1, 1), (2, 0), (3, 1)])
+def test_compress_corner_state_down_by_half(env, corner_id, direction):
+    TorchData, System, sideFromCorner, sparse = env
+    random.seed(corner_id * 2 + direction)
+    np.random.seed(corner_id * 2 + direction)
+    system = System.newRandom()
+    for i in range(4):
+        system.contractTowards(i)
+    e1, n1 = system.computeExpectationAndNormalization()
+    corner_data = system.corners[corner_id][sparse.Identity()]
+    axis = 3 * direction
+    old = corner_data.shape[axis]
+    new = 2 * (old + 1)
+    enl, enl_c = TorchData.newEnlargener(old, new)
+    system.corners[corner_id] = sparse.mapOverSparseData(
+        lambda d: d.absorbMatrixAt(axis, enl).absorbMatrixAt(axis + 1, enl_c), system.corners[corner_id])
+    side_id = sideFromCorner(corner_id, direction)
+    saxis = 3 - axis
+    system.sides[side_id] = sparse.mapOverSparseData(
+        lambda d: d.absorbMatrixAt(saxis, enl_c).absorbMatrixAt(saxis + 1, enl), system.sides[side_id])
+    e2, n2 = system.computeExpectationAndNormalization()
+    assert abs(n2 / n1 - 1) < 1e-9 and abs(e2 / e1 - 1) < 1e-9
+    system.compressCornerStateTowards(corner_id, direction, old)
+    n3 = system.computeNormalization()
+    e3 = system.computeExpectation()
+    assert abs(n3 / n1 - 1) < 1e-7, (n3, n1)
+    assert abs(e3 / e1 - 1) < 1e-7, (e3, e1)
+
+
+@pytest.mark.parametrize("corner_id,direction,terms", [(0, 0, 3), (1, 1, 2), (2, 1, 4), (3, 0, 0)])
+def test_compress_two_site_operator_new_same_as_old(env, corner_id, direction, terms):
+    TorchData, System, sideFromCorner, sparse = env
+    from carcassonne_gb300.utils import L, R
+    np.random.seed(11 + corner_id)
+    side_id = sideFromCorner(corner_id, direction)
+    ops = [TorchData.newRandomHermitian(2, 2) for _ in range(2)]
+    kw = "OO_LR" if side_id in (1, 3) else "OO_UD"
+    system = System.newTrivialWithSimpleSparseOperator(**{kw: ops})
+    system.contractTowards(R(side_id) if direction == 0 else L(side_id))
+    for _ in range(terms):
+        system.contractTowards(side_id)
+    e1, n1 = system.computeExpectationAndNormalization()
+    system.compressCornerTwoSiteOperatorTowards(corner_id, direction, terms)
+    if terms > 0:
+        assert sparse.TwoSiteOperatorCompressed(direction) in system.corners[corner_id]
+        assert sparse.TwoSiteOperatorCompressed(1 - direction) in system.sides[side_id]
+    e2, n2 = system.computeExpectationAndNormalization()
+    assert abs(n2 - n1) < 1e-9
+    assert abs(e2 - e1) < 1e-9
+
+
+@pytest.mark.parametrize("which", ["center", "corner", "side"])
+def test_gauge_normalizations_keep_expectations(env, which):
+    TorchData, System, _, _ = env
+    random.seed(3)
+    np.random.seed(3)
+    system = System.newRandom()
+    e1, n1 = system.computeExpectationAndNormalization()
+    if which == "center":
+        system.normalizeCenterAndDenormalizeSide(1)
+    elif which == "corner":
+        system.normalizeCornerAndDenormalizeSide(2, 1)
+    else:
+        system.normalizeSideAndDenormalizeCenter(3)
+    system.assertNormalizationIsHermitian()
+    e2, n2 = system.computeExpectationAndNormalization()
+    assert abs(n2 - n1) <= 1e-9 * abs(n1)
+    assert abs(e2 - e1) <= 1e-9 * max(1, abs(e1))
+
+
+def test_center_site_expectation(env):
+    TorchData, System, _, _ = env
+    random.seed(5)
+    np.random.seed(5)
+    O = TorchData.newRandomHermitian(2, 2)
+    system = System.newRandom(O=O)
+    for direction in [0, 3, 1]:
+        system.contractTowards(direction)
+        system.setStateCenter(TorchData.newRandom(*system.state_center_data.shape))
+    s = system.formNormalizationMultiplier()(system.state_center_data)
+    sc = system.state_center_data_conj
+    num = sc.ravel().contractWith(s.absorbMatrixAt(4, O).ravel(), (0,), (0,)).extractScalar()
+    den = sc.ravel().contractWith(s.ravel(), (0,), (0,)).extractScalar()
+    assert abs(system.computeCenterSiteExpectation() - num / den) < 1e-10 * max(1, abs(num / den))
