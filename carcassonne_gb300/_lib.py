@@ -60,6 +60,8 @@ SIGNATURES = {
     "carc_stage3_matvec_f64": (ctypes.c_int, [_pi64, _pi64, _i64, _pvp, _i32, _pvp, _i32, _pvp, _i32, _pi32, _i32,
                                               _vp, _vp, _i32, _i32, _vp, _i64, _vp]),
     "carc_stage3_matvec_f64_workspace_size": (_i64, [_pi64, _pi64, _i64, _i32, _i32]),
+    "carc_stage3_matvec_f64_noalloc": (ctypes.c_int, [_pi64, _pi64, _i64, _pvp, _i32, _pvp, _i32, _pvp, _i32, _pi32,
+                                                      _i32, _vp, _vp, _i32, _i32, _vp]),
     "carc_stage3_form_matrix_f64": (ctypes.c_int, [_pi64, _pi64, _i64, _pvp, _i32, _pvp, _i32, _pvp, _i32, _pi32,
                                                    _i32, _vp, _i32, _vp, _i64, _vp]),
     "carc_stage3_form_matrix_f64_workspace_size": (_i64, [_pi64, _pi64, _i64, _i32]),

@@ -37,6 +37,7 @@ enum carc_status_code {
 #define CARC_MAX_SUBDIMS 6   /* index groups per contraction operand side */
 #define CARC_MAX_SLOTS 64    /* tags per sparse boundary in one grouped call */
 #define CARC_MAX_ENTRIES 512 /* tag pairs in one grouped call */
+#define CARC_NOALLOC_SCRATCH_BYTES (16u << 20) /* fixed scratch of carc_stage3_matvec_f64_noalloc */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* carc_last_error_string(void);
@@ -134,6 +135,27 @@ int carc_stage3_matvec_f64(const int64_t* s0_shape, const int64_t* s1_shape, int
 int64_t carc_stage3_matvec_f64_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape,
                                               int64_t d, int32_t n_terms, int32_t nvec);
 
+/*
+ * carc_stage3_matvec_f64 for callers that cannot allocate device memory while
+ * they run (a host application that owns the whole GPU and forbids library
+ * allocations, or a loop that cannot afford the synchronisation cudaMalloc
+ * may cause) and cannot size a workspace in advance.  It allocates nothing:
+ * its scratch is a fixed CARC_NOALLOC_SCRATCH_BYTES (16 MiB) device array
+ * inside this library, held on every GPU that loads the library until the
+ * process exits.  Problems needing more scratch than that (see
+ * carc_stage3_matvec_f64_workspace_size) are rejected with CARC_TOO_LARGE.
+ * The array's address is looked up on the first call made on each device
+ * (with that device current); make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.  No counterpart in the reference (which
+ * never manages device memory).
+ */
+int carc_stage3_matvec_f64_noalloc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                                   const void* const* s0_ptrs, int32_t n0,
+                                   const void* const* s1_ptrs, int32_t n1,
+                                   const void* const* op_ptrs, int32_t nop,
+                                   const int32_t* terms, int32_t n_terms,
+                                   const void* x, void* y, int32_t nvec, int32_t accumulate, void* stream);
 
 /*
  * Dense stage-3 matrix H[(l,p),(k,q)] = sum_t G_t[l,k] O_t[p,q] with
