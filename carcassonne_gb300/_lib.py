@@ -68,6 +68,7 @@ SIGNATURES = {
     "carc_zgesvd_jacobi": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "carc_zgesvd_jacobi_workspace_size": (_i64, [_i32, _i32, _i32]),
     "carc_normalize_axis_finish": (ctypes.c_int, [_i32, _vp, _vp, _dbl, _i32, _vp, _vp, _vp]),
+    "carc_zgeqr_economic": (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp]),
     "carc_zheev_jacobi": (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "carc_zheev_jacobi_workspace_size": (_i64, [_i32, _i32]),
     "carc_zpotrf": (ctypes.c_int, [_i32, _vp, _vp, _vp, _i64, _vp]),
@@ -83,6 +84,18 @@ SIGNATURES = {
     "carc_relax_over": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _i32, _i32, _dbl, ctypes.POINTER(_dbl),
                                        ctypes.POINTER(_i32), ctypes.POINTER(_dbl), _vp, _i64, _vp]),
     "carc_relax_over_workspace_size": (_i64, [_i32, _i32]),
+    "carc_zcontract_tc": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _vp, _vp, _vp, _dbl, _dbl, _i32, _i32, _vp, _i64,
+                                         _vp, _vp]),
+    "carc_zcontract_tc_workspace_size": (_i64, [ctypes.POINTER(ContractDesc), _i32]),
+    "carc_stage3_tc_plan_size": (_i64, [_pi64, _pi64, _i32, _i32]),
+    "carc_stage3_tc_prepare": (ctypes.c_int, [_pi64, _pi64, _pvp, _i32, _pvp, _i32, _vp, _i64, _vp]),
+    "carc_stage3_matvec_tc": (ctypes.c_int, [_pi64, _pi64, _i64, _vp, _i32, _i32, _pvp, _i32, _pi32, _i32, _vp, _vp,
+                                             _i32, _i32, _vp, _i64, _vp, _vp]),
+    "carc_stage3_matvec_tc_workspace_size": (_i64, [_pi64, _pi64, _i64, _i32, _i32]),
+    "carc_stage3_form_matrix_tc": (ctypes.c_int, [_pi64, _pi64, _i64, _pvp, _i32, _pvp, _i32, _pvp, _i32, _pi32, _i32,
+                                                  _vp, _i32, _vp, _i64, _vp, _vp]),
+    "carc_stage3_form_matrix_tc_workspace_size": (_i64, [_pi64, _pi64, _i64, _i32]),
+    "carc_gemm_bf16_tn": (ctypes.c_int, [_vp, _i32, _vp, _i32, _i32, _vp, _i64, _i32, _vp, _vp]),
 }
 
 _lock = threading.Lock()

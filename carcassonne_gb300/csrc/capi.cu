@@ -3,6 +3,8 @@
 #include "contract.cuh"
 #include "stage3.cuh"
 #include "linalg.cuh"
+#include "umma_gemm.cuh"
+#include "stage3_tc.cuh"
 
 using namespace carc;
 
@@ -112,6 +114,11 @@ int carc_normalize_axis_finish(int32_t n, const void* S, const void* Vh, double 
   return normalize_axis_finish(n, S, Vh, dont_recip_under, sqrt_svals, out_a, out_b, as_stream(stream));
 }
 
+int carc_zgeqr_economic(int32_t m, int32_t n, const void* A, void* Q, void* R, void* stream) {
+  if (!A || !Q || !R) return fail(CARC_BAD_ARG, "carc_zgeqr_economic: NULL argument");
+  return qr_mgs(m, n, A, Q, R, as_stream(stream));
+}
+
 int carc_zheev_jacobi(int32_t n, int32_t batch, const void* A, void* W, void* V, void* status, void* workspace,
                       int64_t workspace_bytes, void* stream) {
   if (!A || !W || !V || !status) return fail(CARC_BAD_ARG, "carc_zheev_jacobi: NULL argument");
@@ -185,5 +192,73 @@ int carc_relax_over(int32_t n, const void* H, const void* N, const void* x0, voi
 }
 
 int64_t carc_relax_over_workspace_size(int32_t n, int32_t k) { return relax_workspace_size(n, k); }
+
+int carc_zcontract_tc(const carc_contract_desc* desc, const void* A, const void* B, void* C, double alpha_re,
+                      double alpha_im, int32_t accumulate, int32_t ksplit, void* workspace, int64_t workspace_bytes,
+                      void* status, void* stream) {
+  if (!desc || !A || !B || !C || !status) return fail(CARC_BAD_ARG, "carc_zcontract_tc: NULL argument");
+  CARC_RETURN_IF(validate_desc(*desc));
+  ZView a = zview_a(*desc, A), b = zview_b(*desc, B);
+  ZOut c = zout_c(*desc, C);
+  CARC_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int), as_stream(stream)));
+  return zgemm_tc(a, b, c, cmk(alpha_re, alpha_im), accumulate, ksplit, workspace, workspace_bytes,
+                  static_cast<int*>(status), as_stream(stream));
+}
+
+int64_t carc_zcontract_tc_workspace_size(const carc_contract_desc* desc, int32_t ksplit) {
+  if (!desc || validate_desc(*desc) != CARC_OK) return -1;
+  return zgemm_tc_workspace(zview_a(*desc, nullptr), zview_b(*desc, nullptr), ksplit);
+}
+
+int carc_gemm_bf16_tn(const void* A, int32_t M, const void* B, int32_t N, int32_t K, float* out, int64_t ld_out,
+                      int32_t ksplit, void* status, void* stream) {
+  if (!A || !B || !out || !status) return fail(CARC_BAD_ARG, "carc_gemm_bf16_tn: NULL argument");
+  CARC_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int), as_stream(stream)));
+  return gemm_bf16_tn(A, M, B, N, K, out, ld_out, ksplit, static_cast<int*>(status), as_stream(stream));
+}
+
+int64_t carc_stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, int32_t n0, int32_t n1) {
+  if (!s0_shape || !s1_shape) return -1;
+  return stage3_tc_plan_size(s0_shape, s1_shape, n0, n1);
+}
+
+int carc_stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const void* const* s0_ptrs, int32_t n0,
+                           const void* const* s1_ptrs, int32_t n1, void* plan, int64_t plan_bytes, void* stream) {
+  if (!s0_shape || !s1_shape || !s0_ptrs || !s1_ptrs || !plan) return fail(CARC_BAD_ARG, "carc_stage3_tc_prepare: NULL");
+  return stage3_tc_prepare(s0_shape, s1_shape, s0_ptrs, n0, s1_ptrs, n1, plan, plan_bytes, as_stream(stream));
+}
+
+int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int32_t n0,
+                          int32_t n1, const void* const* op_ptrs, int32_t nop, const int32_t* terms, int32_t n_terms,
+                          const void* x, void* y, int32_t nvec, int32_t accumulate, void* workspace,
+                          int64_t workspace_bytes, void* status, void* stream) {
+  if (!s0_shape || !s1_shape || !plan || (nop > 0 && !op_ptrs) || (n_terms > 0 && !terms) || !x || !y || !status)
+    return fail(CARC_BAD_ARG, "carc_stage3_matvec_tc: NULL argument");
+  return stage3_matvec_tc(s0_shape, s1_shape, d, plan, n0, n1, op_ptrs, nop, terms, n_terms, x, y, nvec, accumulate,
+                          workspace, workspace_bytes, static_cast<int*>(status), as_stream(stream));
+}
+
+int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                                             int32_t n_terms, int32_t nvec) {
+  if (!s0_shape || !s1_shape) return -1;
+  return stage3_matvec_tc_ws(s0_shape, s1_shape, d, n_terms, nvec);
+}
+
+int carc_stage3_form_matrix_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* const* s0_ptrs,
+                               int32_t n0, const void* const* s1_ptrs, int32_t n1, const void* const* op_ptrs,
+                               int32_t nop, const int32_t* terms, int32_t n_terms, void* H, int32_t accumulate,
+                               void* workspace, int64_t workspace_bytes, void* status, void* stream) {
+  if (!s0_shape || !s1_shape || !s0_ptrs || !s1_ptrs || (nop > 0 && !op_ptrs) || (n_terms > 0 && !terms) || !H ||
+      !status)
+    return fail(CARC_BAD_ARG, "carc_stage3_form_matrix_tc: NULL argument");
+  return stage3_form_matrix_tc(s0_shape, s1_shape, d, s0_ptrs, n0, s1_ptrs, n1, op_ptrs, nop, terms, n_terms, H,
+                               accumulate, workspace, workspace_bytes, static_cast<int*>(status), as_stream(stream));
+}
+
+int64_t carc_stage3_form_matrix_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                                                  int32_t n_terms) {
+  if (!s0_shape || !s1_shape) return -1;
+  return stage3_form_matrix_tc_ws(s0_shape, s1_shape, d, n_terms);
+}
 
 }  // extern "C"

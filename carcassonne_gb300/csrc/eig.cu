@@ -208,6 +208,30 @@ __global__ void real_to_complex_kernel(int m, const double* __restrict__ s, doub
   for (int i = threadIdx.x; i < m; i += blockDim.x) h[i] = make_double2(s[i], 0.0);
 }
 
+// u[i] += eps * max|u| * r_i with r_i a fixed hash sequence in [-1, 1]^2 (eps alone when u = 0).
+// Launched as a single block so that every read of u precedes every write.
+__global__ void perturb_start_kernel(int n, double2* __restrict__ u, double eps) {
+  __shared__ double smax;
+  if (threadIdx.x == 0) smax = 0.0;
+  __syncthreads();
+  double m = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) m = fmax(m, sqrt(cabs2(u[i])));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(reinterpret_cast<unsigned long long*>(&smax), __double_as_longlong(m));
+  __syncthreads();
+  const double scale = eps * (smax > 0 ? smax : 1.0);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    uint32_t h = 2654435761u * (uint32_t)(i + 1);
+    h ^= h >> 16;
+    h *= 2246822519u;
+    h ^= h >> 13;
+    uint32_t g = h * 3266489917u;
+    g ^= g >> 16;
+    const double rr = (double)(h & 0xffffff) / 8388608.0 - 1.0, ri = (double)(g & 0xffffff) / 8388608.0 - 1.0;
+    u[i] = cadd(u[i], make_double2(scale * rr, scale * ri));
+  }
+}
+
 inline int blocks_for(int64_t n, int threads = 256) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, threads), 4 * 152));
 }
@@ -406,8 +430,13 @@ int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, d
     int32_t e[3] = {0, 0, 0};
     CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
   } else {
-    CARC_RETURN_IF(fill_launch(n, make_double2(1.0, 0.0), u0, stream));
+    CARC_RETURN_IF(fill_launch(n, make_double2(0.0, 0.0), u0, stream));
   }
+  // Mix a fixed pseudo-random direction into the start vector: a start that is
+  // exactly orthogonal to the ground state (e.g. by a symmetry of the
+  // previous center) would otherwise keep Lanczos out of its sector.
+  perturb_start_kernel<<<1, 256, 0, stream>>>(n, u0, x0 ? 1e-3 : 1.0);  // one block: reads finish before writes
+  CARC_CHECK_LAUNCH();
   int st = lanczos_lowest(n, Cm, u0, u, eigenvalue, max_krylov, max_restarts, tol, iterations, sub, sub_bytes, stream);
   if (st != CARC_OK && st != CARC_NOT_CONVERGED) return st;
   // x = Linv^H u : x[j] = sum_i conj(Li[i][j]) u[i]
@@ -521,53 +550,59 @@ __global__ void small_eig_min_real_kernel(int k, const double2* __restrict__ A0,
   for (int i = 1; i < k; ++i)
     if (ev[i].x < ev[best].x) best = i;
   const double2 lam = ev[best];
-  // null vector of (A0 - lam I) by Gaussian elimination with full pivoting
-  double2 B[SMALLK][SMALLK];
-  int colp[SMALLK];
-  for (int i = 0; i < k; ++i) {
-    colp[i] = i;
-    for (int j = 0; j < k; ++j) B[i][j] = i == j ? csub(A0[i * k + j], lam) : A0[i * k + j];
-  }
-  for (int p = 0; p < k - 1; ++p) {
-    int bi = p, bj = p;
-    double bv = -1.0;
-    for (int i = p; i < k; ++i)
-      for (int j = p; j < k; ++j)
-        if (cabs2(B[i][j]) > bv) {
-          bv = cabs2(B[i][j]);
-          bi = i;
-          bj = j;
-        }
-    for (int j = 0; j < k; ++j) {
-      double2 t = B[p][j];
-      B[p][j] = B[bi][j];
-      B[bi][j] = t;
-    }
-    for (int i = 0; i < k; ++i) {
-      double2 t = B[i][p];
-      B[i][p] = B[i][bj];
-      B[i][bj] = t;
-    }
-    int t = colp[p];
-    colp[p] = colp[bj];
-    colp[bj] = t;
-    if (bv <= 0.0) continue;
-    for (int i = p + 1; i < k; ++i) {
-      double2 f = cdiv(B[i][p], B[p][p]);
-      for (int j = p; j < k; ++j) B[i][j] = csub(B[i][j], cmul(f, B[p][j]));
-    }
-  }
+  // eigenvector by inverse iteration on (A0 - mu I), mu = lam + tiny, with
+  // partial pivoting: small residual even when Ritz values cluster
+  const double2 mu = cadd(lam, make_double2(1e-13 * scale, 1e-13 * scale));
   double2 y[SMALLK];
-  y[k - 1] = make_double2(1.0, 0.0);
-  for (int i = k - 2; i >= 0; --i) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int j = i + 1; j < k; ++j) s = cadd(s, cmul(B[i][j], y[j]));
-    y[i] = cabs2(B[i][i]) > 0 ? cscale(cdiv(s, B[i][i]), -1.0) : make_double2(0.0, 0.0);
+  for (int i = 0; i < k; ++i) y[i] = make_double2(1.0 / sqrt((double)k), 0.01 * i);
+  for (int iter = 0; iter < 4; ++iter) {
+    double2 B[SMALLK][SMALLK];
+    double2 rhs[SMALLK];
+    for (int i = 0; i < k; ++i) {
+      rhs[i] = y[i];
+      for (int j = 0; j < k; ++j) B[i][j] = i == j ? csub(A0[i * k + j], mu) : A0[i * k + j];
+    }
+    for (int p = 0; p < k; ++p) {
+      int piv = p;
+      for (int i = p + 1; i < k; ++i)
+        if (cabs2(B[i][p]) > cabs2(B[piv][p])) piv = i;
+      if (piv != p) {
+        for (int j = 0; j < k; ++j) {
+          double2 t = B[p][j];
+          B[p][j] = B[piv][j];
+          B[piv][j] = t;
+        }
+        double2 t = rhs[p];
+        rhs[p] = rhs[piv];
+        rhs[piv] = t;
+      }
+      if (cabs2(B[p][p]) < 1e-60 * scale * scale) B[p][p] = make_double2(1e-30 * scale, 0.0);
+      for (int i = p + 1; i < k; ++i) {
+        double2 f = cdiv(B[i][p], B[p][p]);
+        for (int j = p; j < k; ++j) B[i][j] = csub(B[i][j], cmul(f, B[p][j]));
+        rhs[i] = csub(rhs[i], cmul(f, rhs[p]));
+      }
+    }
+    for (int i = k - 1; i >= 0; --i) {
+      double2 s2 = rhs[i];
+      for (int j = i + 1; j < k; ++j) s2 = csub(s2, cmul(B[i][j], y[j]));
+      y[i] = cdiv(s2, B[i][i]);
+    }
+    double mx = 0.0;
+    for (int i = 0; i < k; ++i) mx = fmax(mx, sqrt(cabs2(y[i])));
+    if (!(mx > 0.0) || isinf(mx) || isnan(mx)) {
+      for (int i = 0; i < k; ++i) y[i] = make_double2(i == best ? 1.0 : 0.0, 0.0);
+      break;
+    }
+    double nr = 0.0;
+    for (int i = 0; i < k; ++i) {
+      y[i] = cscale(y[i], 1.0 / mx);
+      nr += cabs2(y[i]);
+    }
+    nr = sqrt(nr);
+    for (int i = 0; i < k; ++i) y[i] = cscale(y[i], 1.0 / nr);
   }
-  double nr = 0.0;
-  for (int i = 0; i < k; ++i) nr += cabs2(y[i]);
-  nr = sqrt(nr);
-  for (int i = 0; i < k; ++i) vec_out[colp[i]] = cscale(y[i], 1.0 / nr);
+  for (int i = 0; i < k; ++i) vec_out[i] = y[i];
   *lam_out = lam;
 }
 

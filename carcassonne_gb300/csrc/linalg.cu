@@ -145,6 +145,63 @@ __global__ void svd_finish_kernel(int m, int n, const double2* __restrict__ Wall
   }
 }
 
+// Columns of U whose singular value is negligible (<= tiny * S_max) are
+// replaced by an orthonormal completion (Gram-Schmidt, twice, of the standard
+// basis vectors against the columns already present), so that U stays an
+// isometry for rank-deficient input, as LAPACK's U does.
+__global__ void svd_complete_kernel(int m, int n, double2* __restrict__ Uall, int64_t u_stride,
+                                    const double* __restrict__ Sall, double tiny) {
+  double2* U = Uall + blockIdx.x * u_stride;
+  const double* S = Sall + blockIdx.x * (int64_t)n;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __shared__ double2 coef[SVD_WARPS * 4];
+  __shared__ double nrm;
+  __shared__ int cand;
+  const double smax = S[0];
+  for (int j = 0; j < n; ++j) {
+    if (S[j] > tiny * smax && S[j] > 0.0) continue;
+    if (threadIdx.x == 0) cand = 0;
+    __syncthreads();
+    for (int tries = 0; tries < m; ++tries) {
+      // column j = e_cand
+      for (int i = threadIdx.x; i < m; i += blockDim.x) U[(int64_t)i * n + j] = make_double2(i == cand ? 1.0 : 0.0, 0.0);
+      __syncthreads();
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int c = 0; c < n; ++c) {
+          if (c == j || (c > j && !(S[c] > tiny * smax && S[c] > 0.0))) continue;  // only valid/completed columns
+          double2 acc = make_double2(0.0, 0.0);
+          for (int i = threadIdx.x; i < m; i += blockDim.x) acc = cadd(acc, cmulc(U[(int64_t)i * n + c], U[(int64_t)i * n + j]));
+          acc = warp_sum2(acc);
+          if (lane == 0) coef[warp] = acc;
+          __syncthreads();
+          double2 h = make_double2(0.0, 0.0);
+          for (int w = 0; w < SVD_WARPS; ++w) h = cadd(h, coef[w]);
+          for (int i = threadIdx.x; i < m; i += blockDim.x)
+            U[(int64_t)i * n + j] = csub(U[(int64_t)i * n + j], cmul(h, U[(int64_t)i * n + c]));
+          __syncthreads();
+        }
+      }
+      double a = 0.0;
+      for (int i = threadIdx.x; i < m; i += blockDim.x) a += cabs2(U[(int64_t)i * n + j]);
+      a = warp_sum(a);
+      if (lane == 0) coef[warp] = make_double2(a, 0.0);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < SVD_WARPS; ++w) t += coef[w].x;
+        nrm = sqrt(t);
+      }
+      __syncthreads();
+      if (nrm > 0.5) break;
+      if (threadIdx.x == 0) cand = cand + 1;
+      __syncthreads();
+    }
+    const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) U[(int64_t)i * n + j] = cscale(U[(int64_t)i * n + j], inv);
+    __syncthreads();
+  }
+}
+
 }  // namespace
 
 int64_t svd_workspace_size(int m, int n, int batch) {
@@ -170,6 +227,9 @@ int svd_jacobi(int m, int n, int batch, const void* A, void* U, void* S, void* V
                                                               static_cast<double2*>(U), (int64_t)m * n,
                                                               static_cast<double*>(S), static_cast<double2*>(Vh),
                                                               (int64_t)n * n);
+  CARC_CHECK_LAUNCH();
+  svd_complete_kernel<<<batch, SVD_THREADS, 0, stream>>>(m, n, static_cast<double2*>(U), (int64_t)m * n,
+                                                        static_cast<const double*>(S), 1e-13 * (double)std::max(m, n));
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }
@@ -547,6 +607,71 @@ int normalize_axis_finish(int n, const void* S, const void* Vh, double thresh, i
   normalize_axis_finish_kernel<<<1, 256, 0, stream>>>(n, static_cast<const double*>(S),
                                                        static_cast<const double2*>(Vh), thresh, sqrt_svals,
                                                        static_cast<double2*>(out_a), static_cast<double2*>(out_b));
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Economic QR of a small m x n matrix (m >= n), one CTA: modified
+// Gram-Schmidt with a second orthogonalisation pass; R has a real,
+// non-negative diagonal (LAPACK's Householder QR may flip column signs).
+// Used by NDArrayData.qr / newEnlargener (data/__init__.py:43-50, :314-317).
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void qr_mgs_kernel(int m, int n, const double2* __restrict__ A, double2* __restrict__ Q,
+                              double2* __restrict__ R) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ double2 part[32];
+  __shared__ double2 hsh;
+  for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) R[idx] = make_double2(0.0, 0.0);
+  for (int idx = threadIdx.x; idx < m * n; idx += blockDim.x) Q[idx] = A[idx];
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int c = 0; c < j; ++c) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int i = threadIdx.x; i < m; i += blockDim.x) acc = cadd(acc, cmulc(Q[(int64_t)i * n + c], Q[(int64_t)i * n + j]));
+        acc = warp_sum2(acc);
+        if (lane == 0) part[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double2 h = make_double2(0.0, 0.0);
+          for (int w = 0; w < nw; ++w) h = cadd(h, part[w]);
+          hsh = h;
+          R[c * n + j] = cadd(R[c * n + j], h);
+        }
+        __syncthreads();
+        const double2 h = hsh;
+        for (int i = threadIdx.x; i < m; i += blockDim.x)
+          Q[(int64_t)i * n + j] = csub(Q[(int64_t)i * n + j], cmul(h, Q[(int64_t)i * n + c]));
+        __syncthreads();
+      }
+    }
+    double a = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) a += cabs2(Q[(int64_t)i * n + j]);
+    a = warp_sum(a);
+    if (lane == 0) part[warp] = make_double2(a, 0.0);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < nw; ++w) t += part[w].x;
+      hsh = make_double2(sqrt(t), 0.0);
+      R[j * n + j] = hsh;
+    }
+    __syncthreads();
+    const double inv = hsh.x > 0 ? 1.0 / hsh.x : 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) Q[(int64_t)i * n + j] = cscale(Q[(int64_t)i * n + j], inv);
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+int qr_mgs(int m, int n, const void* A, void* Q, void* R, cudaStream_t stream) {
+  if (m < 1 || n < 1 || m < n) return fail(CARC_BAD_SHAPE, "qr: needs m >= n >= 1 (got %d x %d)", m, n);
+  qr_mgs_kernel<<<1, 256, 0, stream>>>(m, n, static_cast<const double2*>(A), static_cast<double2*>(Q),
+                                      static_cast<double2*>(R));
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }

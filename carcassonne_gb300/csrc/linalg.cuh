@@ -25,4 +25,5 @@ int relax_over(int n, const void* H, const void* N, const void* x0, void* x_out,
                cudaStream_t stream);
 int normalize_axis_finish(int n, const void* S, const void* Vh, double thresh, int sqrt_svals, void* out_a,
                           void* out_b, cudaStream_t stream);
+int qr_mgs(int m, int n, const void* A, void* Q, void* R, cudaStream_t stream);
 }  // namespace carc

@@ -397,17 +397,27 @@ int stage3_form_matrix(const int64_t* s0_shape, const int64_t* s1_shape, int64_t
   for (int g = 0; g < n_groups; ++g) gptr[g] = gbase + (int64_t)g * gsize * 16;
   CARC_RETURN_IF(gett_launch(gd, s0_ptrs, n0, s1_ptrs, n1, gptr.data(), n_groups, entries.data(), n_terms,
                              make_double2(1, 0), 0, gw, gws, stream));
+  std::vector<const void*> gops(n_groups);
+  for (int g = 0; g < n_groups; ++g) gops[g] = group_op[g] < 0 ? nullptr : op_ptrs[group_op[g]];
+  return kron_launch(H, (const void* const*)gptr.data(), gops.data(), n_groups, (int)s.d, s.nl4, s.nk4, accumulate,
+                     stream);
+}
+
+int kron_launch(void* H, const void* const* groups, const void* const* ops, int n_groups, int d, int64_t nl4,
+                int64_t nk4, int accumulate, cudaStream_t stream) {
+  if (n_groups > KRON_MAX_GROUPS || d > KRON_MAX_D) return fail(CARC_TOO_LARGE, "kron: %d groups, d = %d", n_groups, d);
   KronParams kp;
   memset(&kp, 0, sizeof(kp));
   kp.n_groups = n_groups;
-  kp.d = (int)s.d;
-  kp.nl4 = s.nl4;
-  kp.nk4 = s.nk4;
+  kp.d = d;
+  kp.nl4 = nl4;
+  kp.nk4 = nk4;
   kp.accumulate = accumulate;
   for (int g = 0; g < n_groups; ++g) {
-    kp.g[g] = static_cast<const double2*>(gptr[g]);
-    kp.op[g] = group_op[g] < 0 ? nullptr : static_cast<const double2*>(op_ptrs[group_op[g]]);
+    kp.g[g] = static_cast<const double2*>(groups[g]);
+    kp.op[g] = static_cast<const double2*>(ops[g]);
   }
+  const int64_t gsize = nl4 * nk4;
   int blocks = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(gsize, 128), 8 * 152));
   kron_kernel<<<blocks, 128, 0, stream>>>(static_cast<double2*>(H), kp);
   CARC_CHECK_LAUNCH();

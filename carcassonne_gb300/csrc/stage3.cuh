@@ -13,4 +13,7 @@ int stage3_form_matrix(const int64_t* s0_shape, const int64_t* s1_shape, int64_t
                        int n0, const void* const* s1_ptrs, int n1, const void* const* op_ptrs, int nop,
                        const int32_t* terms, int n_terms, void* H, int accumulate, void* ws, int64_t ws_bytes,
                        cudaStream_t stream);
+// H[(l,p),(k,q)] (+)= sum_g G_g[l,k] O_g[p,q] (ops[g] == NULL: identity)
+int kron_launch(void* H, const void* const* groups, const void* const* ops, int n_groups, int d, int64_t nl4,
+                int64_t nk4, int accumulate, cudaStream_t stream);
 }  // namespace carc

@@ -1,0 +1,508 @@
+// The stage-3 operator on the tensor cores (split-BF16 operands, FP32
+// accumulation in TMEM, FP64 reductions):
+//
+//  matvec  y[v] = sum_t S2_0[i0_t] (x) S2_1[i1_t] (x) O[io_t] . x[v]
+//    per term:  step A  W[(x0,x1,l0,l1),(v,k2,k3,p)] = sum_{k0,k1} S2_0 . Vin
+//               (one tcgen05 GEMM; its FP32 partials are folded and re-split
+//               straight into the packed operand layout step B reads),
+//               step B  y^T[(l2,l3),(v,l0,l1,p)] += sum_{x0,x1,k2,k3} S2_1 . W
+//               (split-K tcgen05 GEMM; partial planes of all terms summed in FP64)
+//  matrix  H = sum_g G_g (x) O_g,  G_g = sum_{t in g} S2_0[i0_t] . S2_1[i1_t] over x,
+//          terms of one operator group concatenated along K in one GEMM.
+//
+// The S2 tensors are packed once per operator ("plan"): the many matvecs of a
+// solve reuse them.  Index convention as in stage3.cu (tensors/_2d/dense.py:114-195).
+#include "common.cuh"
+#include "contract.cuh"
+#include "stage3.cuh"
+#include "stage3_tc.cuh"
+#include "umma_gemm.cuh"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+namespace carc {
+
+namespace {
+
+inline int64_t a256(int64_t b) { return (b + 255) / 256 * 256; }
+
+struct S3 {
+  int64_t x0, x1, k0, k1, l0, l1, k2, k3, l2, l3, d;
+  int64_t s0[6], s1[6];
+};
+
+int s3_shapes(const int64_t* a, const int64_t* b, int64_t d, S3* s) {
+  for (int i = 0; i < 6; ++i)
+    if (a[i] < 1 || b[i] < 1) return fail(CARC_BAD_SHAPE, "stage3 tc: non-positive extent");
+  if (a[0] != b[1] || a[1] != b[0]) return fail(CARC_BAD_SHAPE, "stage3 tc: S2 halves do not glue");
+  s->x0 = a[0];
+  s->x1 = a[1];
+  s->k0 = a[2];
+  s->k1 = a[3];
+  s->l0 = a[4];
+  s->l1 = a[5];
+  s->k2 = b[2];
+  s->k3 = b[3];
+  s->l2 = b[4];
+  s->l3 = b[5];
+  s->d = d;
+  int64_t st = 1;
+  for (int i = 5; i >= 0; --i) {
+    s->s0[i] = st;
+    st *= a[i];
+  }
+  st = 1;
+  for (int i = 5; i >= 0; --i) {
+    s->s1[i] = st;
+    st *= b[i];
+  }
+  return CARC_OK;
+}
+
+// packed operand geometry of the matvec
+struct Geo {
+  int64_t rowsA_a, kpA;   // step A: S2_0 as A operand (rows 4*(x0 x1 l0 l1)), K' over (k0,k1)
+  int64_t rowsB_a, kpB;   // step B: S2_1 as A operand (rows 4*(l2 l3)), K' over (x0,x1,k2,k3)
+  int64_t rowsA_b;        // step A: Vin as B operand (rows nvec*k2*k3*d)
+  int64_t rowsB_b;        // step B: W as B operand (rows nvec*l0*l1*d)
+  int64_t kcA, kcB;       // complex K of the two steps
+};
+
+Geo geometry(const S3& s, int nvec) {
+  Geo g;
+  g.kcA = s.k0 * s.k1;
+  g.kcB = s.x0 * s.x1 * s.k2 * s.k3;
+  g.rowsA_a = round_up(4 * s.x0 * s.x1 * s.l0 * s.l1, 128);
+  g.kpA = round_up(4 * g.kcA, 64);
+  g.rowsB_a = round_up(4 * s.l2 * s.l3, 128);
+  g.kpB = round_up(4 * g.kcB, 64);
+  g.rowsA_b = round_up((int64_t)nvec * s.k2 * s.k3 * s.d, 16);
+  g.rowsB_b = round_up((int64_t)nvec * s.l0 * s.l1 * s.d, 16);
+  return g;
+}
+
+ZView view_s2_0_stepA(const S3& s, const void* base) {
+  ZView v;
+  memset(&v, 0, sizeof(v));
+  v.base = base;
+  v.nr = 4;
+  v.r_ext[0] = s.x0; v.r_str[0] = s.s0[0];
+  v.r_ext[1] = s.x1; v.r_str[1] = s.s0[1];
+  v.r_ext[2] = s.l0; v.r_str[2] = s.s0[4];
+  v.r_ext[3] = s.l1; v.r_str[3] = s.s0[5];
+  v.nk = 2;
+  v.k_ext[0] = s.k0; v.k_str[0] = s.s0[2];
+  v.k_ext[1] = s.k1; v.k_str[1] = s.s0[3];
+  return v;
+}
+
+ZView view_s2_1_stepB(const S3& s, const void* base) {
+  ZView v;
+  memset(&v, 0, sizeof(v));
+  v.base = base;
+  v.nr = 2;
+  v.r_ext[0] = s.l2; v.r_str[0] = s.s1[4];
+  v.r_ext[1] = s.l3; v.r_str[1] = s.s1[5];
+  v.nk = 4;  // (x0, x1, k2, k3): x0 is S2_1's axis 1, x1 its axis 0
+  v.k_ext[0] = s.x0; v.k_str[0] = s.s1[1];
+  v.k_ext[1] = s.x1; v.k_str[1] = s.s1[0];
+  v.k_ext[2] = s.k2; v.k_str[2] = s.s1[2];
+  v.k_ext[3] = s.k3; v.k_str[3] = s.s1[3];
+  return v;
+}
+
+// Vin[vec][k0][k1][k2][k3][p] as a B operand: rows (vec,k2,k3,p), k (k0,k1)
+ZView view_vin(const S3& s, int nvec, const void* base) {
+  const int64_t p1 = 1, k3 = s.d, k2 = s.k3 * k3, k1 = s.k2 * k2, k0 = s.k1 * k1, vec = s.k0 * k0;
+  ZView v;
+  memset(&v, 0, sizeof(v));
+  v.base = base;
+  v.nr = 4;
+  v.r_ext[0] = nvec; v.r_str[0] = vec;
+  v.r_ext[1] = s.k2; v.r_str[1] = k2;
+  v.r_ext[2] = s.k3; v.r_str[2] = k3;
+  v.r_ext[3] = s.d; v.r_str[3] = p1;
+  v.nk = 2;
+  v.k_ext[0] = s.k0; v.k_str[0] = k0;
+  v.k_ext[1] = s.k1; v.k_str[1] = k1;
+  return v;
+}
+
+// Fold the step-A partials (rows 4m + 2c + s, column n) into complex W[m, n]
+// and write it split into the packed B operand of step B:
+//   m = (x0,x1,l0,l1), n = (vec,k2,k3,p)  ->  row (vec,l0,l1,p), k (x0,x1,k2,k3).
+struct FoldParams {
+  int64_t x0, x1, l0, l1, nvec, k2, k3, d;
+  int64_t ld, kcB, kpB, M;
+};
+
+__global__ void fold_pack_w_kernel(const float* __restrict__ P, __nv_bfloat16* __restrict__ W,
+                                   const __grid_constant__ FoldParams f) {
+  const int64_t N = f.nvec * f.k2 * f.k3 * f.d;
+  const int64_t total = f.M * N;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = t / N, n = t % N;
+    const float* b = P + (4 * m) * f.ld + n;
+    const double re = (double)b[0] + (double)b[f.ld];
+    const double im = (double)b[2 * f.ld] + (double)b[3 * f.ld];
+    // m -> (x0,x1,l0,l1) ; n -> (vec,k2,k3,p)
+    int64_t r = m;
+    const int64_t l1 = r % f.l1; r /= f.l1;
+    const int64_t l0 = r % f.l0; r /= f.l0;
+    const int64_t x1 = r % f.x1; r /= f.x1;
+    const int64_t x0 = r;
+    int64_t q = n;
+    const int64_t p = q % f.d; q /= f.d;
+    const int64_t k3 = q % f.k3; q /= f.k3;
+    const int64_t k2 = q % f.k2; q /= f.k2;
+    const int64_t vec = q;
+    const int64_t row = ((vec * f.l0 + l0) * f.l1 + l1) * f.d + p;
+    const int64_t kk = ((x0 * f.x1 + x1) * f.k2 + k2) * f.k3 + k3;
+    const float fr = (float)re, fi = (float)im;
+    const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hi = __float2bfloat16_rn(fi);
+    const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
+    const __nv_bfloat16 li = __float2bfloat16_rn(fi - __bfloat162float(hi));
+    __nv_bfloat16* rowp = W + row * f.kpB;
+    *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * kk) = __halves2bfloat162(hr, hi);
+    *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * f.kcB + 2 * kk) = __halves2bfloat162(lr, li);
+  }
+}
+
+// zero the rows [r0, r1) and the K padding [4 kc, kp) of the packed W
+__global__ void clear_w_padding_kernel(__nv_bfloat16* __restrict__ W, int64_t rows_valid, int64_t rows_total,
+                                       int64_t kc4, int64_t kp) {
+  const int64_t pad = kp - kc4;
+  const int64_t t1 = rows_valid * pad, t2 = (rows_total - rows_valid) * kp;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < t1 + t2; t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < t1)
+      W[(t / pad) * kp + kc4 + t % pad] = __float2bfloat16_rn(0.f);
+    else
+      W[rows_valid * kp + (t - t1)] = __float2bfloat16_rn(0.f);
+  }
+}
+
+inline int grid_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * 152)); }
+
+int choose_ksplit(int64_t tiles, int64_t kp) {
+  const int64_t kb = kp / 64;
+  int64_t ks = (2 * 148 + tiles - 1) / tiles;
+  ks = std::max<int64_t>(1, std::min<int64_t>(ks, kb));
+  return (int)ks;
+}
+
+int bn_for(int64_t n) { return n % 256 == 0 ? 256 : n % 128 == 0 ? 128 : n % 64 == 0 ? 64 : n % 32 == 0 ? 32 : 16; }
+
+}  // namespace
+
+int64_t stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, int n0, int n1) {
+  S3 s;
+  if (s3_shapes(s0_shape, s1_shape, 1, &s) != CARC_OK) return -1;
+  Geo g = geometry(s, 1);
+  return (int64_t)n0 * a256(g.rowsA_a * g.kpA * 2) + (int64_t)n1 * a256(g.rowsB_a * g.kpB * 2);
+}
+
+int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const void* const* s0_ptrs, int n0,
+                      const void* const* s1_ptrs, int n1, void* plan, int64_t plan_bytes, cudaStream_t stream) {
+  S3 s;
+  CARC_RETURN_IF(s3_shapes(s0_shape, s1_shape, 1, &s));
+  if (plan_bytes < stage3_tc_plan_size(s0_shape, s1_shape, n0, n1)) return fail(CARC_BAD_ARG, "stage3 tc: plan too small");
+  Geo g = geometry(s, 1);
+  char* p = static_cast<char*>(plan);
+  for (int i = 0; i < n0; ++i) {
+    CARC_RETURN_IF(pack_operand(view_s2_0_stepA(s, s0_ptrs[i]), 0, p, g.rowsA_a, g.kpA, stream));
+    p += a256(g.rowsA_a * g.kpA * 2);
+  }
+  for (int i = 0; i < n1; ++i) {
+    CARC_RETURN_IF(pack_operand(view_s2_1_stepB(s, s1_ptrs[i]), 0, p, g.rowsB_a, g.kpB, stream));
+    p += a256(g.rowsB_a * g.kpB * 2);
+  }
+  return CARC_OK;
+}
+
+namespace {
+
+struct MvWs {
+  char* vop;      // n_ops x (nvec x nk4 x d) complex128
+  char* vin_pk;   // packed Vin (rowsA_b x kpA bf16)
+  float* pA;      // step A partials (rowsA_a x rowsA_b fp32)
+  char* w_pk;     // packed W (rowsB_b x kpB bf16)
+  float* pB;      // step B partials, n_terms * ksB planes (rowsB_a x rowsB_b)
+  int ksB;
+};
+
+int64_t mv_layout(const S3& s, int nvec, int n_terms, MvWs* w, void* base) {
+  Geo g = geometry(s, nvec);
+  const int64_t tilesB = (g.rowsB_a / 128) * (g.rowsB_b / bn_for(g.rowsB_b));
+  const int ksB = gemm_effective_ksplit((int)g.kpB, choose_ksplit(tilesB, g.kpB));
+  const int64_t nk4 = s.k0 * s.k1 * s.k2 * s.k3;
+  int64_t sizes[5] = {(int64_t)n_terms * nvec * nk4 * s.d * 16, g.rowsA_b * g.kpA * 2, g.rowsA_a * g.rowsA_b * 4,
+                      g.rowsB_b * g.kpB * 2, (int64_t)n_terms * ksB * g.rowsB_a * g.rowsB_b * 4};
+  char* p = static_cast<char*>(base);
+  int64_t off = 0;
+  char* ptrs[5];
+  for (int i = 0; i < 5; ++i) {
+    ptrs[i] = p ? p + off : nullptr;
+    off += a256(sizes[i]);
+  }
+  if (w) {
+    w->vop = ptrs[0];
+    w->vin_pk = ptrs[1];
+    w->pA = reinterpret_cast<float*>(ptrs[2]);
+    w->w_pk = ptrs[3];
+    w->pB = reinterpret_cast<float*>(ptrs[4]);
+    w->ksB = ksB;
+  }
+  return off;
+}
+
+}  // namespace
+
+int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int n_terms, int nvec) {
+  S3 s;
+  if (s3_shapes(s0_shape, s1_shape, d, &s) != CARC_OK) return -1;
+  if (n_terms < 1 || nvec < 1) return 0;
+  return mv_layout(s, nvec, n_terms, nullptr, nullptr);
+}
+
+int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int n0, int n1,
+                     const void* const* op_ptrs, int nop, const int32_t* terms, int n_terms, const void* x, void* y,
+                     int nvec, int accumulate, void* ws, int64_t ws_bytes, int* status, cudaStream_t stream) {
+  S3 s;
+  CARC_RETURN_IF(s3_shapes(s0_shape, s1_shape, d, &s));
+  const int64_t nl4 = s.l0 * s.l1 * s.l2 * s.l3, nk4 = s.k0 * s.k1 * s.k2 * s.k3;
+  if (n_terms == 0) {
+    if (!accumulate) return fill_launch((int64_t)nvec * nl4 * d, make_double2(0, 0), y, stream);
+    return CARC_OK;
+  }
+  if (ws_bytes < stage3_matvec_tc_ws(s0_shape, s1_shape, d, n_terms, nvec))
+    return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
+  for (int t = 0; t < n_terms; ++t) {
+    int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
+    if (i0 < 0 || i0 >= n0 || i1 < 0 || i1 >= n1 || io >= nop)
+      return fail(CARC_BAD_ARG, "stage3 tc matvec: term %d out of range", t);
+  }
+  Geo gA = geometry(s, 1);
+  Geo g = geometry(s, nvec);
+  MvWs w;
+  mv_layout(s, nvec, n_terms, &w, ws);
+  const char* planA = static_cast<const char*>(plan);
+  const char* planB = planA + (int64_t)n0 * a256(gA.rowsA_a * gA.kpA * 2);
+  // operators applied to x (FP64, tiny): Vop_o[vec][k4][p] = sum_q O[p,q] x[vec][k4][q]
+  std::map<int, int> op_slot;
+  for (int t = 0; t < n_terms; ++t) {
+    int io = terms[3 * t + 2];
+    if (io >= 0 && !op_slot.count(io)) {
+      int slot = (int)op_slot.size();
+      op_slot[io] = slot;
+      carc_contract_desc dop = DescBuilder()
+                                   .m(s.d, s.d, 1)
+                                   .n(nvec, nk4 * s.d, nk4 * s.d)
+                                   .n(nk4, s.d, s.d)
+                                   .k(s.d, 1, 1)
+                                   .d;
+      const void* pa[1] = {op_ptrs[io]};
+      const void* pb[1] = {x};
+      void* pc[1] = {w.vop + (int64_t)slot * nvec * nk4 * s.d * 16};
+      int32_t e[3] = {0, 0, 0};
+      CARC_RETURN_IF(gett_launch(dop, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, nullptr, 0, stream));
+    }
+  }
+  const int64_t MA = s.x0 * s.x1 * s.l0 * s.l1;
+  FoldParams fp;
+  fp.x0 = s.x0;
+  fp.x1 = s.x1;
+  fp.l0 = s.l0;
+  fp.l1 = s.l1;
+  fp.nvec = nvec;
+  fp.k2 = s.k2;
+  fp.k3 = s.k3;
+  fp.d = s.d;
+  fp.ld = g.rowsA_b;
+  fp.kcB = g.kcB;
+  fp.kpB = g.kpB;
+  fp.M = MA;
+  const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
+  const int64_t planeB = g.rowsB_a * g.rowsB_b;
+  for (int t = 0; t < n_terms; ++t) {
+    const int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
+    const void* vin = io < 0 ? x : (const void*)(w.vop + (int64_t)op_slot[io] * nvec * nk4 * s.d * 16);
+    CARC_RETURN_IF(pack_operand(view_vin(s, nvec, vin), 1, w.vin_pk, g.rowsA_b, g.kpA, stream));
+    // step A: W = S2_0 . Vin  (single pass over K = k0 k1)
+    const char* a_op = planA + (int64_t)i0 * a256(gA.rowsA_a * gA.kpA * 2);
+    CARC_RETURN_IF(gemm_bf16_tn(a_op, (int)g.rowsA_a, w.vin_pk, (int)g.rowsA_b, (int)g.kpA, w.pA, g.rowsA_b, 1,
+                                status, stream));
+    clear_w_padding_kernel<<<grid_of(rows_valid_w * (g.kpB - 4 * g.kcB) + (g.rowsB_b - rows_valid_w) * g.kpB), 256, 0,
+                             stream>>>(reinterpret_cast<__nv_bfloat16*>(w.w_pk), rows_valid_w, g.rowsB_b, 4 * g.kcB,
+                                       g.kpB);
+    CARC_CHECK_LAUNCH();
+    fold_pack_w_kernel<<<grid_of(MA * nvec * s.k2 * s.k3 * s.d), 256, 0, stream>>>(
+        w.pA, reinterpret_cast<__nv_bfloat16*>(w.w_pk), fp);
+    CARC_CHECK_LAUNCH();
+    // step B: y^T += S2_1 . W   (split K over x0 x1 k2 k3)
+    const char* b_op = planB + (int64_t)i1 * a256(gA.rowsB_a * gA.kpB * 2);
+    CARC_RETURN_IF(gemm_bf16_tn(b_op, (int)g.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)g.kpB,
+                                w.pB + (int64_t)t * w.ksB * planeB, g.rowsB_b, w.ksB, status, stream));
+  }
+  // y[vec][l0][l1][l2][l3][p] (+)= sum over all term and split planes
+  ZOut o;
+  memset(&o, 0, sizeof(o));
+  o.base = y;
+  const int64_t yl3 = s.d, yl2 = s.l3 * yl3, yl1 = s.l2 * yl2, yl0 = s.l1 * yl1, yv = s.l0 * yl0;
+  o.nm = 2;
+  o.m_ext[0] = s.l2; o.m_str[0] = yl2;
+  o.m_ext[1] = s.l3; o.m_str[1] = yl3;
+  o.nn = 4;
+  o.n_ext[0] = nvec; o.n_str[0] = yv;
+  o.n_ext[1] = s.l0; o.n_str[1] = yl0;
+  o.n_ext[2] = s.l1; o.n_str[2] = yl1;
+  o.n_ext[3] = s.d; o.n_str[3] = 1;
+  return reduce_partials(w.pB, g.rowsB_b, planeB, n_terms * w.ksB, o, make_double2(1, 0), accumulate, stream);
+}
+
+// ---------------------------------------------------------------------------
+// H_eff on the tensor cores
+// ---------------------------------------------------------------------------
+namespace {
+
+ZView view_s2_0_G(const S3& s, const void* base) {  // rows (l0,l1,k0,k1), k (x0,x1)
+  ZView v;
+  memset(&v, 0, sizeof(v));
+  v.base = base;
+  v.nr = 4;
+  v.r_ext[0] = s.l0; v.r_str[0] = s.s0[4];
+  v.r_ext[1] = s.l1; v.r_str[1] = s.s0[5];
+  v.r_ext[2] = s.k0; v.r_str[2] = s.s0[2];
+  v.r_ext[3] = s.k1; v.r_str[3] = s.s0[3];
+  v.nk = 2;
+  v.k_ext[0] = s.x0; v.k_str[0] = s.s0[0];
+  v.k_ext[1] = s.x1; v.k_str[1] = s.s0[1];
+  return v;
+}
+
+ZView view_s2_1_G(const S3& s, const void* base) {  // rows (l2,l3,k2,k3), k (x0,x1)
+  ZView v;
+  memset(&v, 0, sizeof(v));
+  v.base = base;
+  v.nr = 4;
+  v.r_ext[0] = s.l2; v.r_str[0] = s.s1[4];
+  v.r_ext[1] = s.l3; v.r_str[1] = s.s1[5];
+  v.r_ext[2] = s.k2; v.r_str[2] = s.s1[2];
+  v.r_ext[3] = s.k3; v.r_str[3] = s.s1[3];
+  v.nk = 2;
+  v.k_ext[0] = s.x0; v.k_str[0] = s.s1[1];
+  v.k_ext[1] = s.x1; v.k_str[1] = s.s1[0];
+  return v;
+}
+
+struct FormGeo {
+  int64_t M, N, rows_a, rows_b, region, kp_max;
+  int max_terms, ks;
+};
+
+FormGeo form_geometry(const S3& s, int max_terms) {
+  FormGeo f;
+  f.M = s.l0 * s.l1 * s.k0 * s.k1;
+  f.N = s.l2 * s.l3 * s.k2 * s.k3;
+  f.rows_a = round_up(4 * f.M, 128);
+  f.rows_b = round_up(f.N, 16);
+  f.region = round_up(4 * s.x0 * s.x1, 64);
+  f.max_terms = max_terms;
+  f.kp_max = f.region * max_terms;
+  const int64_t tiles = (f.rows_a / 128) * (f.rows_b / bn_for(f.rows_b));
+  f.ks = gemm_effective_ksplit((int)f.kp_max, choose_ksplit(tiles, f.kp_max));
+  return f;
+}
+
+}  // namespace
+
+int64_t stage3_form_matrix_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int n_terms) {
+  S3 s;
+  if (s3_shapes(s0_shape, s1_shape, d, &s) != CARC_OK) return -1;
+  if (n_terms < 1) return 0;
+  FormGeo f = form_geometry(s, n_terms);
+  return a256(f.rows_a * f.kp_max * 2) + a256(f.rows_b * f.kp_max * 2) + a256((int64_t)f.ks * f.rows_a * f.rows_b * 4) +
+         (int64_t)n_terms * a256(f.M * f.N * 16);
+}
+
+int stage3_form_matrix_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* const* s0_ptrs,
+                          int n0, const void* const* s1_ptrs, int n1, const void* const* op_ptrs, int nop,
+                          const int32_t* terms, int n_terms, void* H, int accumulate, void* ws, int64_t ws_bytes,
+                          int* status, cudaStream_t stream) {
+  S3 s;
+  CARC_RETURN_IF(s3_shapes(s0_shape, s1_shape, d, &s));
+  const int64_t nrow = s.l0 * s.l1 * s.l2 * s.l3 * d, ncol = s.k0 * s.k1 * s.k2 * s.k3 * d;
+  if (n_terms == 0) {
+    if (!accumulate) return fill_launch(nrow * ncol, make_double2(0, 0), H, stream);
+    return CARC_OK;
+  }
+  if (ws_bytes < stage3_form_matrix_tc_ws(s0_shape, s1_shape, d, n_terms))
+    return fail(CARC_BAD_ARG, "stage3 tc matrix: workspace too small");
+  // operator groups
+  std::vector<int> group_op;
+  std::vector<std::vector<int>> group_terms;
+  for (int t = 0; t < n_terms; ++t) {
+    int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
+    if (i0 < 0 || i0 >= n0 || i1 < 0 || i1 >= n1 || io >= nop)
+      return fail(CARC_BAD_ARG, "stage3 tc matrix: term %d out of range", t);
+    int key = io < 0 ? -1 : io;
+    int g = -1;
+    for (size_t q = 0; q < group_op.size(); ++q)
+      if (group_op[q] == key) g = (int)q;
+    if (g < 0) {
+      g = (int)group_op.size();
+      group_op.push_back(key);
+      group_terms.emplace_back();
+    }
+    group_terms[g].push_back(t);
+  }
+  FormGeo f = form_geometry(s, n_terms);
+  char* p = static_cast<char*>(ws);
+  char* A_op = p;
+  char* B_op = A_op + a256(f.rows_a * f.kp_max * 2);
+  float* P = reinterpret_cast<float*>(B_op + a256(f.rows_b * f.kp_max * 2));
+  char* Gbase = reinterpret_cast<char*>(P) + a256((int64_t)f.ks * f.rows_a * f.rows_b * 4);
+  std::vector<const void*> gptr(group_op.size()), gops(group_op.size());
+  for (size_t g = 0; g < group_op.size(); ++g) {
+    const std::vector<int>& tl = group_terms[g];
+    const int64_t kp = f.region * (int64_t)tl.size();
+    for (size_t j = 0; j < tl.size(); ++j) {
+      const int t = tl[j];
+      CARC_RETURN_IF(pack_operand_region(view_s2_0_G(s, s0_ptrs[terms[3 * t]]), 0, A_op, f.rows_a, kp,
+                                         (int64_t)j * f.region, f.region, stream));
+      CARC_RETURN_IF(pack_operand_region(view_s2_1_G(s, s1_ptrs[terms[3 * t + 1]]), 1, B_op, f.rows_b, kp,
+                                         (int64_t)j * f.region, f.region, stream));
+    }
+    const int64_t tiles = (f.rows_a / 128) * (f.rows_b / bn_for(f.rows_b));
+    const int ks = gemm_effective_ksplit((int)kp, choose_ksplit(tiles, kp));
+    CARC_RETURN_IF(gemm_bf16_tn(A_op, (int)f.rows_a, B_op, (int)f.rows_b, (int)kp, P, f.rows_b, ks, status, stream));
+    void* G = Gbase + (int64_t)g * a256(f.M * f.N * 16);
+    // G[(l0,l1,l2,l3),(k0,k1,k2,k3)] from rows (l0,l1,k0,k1) x cols (l2,l3,k2,k3)
+    const int64_t gk3 = 1, gk2 = s.k3, gk1 = s.k2 * gk2, gk0 = s.k1 * gk1, gl3 = s.k0 * gk0, gl2 = s.l3 * gl3,
+                  gl1 = s.l2 * gl2, gl0 = s.l1 * gl1;
+    ZOut o;
+    memset(&o, 0, sizeof(o));
+    o.base = G;
+    o.nm = 4;
+    o.m_ext[0] = s.l0; o.m_str[0] = gl0;
+    o.m_ext[1] = s.l1; o.m_str[1] = gl1;
+    o.m_ext[2] = s.k0; o.m_str[2] = gk0;
+    o.m_ext[3] = s.k1; o.m_str[3] = gk1;
+    o.nn = 4;
+    o.n_ext[0] = s.l2; o.n_str[0] = gl2;
+    o.n_ext[1] = s.l3; o.n_str[1] = gl3;
+    o.n_ext[2] = s.k2; o.n_str[2] = gk2;
+    o.n_ext[3] = s.k3; o.n_str[3] = gk3;
+    CARC_RETURN_IF(reduce_partials(P, f.rows_b, f.rows_a * f.rows_b, ks, o, make_double2(1, 0), 0, stream));
+    gptr[g] = G;
+    gops[g] = group_op[g] < 0 ? nullptr : op_ptrs[group_op[g]];
+  }
+  return kron_launch(H, gptr.data(), gops.data(), (int)group_op.size(), (int)s.d, s.l0 * s.l1 * s.l2 * s.l3,
+                     s.k0 * s.k1 * s.k2 * s.k3, accumulate, stream);
+}
+
+}  // namespace carc

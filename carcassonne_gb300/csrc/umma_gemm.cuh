@@ -1,0 +1,50 @@
+// Host-side interface of the split-BF16 tensor-core complex GEMM (umma_gemm.cu).
+#pragma once
+#include "common.cuh"
+
+namespace carc {
+
+// A complex128 operand seen as a (rows x k) matrix through strided index groups.
+struct ZView {
+  const void* base;
+  int nr, nk;
+  int64_t r_ext[CARC_MAX_SUBDIMS], r_str[CARC_MAX_SUBDIMS];
+  int64_t k_ext[CARC_MAX_SUBDIMS], k_str[CARC_MAX_SUBDIMS];
+  int conj;
+};
+
+// A complex128 output seen as (m x n) through strided index groups.
+struct ZOut {
+  void* base;
+  int nm, nn;
+  int64_t m_ext[CARC_MAX_SUBDIMS], m_str[CARC_MAX_SUBDIMS];
+  int64_t n_ext[CARC_MAX_SUBDIMS], n_str[CARC_MAX_SUBDIMS];
+};
+
+int64_t zview_rows(const ZView& v);
+int64_t zview_k(const ZView& v);
+int64_t round_up(int64_t a, int64_t b);
+
+// Raw GEMM: out[z][m][n] (fp32, ld_out) = sum over split z's K range of A[m,:] . B[n,:]
+// (A: M x K, B: N x K, BF16 K-major; M % 128 == 0, K % 64 == 0, N % 16 == 0).
+int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
+                 cudaStream_t stream);
+int gemm_effective_ksplit(int K, int ksplit);
+// role 0: A operand (rows (m, re/im, hi/lo)); role 1: B operand (row n, K = [hi | lo]).
+int pack_operand(const ZView& v, int role, void* out, int64_t rows_out, int64_t kp_out, cudaStream_t stream);
+// Pack into the K-column region [col_off, col_off + region) of rows of pitch kp_out (region >= 4K, rest zeroed).
+int pack_operand_region(const ZView& v, int role, void* out, int64_t rows_out, int64_t kp_out, int64_t col_off,
+                        int64_t region, cudaStream_t stream);
+int reduce_partials(const float* P, int64_t ld, int64_t split_stride, int ksplit, const ZOut& o, double2 alpha,
+                    int accumulate, cudaStream_t stream);
+
+ZView zview_a(const carc_contract_desc& d, const void* base);
+ZView zview_b(const carc_contract_desc& d, const void* base);
+ZOut zout_c(const carc_contract_desc& d, void* base);
+
+// C (+)= alpha A B^T, complex, on the tensor cores with split-BF16 operands.
+int64_t zgemm_tc_workspace(const ZView& a, const ZView& b, int ksplit);
+int zgemm_tc(const ZView& a, const ZView& b, const ZOut& c, double2 alpha, int accumulate, int ksplit, void* ws,
+             int64_t ws_bytes, int* err, cudaStream_t stream);
+
+}  // namespace carc

@@ -40,7 +40,6 @@ class Data:
 
 
 class TorchData(Data):
-    __slots__ = ["_t"]
 
     # -- construction ---------------------------------------------------------
     def __init__(self, t):

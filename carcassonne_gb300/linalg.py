@@ -92,6 +92,23 @@ def normalize_axis(data, axis, sqrt_svals=False, dont_recip_under=1e-14):
     return iso.split(*split).join(*inv), TorchData(a), TorchData(b)
 
 
+def qr(data, mode="full"):
+    """Q, R of a matrix; only the economic factorisation is computed (mode
+    'full' is accepted for tall matrices whose economic Q is what callers use)."""
+    t = (data._t if isinstance(data, TorchData) else TorchData(data)._t).contiguous()
+    m, n = t.shape
+    if m < n:
+        raise ValueError("qr on the GPU needs rows >= columns")
+    Q = torch.empty((m, n), dtype=CDT, device=t.device)
+    R = torch.empty((n, n), dtype=CDT, device=t.device)
+    _lib.call("carc_zgeqr_economic", m, n, _vp(t), _vp(Q), _vp(R), current_stream_handle())
+    return TorchData(Q), TorchData(R)
+
+
+def qr_economic(data):
+    return qr(data, "economic")[0]
+
+
 def eigh_small(matrix):
     """(W ascending, V) of a small Hermitian matrix (Jacobi, n <= 512)."""
     t = matrix._t if isinstance(matrix, TorchData) else TorchData(matrix)._t
@@ -158,4 +175,4 @@ def hegv_lowest(H, N, x0=None, tol=1e-13, max_krylov=256, max_restarts=8):
     return lam.value, TorchData(x), iters.value
 
 
-__all__ = ["svd", "unitize", "normalize_axis", "eigh_small", "cholesky", "tri_inverse_lower", "hegv_lowest"]
+__all__ = ["svd", "unitize", "normalize_axis", "qr", "qr_economic", "eigh_small", "cholesky", "tri_inverse_lower", "hegv_lowest"]

@@ -61,24 +61,41 @@ class _PairContractor:
         return TorchData(out)
 
     def grouped(self, list_a, list_b, table, n_out):
+        """All (i, j, slot) pairs of a sparse contraction.  Pairs are launched
+        together per operand-shape class (tags of one boundary may differ in
+        shape, e.g. a compressed operator axis); a slot reached by several
+        launches accumulates, in table order within each launch."""
         ta = [_t(x) for x in list_a]
         tb = [_t(x) for x in list_b]
-        self._validate(ta[0], tb[0])
-        shape = self.shape_fn(ta[0].shape, tb[0].shape)
-        outs = [torch.empty(shape, dtype=CDT, device=ta[0].device) for _ in range(n_out)]
-        for lo in range(0, len(table), _lib.MAX_ENTRIES):
-            chunk = table[lo:lo + _lib.MAX_ENTRIES]
-            used_a = sorted({e[0] for e in chunk})
-            used_b = sorted({e[1] for e in chunk})
-            used_c = sorted({e[2] for e in chunk})
-            ma = {v: i for i, v in enumerate(used_a)}
-            mb = {v: i for i, v in enumerate(used_b)}
-            mc = {v: i for i, v in enumerate(used_c)}
-            # output slots already written by an earlier chunk accumulate
-            first = all(e[2] not in {x[2] for x in table[:lo]} for e in chunk)
-            engine.contract_grouped(self.spec, [ta[i] for i in used_a], [tb[i] for i in used_b],
-                                    [outs[i] for i in used_c], [(ma[i], mb[j], mc[k]) for i, j, k in chunk],
-                                    accumulate=not first)
+        classes = {}
+        for e in table:
+            key = (tuple(ta[e[0]].shape), tuple(tb[e[1]].shape))
+            classes.setdefault(key, []).append(e)
+        outs = [None] * n_out
+        for (sa, sb), entries in classes.items():
+            a0 = next(ta[e[0]] for e in entries)
+            b0 = next(tb[e[1]] for e in entries)
+            self._validate(a0, b0)
+            shape = self.shape_fn(a0.shape, b0.shape)
+            for lo in range(0, len(entries), _lib.MAX_ENTRIES):
+                chunk = entries[lo:lo + _lib.MAX_ENTRIES]
+                used_a = sorted({e[0] for e in chunk})
+                used_b = sorted({e[1] for e in chunk})
+                used_c = sorted({e[2] for e in chunk})
+                written = [outs[c] is not None for c in used_c]
+                for c in used_c:
+                    if outs[c] is None:
+                        outs[c] = TorchData.newZeros(shape)._t
+                    elif tuple(outs[c].shape) != tuple(shape):
+                        raise ValueError("operands could not be broadcast together with shapes %s %s"
+                                         % (tuple(outs[c].shape), tuple(shape)))
+                ma = {v: i for i, v in enumerate(used_a)}
+                mb = {v: i for i, v in enumerate(used_b)}
+                mc = {v: i for i, v in enumerate(used_c)}
+                single = len(classes) == 1 and lo == 0
+                engine.contract_grouped(self.spec, [ta[i] for i in used_a], [tb[i] for i in used_b],
+                                        [outs[i] for i in used_c], [(ma[i], mb[j], mc[k]) for i, j, k in chunk],
+                                        accumulate=not single or any(written))
         return [TorchData(o) for o in outs]
 
 
@@ -158,17 +175,33 @@ def _side_out_shape(side_shape, e_shape):
 
 
 def _absorb_pairs(direction, sides, pairs_e, table, n_out):
+    """Grouped side (x) center-pair contractions; launched per side-shape class
+    (a compressed operator tag has its own shape), slots accumulating."""
     ts = [_t(x) for x in sides]
     for t in ts:
         _check_rank(0, t, 8)
     e0 = pairs_e[0]
-    if ts[0].shape[6] != e0.shape[6]:
-        raise DimensionMismatchError(0, 6, int(ts[0].shape[6]), 1, direction, int(e0.shape[6]))
-    if ts[0].shape[7] != e0.shape[7]:
-        raise DimensionMismatchError(0, 7, int(ts[0].shape[7]), 2, direction, int(e0.shape[7]))
-    shape = _side_out_shape(ts[0].shape, e0.shape)
-    outs = [torch.empty(shape, dtype=CDT, device=ts[0].device) for _ in range(n_out)]
-    engine.contract_grouped(_SIDE_SPEC, ts, pairs_e, outs, table)
+    classes = {}
+    for e in table:
+        classes.setdefault(tuple(ts[e[0]].shape), []).append(e)
+    outs = [None] * n_out
+    for sshape, entries in classes.items():
+        if sshape[6] != e0.shape[6]:
+            raise DimensionMismatchError(0, 6, int(sshape[6]), 1, direction, int(e0.shape[6]))
+        if sshape[7] != e0.shape[7]:
+            raise DimensionMismatchError(0, 7, int(sshape[7]), 2, direction, int(e0.shape[7]))
+        shape = _side_out_shape(sshape, e0.shape)
+        used_s = sorted({e[0] for e in entries})
+        used_c = sorted({e[2] for e in entries})
+        written = any(outs[c] is not None for c in used_c)
+        for c in used_c:
+            if outs[c] is None:
+                outs[c] = TorchData.newZeros(shape)._t if len(classes) > 1 else \
+                    torch.empty(shape, dtype=CDT, device=ts[0].device)
+        ms = {v: i for i, v in enumerate(used_s)}
+        mc = {v: i for i, v in enumerate(used_c)}
+        engine.contract_grouped(_SIDE_SPEC, [ts[i] for i in used_s], pairs_e, [outs[c] for c in used_c],
+                                [(ms[i], j, mc[k]) for i, j, k in entries], accumulate=len(classes) > 1 or written)
     return [TorchData(o) for o in outs]
 
 
@@ -202,39 +235,130 @@ class Stage3Operator:
         self.ops = [_t(x).contiguous() for x in ops]
         self.terms = [tuple(int(v) for v in t) for t in terms]
         self.d = int(d)
-        if self.s2_0:
-            _check_rank(0, self.s2_0[0], 6)
-            _check_rank(1, self.s2_1[0], 6)
-            if self.s2_0[0].shape[0] != self.s2_1[0].shape[1]:
-                raise DimensionMismatchError(0, 0, int(self.s2_0[0].shape[0]), 1, 1, int(self.s2_1[0].shape[1]))
-            if self.s2_0[0].shape[1] != self.s2_1[0].shape[0]:
-                raise DimensionMismatchError(0, 1, int(self.s2_0[0].shape[1]), 1, 0, int(self.s2_1[0].shape[0]))
-        self.s0_shape = tuple(int(x) for x in self.s2_0[0].shape)
-        self.s1_shape = tuple(int(x) for x in self.s2_1[0].shape)
+        for t in self.s2_0:
+            _check_rank(0, t, 6)
+        for t in self.s2_1:
+            _check_rank(1, t, 6)
+        for i0, i1, _ in self.terms:
+            a, b = self.s2_0[i0], self.s2_1[i1]
+            if a.shape[0] != b.shape[1]:
+                raise DimensionMismatchError(0, 0, int(a.shape[0]), 1, 1, int(b.shape[1]))
+            if a.shape[1] != b.shape[0]:
+                raise DimensionMismatchError(0, 1, int(a.shape[1]), 1, 0, int(b.shape[0]))
+        ref0 = self.s2_0[self.terms[0][0]] if self.terms else self.s2_0[0]
+        ref1 = self.s2_1[self.terms[0][1]] if self.terms else self.s2_1[0]
+        self.s0_shape = tuple(int(x) for x in ref0.shape)
+        self.s1_shape = tuple(int(x) for x in ref1.shape)
         k0, k1, l0, l1 = self.s0_shape[2:6]
         k2, k3, l2, l3 = self.s1_shape[2:6]
         self.in_shape = (k0, k1, k2, k3, self.d)
         self.out_shape = (l0, l1, l2, l3, self.d)
-        self.device = self.s2_0[0].device
+        self.device = ref0.device
         self._pack()
 
     def _pack(self):
-        self._p0, self._k0 = _lib.ptr_array([t.data_ptr() for t in self.s2_0])
-        self._p1, self._k1 = _lib.ptr_array([t.data_ptr() for t in self.s2_1])
+        """One library call per shape class of (S2_0, S2_1) pairs; the stage-2
+        tags of a boundary differ in shape only through a compressed operator axis."""
+        classes = {}
+        for t in self.terms:
+            key = (tuple(self.s2_0[t[0]].shape), tuple(self.s2_1[t[1]].shape))
+            classes.setdefault(key, []).append(t)
+        self._groups = []
         self._po, self._ko = _lib.ptr_array([t.data_ptr() for t in self.ops])
-        self._pt, self._kt = _lib.i32_array([v for t in self.terms for v in t])
-        self._s0, self._ks0 = _lib.i64_array(self.s0_shape)
-        self._s1, self._ks1 = _lib.i64_array(self.s1_shape)
+        for (sh0, sh1), terms in classes.items():
+            i0s = sorted({t[0] for t in terms})
+            i1s = sorted({t[1] for t in terms})
+            m0 = {v: i for i, v in enumerate(i0s)}
+            m1 = {v: i for i, v in enumerate(i1s)}
+            g = dict(shape0=sh0, shape1=sh1, n0=len(i0s), n1=len(i1s),
+                     terms=[(m0[a], m1[b], c) for a, b, c in terms])
+            g["p0"], g["k0"] = _lib.ptr_array([self.s2_0[i].data_ptr() for i in i0s])
+            g["p1"], g["k1"] = _lib.ptr_array([self.s2_1[i].data_ptr() for i in i1s])
+            g["pt"], g["kt"] = _lib.i32_array([v for t in g["terms"] for v in t])
+            g["s0"], g["ks0"] = _lib.i64_array(sh0)
+            g["s1"], g["ks1"] = _lib.i64_array(sh1)
+            self._groups.append(g)
 
     @property
     def n(self):
         return int(np.prod(self.out_shape))
 
     def cost_of_multiply(self):
-        return sum(stage3_multiply_cost(self.s0_shape, self.s1_shape, self.d, io < 0) for _, _, io in self.terms)
+        return sum(stage3_multiply_cost(self.s2_0[i0].shape, self.s2_1[i1].shape, self.d, io < 0)
+                   for i0, i1, io in self.terms)
 
     def cost_of_formMatrix(self):
-        return len(self.terms) * stage3_form_matrix_cost(self.s0_shape, self.s1_shape, self.d)
+        return sum(stage3_form_matrix_cost(self.s2_0[i0].shape, self.s2_1[i1].shape, self.d)
+                   for i0, i1, _ in self.terms)
+
+    # -- tensor-core (split-BF16) path --------------------------------------
+    def _tc_plan(self, g):
+        """Packed split-BF16 copies of this class's S2 tags (built once)."""
+        if "plan" not in g:
+            lib = _lib.load()
+            nbytes = lib.carc_stage3_tc_plan_size(g["s0"], g["s1"], g["n0"], g["n1"])
+            if nbytes < 0:
+                _lib.check(_lib.CARC_BAD_SHAPE)
+            g["plan"] = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
+            _lib.call("carc_stage3_tc_prepare", g["s0"], g["s1"], g["p0"], g["n0"], g["p1"], g["n1"],
+                      ctypes.c_void_p(g["plan"].data_ptr()), nbytes, current_stream_handle())
+        return g["plan"]
+
+    def _status(self):
+        if not hasattr(self, "_tc_status"):
+            self._tc_status = torch.zeros((), dtype=torch.int32, device=self.device)
+        return self._tc_status
+
+    def check_status(self):
+        """Raise if a tensor-core pipeline wait timed out in an earlier call (syncs)."""
+        if hasattr(self, "_tc_status") and int(self._tc_status.item()) != 0:
+            raise _lib.CarcError(_lib.CARC_NOT_CONVERGED, "tensor-core pipeline wait timed out")
+
+    def apply_tc(self, x, y=None, nvec=1, accumulate=False):
+        """y = op . x on the tensor cores (split-BF16 operands, ~1e-5 relative)."""
+        lib = _lib.load()
+        x = x.contiguous()
+        if y is None:
+            y = torch.empty((nvec,) + self.out_shape if nvec > 1 else self.out_shape, dtype=CDT, device=x.device)
+        if not self._groups:
+            if not accumulate:
+                _lib.call("carc_zfill", y.numel(), 0.0, 0.0, ctypes.c_void_p(y.data_ptr()), current_stream_handle())
+            return y
+        st = self._status()
+        for gi, g in enumerate(self._groups):
+            plan = self._tc_plan(g)
+            ws_bytes = lib.carc_stage3_matvec_tc_workspace_size(g["s0"], g["s1"], self.d, len(g["terms"]), nvec)
+            if ws_bytes < 0:
+                _lib.check(_lib.CARC_BAD_SHAPE)
+            ws = engine.Workspace.get(ws_bytes, x.device)
+            _lib.call("carc_stage3_matvec_tc", g["s0"], g["s1"], self.d, ctypes.c_void_p(plan.data_ptr()), g["n0"],
+                      g["n1"], self._po, len(self.ops), g["pt"], len(g["terms"]), ctypes.c_void_p(x.data_ptr()),
+                      ctypes.c_void_p(y.data_ptr()), nvec, int(bool(accumulate or gi > 0)),
+                      ctypes.c_void_p(ws.data_ptr()), ws_bytes, ctypes.c_void_p(st.data_ptr()),
+                      current_stream_handle())
+        return y
+
+    def form_matrix_tc(self, out=None, accumulate=False):
+        """H on the tensor cores (split-BF16 operands, ~1e-5 relative)."""
+        lib = _lib.load()
+        n_r, n_c = self.n, int(np.prod(self.in_shape))
+        if out is None:
+            out = torch.empty((n_r, n_c), dtype=CDT, device=self.device)
+        if not self._groups:
+            if not accumulate:
+                _lib.call("carc_zfill", out.numel(), 0.0, 0.0, ctypes.c_void_p(out.data_ptr()), current_stream_handle())
+            return out
+        st = self._status()
+        for gi, g in enumerate(self._groups):
+            ws_bytes = lib.carc_stage3_form_matrix_tc_workspace_size(g["s0"], g["s1"], self.d, len(g["terms"]))
+            if ws_bytes < 0:
+                _lib.check(_lib.CARC_BAD_SHAPE)
+            ws = engine.Workspace.get(ws_bytes, self.device)
+            _lib.call("carc_stage3_form_matrix_tc", g["s0"], g["s1"], self.d, g["p0"], g["n0"], g["p1"], g["n1"],
+                      self._po, len(self.ops), g["pt"], len(g["terms"]), ctypes.c_void_p(out.data_ptr()),
+                      int(bool(accumulate or gi > 0)), ctypes.c_void_p(ws.data_ptr()), ws_bytes,
+                      ctypes.c_void_p(st.data_ptr()), current_stream_handle())
+        return out
 
     def apply(self, x, y=None, nvec=1, accumulate=False):
         """y = op . x for nvec stacked centers (torch tensors, contiguous)."""
@@ -242,14 +366,19 @@ class Stage3Operator:
         x = x.contiguous()
         if y is None:
             y = torch.empty((nvec,) + self.out_shape if nvec > 1 else self.out_shape, dtype=CDT, device=x.device)
-        ws_bytes = lib.carc_stage3_matvec_f64_workspace_size(self._s0, self._s1, self.d, len(self.terms), nvec)
-        if ws_bytes < 0:
-            _lib.check(_lib.CARC_BAD_SHAPE)
-        ws = engine.Workspace.get(ws_bytes, x.device)
-        _lib.call("carc_stage3_matvec_f64", self._s0, self._s1, self.d, self._p0, len(self.s2_0), self._p1,
-                  len(self.s2_1), self._po, len(self.ops), self._pt, len(self.terms), ctypes.c_void_p(x.data_ptr()),
-                  ctypes.c_void_p(y.data_ptr()), nvec, int(bool(accumulate)), ctypes.c_void_p(ws.data_ptr()),
-                  ws_bytes, current_stream_handle())
+        if not self._groups:
+            if not accumulate:
+                _lib.call("carc_zfill", y.numel(), 0.0, 0.0, ctypes.c_void_p(y.data_ptr()), current_stream_handle())
+            return y
+        for gi, g in enumerate(self._groups):
+            ws_bytes = lib.carc_stage3_matvec_f64_workspace_size(g["s0"], g["s1"], self.d, len(g["terms"]), nvec)
+            if ws_bytes < 0:
+                _lib.check(_lib.CARC_BAD_SHAPE)
+            ws = engine.Workspace.get(ws_bytes, x.device)
+            _lib.call("carc_stage3_matvec_f64", g["s0"], g["s1"], self.d, g["p0"], g["n0"], g["p1"], g["n1"],
+                      self._po, len(self.ops), g["pt"], len(g["terms"]), ctypes.c_void_p(x.data_ptr()),
+                      ctypes.c_void_p(y.data_ptr()), nvec, int(bool(accumulate or gi > 0)),
+                      ctypes.c_void_p(ws.data_ptr()), ws_bytes, current_stream_handle())
         return y
 
     def __call__(self, v):
@@ -264,13 +393,19 @@ class Stage3Operator:
         n_c = int(np.prod(self.in_shape))
         if out is None:
             out = torch.empty((n_r, n_c), dtype=CDT, device=self.device)
-        ws_bytes = lib.carc_stage3_form_matrix_f64_workspace_size(self._s0, self._s1, self.d, len(self.terms))
-        if ws_bytes < 0:
-            _lib.check(_lib.CARC_BAD_SHAPE)
-        ws = engine.Workspace.get(ws_bytes, self.device)
-        _lib.call("carc_stage3_form_matrix_f64", self._s0, self._s1, self.d, self._p0, len(self.s2_0), self._p1,
-                  len(self.s2_1), self._po, len(self.ops), self._pt, len(self.terms), ctypes.c_void_p(out.data_ptr()),
-                  int(bool(accumulate)), ctypes.c_void_p(ws.data_ptr()), ws_bytes, current_stream_handle())
+        if not self._groups:
+            if not accumulate:
+                _lib.call("carc_zfill", out.numel(), 0.0, 0.0, ctypes.c_void_p(out.data_ptr()), current_stream_handle())
+            return out
+        for gi, g in enumerate(self._groups):
+            ws_bytes = lib.carc_stage3_form_matrix_f64_workspace_size(g["s0"], g["s1"], self.d, len(g["terms"]))
+            if ws_bytes < 0:
+                _lib.check(_lib.CARC_BAD_SHAPE)
+            ws = engine.Workspace.get(ws_bytes, self.device)
+            _lib.call("carc_stage3_form_matrix_f64", g["s0"], g["s1"], self.d, g["p0"], g["n0"], g["p1"], g["n1"],
+                      self._po, len(self.ops), g["pt"], len(g["terms"]), ctypes.c_void_p(out.data_ptr()),
+                      int(bool(accumulate or gi > 0)), ctypes.c_void_p(ws.data_ptr()), ws_bytes,
+                      current_stream_handle())
         return out
 
     def formMatrix(self):

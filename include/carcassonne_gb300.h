@@ -136,6 +136,56 @@ int64_t carc_stage3_matvec_f64_workspace_size(const int64_t* s0_shape, const int
                                               int64_t d, int32_t n_terms, int32_t nvec);
 
 /*
+ * The strided complex contraction of carc_contract_desc (one pair, no
+ * grouping) on the tensor cores: operands split into BF16 hi+lo parts
+ * (~16 significant bits), one BF16 tcgen05 GEMM with FP32 accumulation in
+ * TMEM (TMA-fed, 128-byte swizzled shared memory), partial products summed
+ * in FP64.  Relative error ~1e-5 of the operands' scale.  ksplit splits K
+ * across CTAs.  *status (device int32) is nonzero if a pipeline wait timed out.
+ * Replaces NDArrayData.contractWith (data/__init__.py:157-159) where the
+ * caller accepts split-BF16 accuracy.
+ */
+int carc_zcontract_tc(const carc_contract_desc* desc, const void* A, const void* B, void* C,
+                      double alpha_re, double alpha_im, int32_t accumulate, int32_t ksplit,
+                      void* workspace, int64_t workspace_bytes, void* status, void* stream);
+int64_t carc_zcontract_tc_workspace_size(const carc_contract_desc* desc, int32_t ksplit);
+/* The raw tensor-core GEMM: out[z][m][n] = sum over K-split z of A[m,:].B[n,:]
+ * (BF16, K-major, M % 128 == 0, K % 64 == 0, N % 16 == 0, FP32 out with row
+ * pitch ld_out, ksplit partial planes of M*ld_out floats). */
+int carc_gemm_bf16_tn(const void* A, int32_t M, const void* B, int32_t N, int32_t K, float* out,
+                      int64_t ld_out, int32_t ksplit, void* status, void* stream);
+
+/*
+ * The stage-3 operator on the tensor cores (split-BF16 operands, FP32
+ * accumulation in TMEM, FP64 reductions; relative error ~1e-5).
+ * carc_stage3_tc_prepare packs the S2 tags once into a caller-provided plan
+ * buffer of carc_stage3_tc_plan_size bytes (the many matvecs of a solve reuse
+ * it); carc_stage3_matvec_tc then applies the operator exactly as
+ * carc_stage3_matvec_f64 does (same terms, x, y layout), and
+ * carc_stage3_form_matrix_tc forms H as carc_stage3_form_matrix_f64 does.
+ * *status (device int32) is nonzero if a pipeline wait timed out.
+ * Replaces formDenseStage3 / formNormalizationStage3 multiply and formMatrix
+ * (tensors/_2d/dense.py:114-203) where split-BF16 accuracy is accepted.
+ */
+int64_t carc_stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, int32_t n0, int32_t n1);
+int carc_stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape,
+                           const void* const* s0_ptrs, int32_t n0, const void* const* s1_ptrs, int32_t n1,
+                           void* plan, int64_t plan_bytes, void* stream);
+int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan,
+                          int32_t n0, int32_t n1, const void* const* op_ptrs, int32_t nop,
+                          const int32_t* terms, int32_t n_terms, const void* x, void* y, int32_t nvec,
+                          int32_t accumulate, void* workspace, int64_t workspace_bytes, void* status, void* stream);
+int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                                             int32_t n_terms, int32_t nvec);
+int carc_stage3_form_matrix_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                               const void* const* s0_ptrs, int32_t n0, const void* const* s1_ptrs, int32_t n1,
+                               const void* const* op_ptrs, int32_t nop, const int32_t* terms, int32_t n_terms,
+                               void* H, int32_t accumulate, void* workspace, int64_t workspace_bytes,
+                               void* status, void* stream);
+int64_t carc_stage3_form_matrix_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
+                                                  int32_t n_terms);
+
+/*
  * carc_stage3_matvec_f64 for callers that cannot allocate device memory while
  * they run (a host application that owns the whole GPU and forbids library
  * allocations, or a loop that cannot afford the synchronisation cudaMalloc
@@ -193,6 +243,12 @@ int64_t carc_zgesvd_jacobi_workspace_size(int32_t m, int32_t n, int32_t batch);
  */
 int carc_normalize_axis_finish(int32_t n, const void* S, const void* Vh, double dont_recip_under,
                                int32_t sqrt_svals, void* out_a, void* out_b, void* stream);
+
+/* Economic QR A = Q R of a small m x n matrix (m >= n), row-major: modified
+ * Gram-Schmidt with reorthogonalisation, R with a non-negative real diagonal.
+ * Replaces NDArrayData.qr(mode='economic') (data/__init__.py:314-317) as used
+ * by newEnlargener (:43-50). */
+int carc_zgeqr_economic(int32_t m, int32_t n, const void* A, void* Q, void* R, void* stream);
 
 /*
  * Batched Hermitian eigensolver (parallel cyclic Jacobi), n <= 512:

@@ -164,13 +164,17 @@ def operators():
 
 
 def bond_system(op, D_, seed):
-    """Unit corners and identity bond boundaries (a positive-definite norm
-    environment) of bond dimension D_ around a random center."""
+    """Unit corners and random Hermitian positive-definite bond boundaries of
+    bond dimension D_ around a random center (a generic, non-degenerate start)."""
     rng = np.random.default_rng(seed)
     d = next(iter(op.values())).shape[0]
     corners = tuple({rsparse.Identity(): NDArrayData.newTrivial((1,) * 6, dtype=np.complex128)} for _ in range(4))
-    eye = np.eye(D_, dtype=np.complex128).reshape((1,) * 6 + (D_, D_))
-    sides = tuple({rsparse.Identity(): NDArrayData(eye.copy())} for _ in range(4))
+    sides = []
+    for _ in range(4):
+        a = rng.standard_normal((D_, D_)) + 1j * rng.standard_normal((D_, D_))
+        bond = a @ a.conj().T + 0.5 * np.eye(D_)  # Hermitian positive definite, generic
+        sides.append({rsparse.Identity(): NDArrayData(bond.reshape((1,) * 6 + (D_, D_)).astype(np.complex128))})
+    sides = tuple(sides)
     st = rng.standard_normal((D_,) * 4 + (d,)).astype(np.complex128)
     st /= np.linalg.norm(st)
     return System(corners, sides, NDArrayData(st), op)

@@ -1,0 +1,113 @@
+"""The tcgen05 tensor-core path: the raw BF16 GEMM against an FP32 torch
+reference of the same BF16 inputs, and the split-BF16 complex contraction
+against numpy complex128 (tolerance 5e-5 of the result's scale: operands are
+carried with ~16 significant bits)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _vp(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from carcassonne_gb300 import _lib
+    return _lib
+
+
+@pytest.mark.parametrize("M,N,K,ksplit", [(128, 16, 64, 1), (256, 64, 256, 1), (128, 256, 512, 3),
+                                          (384, 48, 192, 2), (128, 128, 1024, 4)])
+def test_raw_bf16_gemm(lib, M, N, K, ksplit):
+    L = lib.load()
+    g = torch.Generator().manual_seed(M + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    ks = ksplit
+    out = torch.full((ks, M, N), float("nan"), dtype=torch.float32, device="cuda")
+    status = torch.zeros((), dtype=torch.int32, device="cuda")
+    lib.check(L.carc_gemm_bf16_tn(_vp(A), M, _vp(B), N, K, ctypes.cast(ctypes.c_void_p(out.data_ptr()),
+                                  ctypes.c_void_p), N, ks, _vp(status), _stream()))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    ref = A.float() @ B.float().T
+    got = out.sum(0)
+    err = (got - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 1e-5, err
+
+
+def _desc_matrix(lib, M, N, K, a_strides, b_strides):
+    d = lib.ContractDesc()
+    d.nm, d.nn, d.nk = 1, 1, 1
+    d.m_ext[0], d.n_ext[0], d.k_ext[0] = M, N, K
+    d.a_m[0], d.a_k[0] = a_strides
+    d.b_n[0], d.b_k[0] = b_strides
+    d.c_m[0], d.c_n[0] = N, 1
+    return d
+
+
+@pytest.mark.parametrize("M,N,K,transpose_b,ksplit", [(32, 16, 16, False, 1), (100, 70, 300, True, 2),
+                                                      (256, 256, 1024, False, 4), (5, 3, 7, True, 1)])
+def test_split_bf16_complex_contraction(lib, M, N, K, transpose_b, ksplit):
+    L = lib.load()
+    rng = np.random.default_rng(M * N + K)
+    a = rng.standard_normal((M, K)) + 1j * rng.standard_normal((M, K))
+    b = rng.standard_normal((N, K)) + 1j * rng.standard_normal((N, K))
+    A = torch.as_tensor(a).cuda()
+    if transpose_b:
+        Bt = torch.as_tensor(np.ascontiguousarray(b.T)).cuda()  # stored (K, N)
+        bstr = (1, N)
+        Bp = Bt
+    else:
+        Bp = torch.as_tensor(b).cuda()
+        bstr = (K, 1)
+    d = _desc_matrix(lib, M, N, K, (K, 1), bstr)
+    C = torch.zeros((M, N), dtype=torch.complex128, device="cuda")
+    ws_bytes = L.carc_zcontract_tc_workspace_size(ctypes.byref(d), ksplit)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    status = torch.zeros((), dtype=torch.int32, device="cuda")
+    lib.check(L.carc_zcontract_tc(ctypes.byref(d), _vp(A), _vp(Bp), _vp(C), 1.0, 0.0, 0, ksplit, _vp(ws), ws_bytes,
+                                  _vp(status), _stream()))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    ref = a @ b.T
+    err = np.abs(C.cpu().numpy() - ref).max() / np.abs(ref).max()
+    assert err < 5e-5, err
+
+
+@pytest.mark.parametrize("D,c_ket,c_bra,nvec", [(2, 2, 2, 1), (2, 4, 2, 3), (4, 8, 4, 8), (3, 3, 3, 2)])
+def test_stage3_tensorcore_matches_fp64(lib, D, c_ket, c_bra, nvec):
+    from carcassonne_gb300 import workloads
+    from carcassonne_gb300.tensors._2d import sparse as tsp
+    corners_a, sides_a, op_a = workloads.matvec_problem_arrays(D=D, c_ket=c_ket, c_bra=c_bra, seed=D + c_ket)
+    corners, sides, op = workloads.to_device(corners_a, sides_a, op_a)
+    H, N = tsp.formExpectationAndNormalizationMultipliers(corners, sides, op)
+    for m in (H, N):
+        opr = m.operator if hasattr(m, "operator") else None
+        if opr is None:
+            continue
+        rng = np.random.default_rng(nvec)
+        shape = (nvec,) + opr.in_shape
+        x = torch.as_tensor(rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).cuda()
+        y64 = opr.apply(x, nvec=nvec).cpu().numpy()
+        ytc = opr.apply_tc(x, nvec=nvec).cpu().numpy()
+        opr.check_status()
+        err = np.abs(ytc - y64).max() / np.abs(y64).max()
+        assert err < 5e-5, err
+        if opr.n <= 1296:
+            H64 = opr.form_matrix().cpu().numpy()
+            Htc = opr.form_matrix_tc().cpu().numpy()
+            opr.check_status()
+            err = np.abs(Htc - H64).max() / np.abs(H64).max()
+            assert err < 5e-5, err
