@@ -217,15 +217,19 @@ int carc_gemm_bf16_tn(const void* A, int32_t M, const void* B, int32_t N, int32_
   return gemm_bf16_tn(A, M, B, N, K, out, ld_out, ksplit, static_cast<int*>(status), as_stream(stream));
 }
 
-int64_t carc_stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, int32_t n0, int32_t n1) {
-  if (!s0_shape || !s1_shape) return -1;
-  return stage3_tc_plan_size(s0_shape, s1_shape, n0, n1);
+int64_t carc_stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, const int32_t* terms,
+                                 int32_t n_terms) {
+  if (!s0_shape || !s1_shape || (n_terms > 0 && !terms)) return -1;
+  return stage3_tc_plan_size(s0_shape, s1_shape, terms, n_terms);
 }
 
 int carc_stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const void* const* s0_ptrs, int32_t n0,
-                           const void* const* s1_ptrs, int32_t n1, void* plan, int64_t plan_bytes, void* stream) {
-  if (!s0_shape || !s1_shape || !s0_ptrs || !s1_ptrs || !plan) return fail(CARC_BAD_ARG, "carc_stage3_tc_prepare: NULL");
-  return stage3_tc_prepare(s0_shape, s1_shape, s0_ptrs, n0, s1_ptrs, n1, plan, plan_bytes, as_stream(stream));
+                           const void* const* s1_ptrs, int32_t n1, const int32_t* terms, int32_t n_terms, void* plan,
+                           int64_t plan_bytes, void* stream) {
+  if (!s0_shape || !s1_shape || !s0_ptrs || !s1_ptrs || !plan || (n_terms > 0 && !terms))
+    return fail(CARC_BAD_ARG, "carc_stage3_tc_prepare: NULL");
+  return stage3_tc_prepare(s0_shape, s1_shape, s0_ptrs, n0, s1_ptrs, n1, terms, n_terms, plan, plan_bytes,
+                           as_stream(stream));
 }
 
 int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int32_t n0,
@@ -239,9 +243,9 @@ int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int6
 }
 
 int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
-                                             int32_t n_terms, int32_t nvec) {
-  if (!s0_shape || !s1_shape) return -1;
-  return stage3_matvec_tc_ws(s0_shape, s1_shape, d, n_terms, nvec);
+                                             const int32_t* terms, int32_t n_terms, int32_t nvec) {
+  if (!s0_shape || !s1_shape || (n_terms > 0 && !terms)) return -1;
+  return stage3_matvec_tc_ws(s0_shape, s1_shape, d, terms, n_terms, nvec);
 }
 
 int carc_stage3_form_matrix_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* const* s0_ptrs,

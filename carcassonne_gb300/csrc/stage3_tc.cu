@@ -2,16 +2,20 @@
 // accumulation in TMEM, FP64 reductions):
 //
 //  matvec  y[v] = sum_t S2_0[i0_t] (x) S2_1[i1_t] (x) O[io_t] . x[v]
-//    per term:  step A  W[(x0,x1,l0,l1),(v,k2,k3,p)] = sum_{k0,k1} S2_0 . Vin
-//               (one tcgen05 GEMM; its FP32 partials are folded and re-split
-//               straight into the packed operand layout step B reads),
-//               step B  y^T[(l2,l3),(v,l0,l1,p)] += sum_{x0,x1,k2,k3} S2_1 . W
-//               (split-K tcgen05 GEMM; partial planes of all terms summed in FP64)
-//  matrix  H = sum_g G_g (x) O_g,  G_g = sum_{t in g} S2_0[i0_t] . S2_1[i1_t] over x,
+//    terms are grouped by their S2_1 tag g;
+//    step A (one tcgen05 GEMM per group, terms concatenated along K):
+//      W_g[(x0,x1,l0,l1),(v,k2,k3,p)] = sum_{t in g} sum_{k0,k1} S2_0[i0_t] . Vin_t
+//      whose epilogue folds the (hi,lo) and (re,im) rows and writes W_g split
+//      straight into region g of step B's packed operand;
+//    step B (one split-K tcgen05 GEMM over all groups, concatenated along K):
+//      y^T[(l2,l3),(v,l0,l1,p)] = sum_g sum_{x0,x1,k2,k3} S2_1[g] . W_g,
+//      split planes summed in FP64 by a two-level coalesced reduction.
+//  matrix  H = sum_o G_o (x) O_o,  G_o = sum_{t in o} S2_0[i0_t] . S2_1[i1_t] over x,
 //          terms of one operator group concatenated along K in one GEMM.
 //
-// The S2 tensors are packed once per operator ("plan"): the many matvecs of a
-// solve reuse them.  Index convention as in stage3.cu (tensors/_2d/dense.py:114-195).
+// The S2 tensors are packed once per operator ("plan", in term-group order):
+// the many matvecs of a solve reuse them.  Index convention as in stage3.cu
+// (tensors/_2d/dense.py:114-195).
 #include "common.cuh"
 #include "contract.cuh"
 #include "stage3.cuh"
@@ -64,24 +68,53 @@ int s3_shapes(const int64_t* a, const int64_t* b, int64_t d, S3* s) {
   return CARC_OK;
 }
 
-// packed operand geometry of the matvec
+// The matvec's term structure: terms sharing their S2_1 tag (i1) form one
+// group; a group's step-A GEMM concatenates its terms along K, so it yields
+// sum_t S2_0[i0_t] . Vin_t directly, and the single step-B GEMM concatenates
+// the groups along K.
+struct TermGroups {
+  std::vector<int> i1;                  // S2_1 tag of each group
+  std::vector<std::vector<int>> terms;  // term indices of each group
+  int max_terms = 0;
+};
+
+TermGroups group_terms(const int32_t* terms, int n_terms) {
+  TermGroups g;
+  for (int t = 0; t < n_terms; ++t) {
+    const int i1 = terms[3 * t + 1];
+    int k = -1;
+    for (size_t q = 0; q < g.i1.size(); ++q)
+      if (g.i1[q] == i1) k = (int)q;
+    if (k < 0) {
+      k = (int)g.i1.size();
+      g.i1.push_back(i1);
+      g.terms.emplace_back();
+    }
+    g.terms[k].push_back(t);
+  }
+  for (auto& v : g.terms) g.max_terms = std::max(g.max_terms, (int)v.size());
+  return g;
+}
+
 struct Geo {
-  int64_t rowsA_a, kpA;   // step A: S2_0 as A operand (rows 4*(x0 x1 l0 l1)), K' over (k0,k1)
-  int64_t rowsB_a, kpB;   // step B: S2_1 as A operand (rows 4*(l2 l3)), K' over (x0,x1,k2,k3)
-  int64_t rowsA_b;        // step A: Vin as B operand (rows nvec*k2*k3*d)
-  int64_t rowsB_b;        // step B: W as B operand (rows nvec*l0*l1*d)
-  int64_t kcA, kcB;       // complex K of the two steps
+  int64_t MA, NA;         // step A: complex rows (x0 x1 l0 l1) / columns (nvec k2 k3 d)
+  int64_t rowsA_a, regA;  // packed rows of S2_0 (4 MA), K region per term (4 k0 k1)
+  int64_t rowsA_b;        // packed rows of Vin
+  int64_t rowsB_a, regB;  // step B: packed rows of S2_1 (4 l2 l3), K region per group (4 x0 x1 k2 k3)
+  int64_t rowsB_b;        // packed rows of W (nvec l0 l1 d)
+  int64_t kcB;
 };
 
 Geo geometry(const S3& s, int nvec) {
   Geo g;
-  g.kcA = s.k0 * s.k1;
+  g.MA = s.x0 * s.x1 * s.l0 * s.l1;
+  g.NA = (int64_t)nvec * s.k2 * s.k3 * s.d;
+  g.rowsA_a = round_up(4 * g.MA, 128);
+  g.regA = round_up(4 * s.k0 * s.k1, 64);
+  g.rowsA_b = round_up(g.NA, 16);
   g.kcB = s.x0 * s.x1 * s.k2 * s.k3;
-  g.rowsA_a = round_up(4 * s.x0 * s.x1 * s.l0 * s.l1, 128);
-  g.kpA = round_up(4 * g.kcA, 64);
   g.rowsB_a = round_up(4 * s.l2 * s.l3, 128);
-  g.kpB = round_up(4 * g.kcB, 64);
-  g.rowsA_b = round_up((int64_t)nvec * s.k2 * s.k3 * s.d, 16);
+  g.regB = round_up(4 * g.kcB, 64);
   g.rowsB_b = round_up((int64_t)nvec * s.l0 * s.l1 * s.d, 16);
   return g;
 }
@@ -118,7 +151,7 @@ ZView view_s2_1_stepB(const S3& s, const void* base) {
 
 // Vin[vec][k0][k1][k2][k3][p] as a B operand: rows (vec,k2,k3,p), k (k0,k1)
 ZView view_vin(const S3& s, int nvec, const void* base) {
-  const int64_t p1 = 1, k3 = s.d, k2 = s.k3 * k3, k1 = s.k2 * k2, k0 = s.k1 * k1, vec = s.k0 * k0;
+  const int64_t k3 = s.d, k2 = s.k3 * k3, k1 = s.k2 * k2, k0 = s.k1 * k1, vec = s.k0 * k0;
   ZView v;
   memset(&v, 0, sizeof(v));
   v.base = base;
@@ -126,63 +159,26 @@ ZView view_vin(const S3& s, int nvec, const void* base) {
   v.r_ext[0] = nvec; v.r_str[0] = vec;
   v.r_ext[1] = s.k2; v.r_str[1] = k2;
   v.r_ext[2] = s.k3; v.r_str[2] = k3;
-  v.r_ext[3] = s.d; v.r_str[3] = p1;
+  v.r_ext[3] = s.d; v.r_str[3] = 1;
   v.nk = 2;
   v.k_ext[0] = s.k0; v.k_str[0] = k0;
   v.k_ext[1] = s.k1; v.k_str[1] = k1;
   return v;
 }
 
-// Fold the step-A partials (rows 4m + 2c + s, column n) into complex W[m, n]
-// and write it split into the packed B operand of step B:
-//   m = (x0,x1,l0,l1), n = (vec,k2,k3,p)  ->  row (vec,l0,l1,p), k (x0,x1,k2,k3).
-struct FoldParams {
-  int64_t x0, x1, l0, l1, nvec, k2, k3, d;
-  int64_t ld, kcB, kpB, M;
-};
-
-__global__ void fold_pack_w_kernel(const float* __restrict__ P, __nv_bfloat16* __restrict__ W,
-                                   const __grid_constant__ FoldParams f) {
-  const int64_t N = f.nvec * f.k2 * f.k3 * f.d;
-  const int64_t total = f.M * N;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t m = t / N, n = t % N;
-    const float* b = P + (4 * m) * f.ld + n;
-    const double re = (double)b[0] + (double)b[f.ld];
-    const double im = (double)b[2 * f.ld] + (double)b[3 * f.ld];
-    // m -> (x0,x1,l0,l1) ; n -> (vec,k2,k3,p)
-    int64_t r = m;
-    const int64_t l1 = r % f.l1; r /= f.l1;
-    const int64_t l0 = r % f.l0; r /= f.l0;
-    const int64_t x1 = r % f.x1; r /= f.x1;
-    const int64_t x0 = r;
-    int64_t q = n;
-    const int64_t p = q % f.d; q /= f.d;
-    const int64_t k3 = q % f.k3; q /= f.k3;
-    const int64_t k2 = q % f.k2; q /= f.k2;
-    const int64_t vec = q;
-    const int64_t row = ((vec * f.l0 + l0) * f.l1 + l1) * f.d + p;
-    const int64_t kk = ((x0 * f.x1 + x1) * f.k2 + k2) * f.k3 + k3;
-    const float fr = (float)re, fi = (float)im;
-    const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hi = __float2bfloat16_rn(fi);
-    const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
-    const __nv_bfloat16 li = __float2bfloat16_rn(fi - __bfloat162float(hi));
-    __nv_bfloat16* rowp = W + row * f.kpB;
-    *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * kk) = __halves2bfloat162(hr, hi);
-    *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * f.kcB + 2 * kk) = __halves2bfloat162(lr, li);
-  }
-}
-
-// zero the rows [r0, r1) and the K padding [4 kc, kp) of the packed W
+// zero the padding of the packed W: rows >= rows_valid, and per region the
+// columns [4 kc, reg) (the folding epilogue writes only the valid entries)
 __global__ void clear_w_padding_kernel(__nv_bfloat16* __restrict__ W, int64_t rows_valid, int64_t rows_total,
-                                       int64_t kc4, int64_t kp) {
-  const int64_t pad = kp - kc4;
-  const int64_t t1 = rows_valid * pad, t2 = (rows_total - rows_valid) * kp;
+                                       int64_t kc4, int64_t reg, int64_t n_reg) {
+  const int64_t kp = reg * n_reg, pad = reg - kc4;
+  const int64_t t1 = rows_valid * n_reg * pad, t2 = (rows_total - rows_valid) * kp;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < t1 + t2; t += (int64_t)gridDim.x * blockDim.x) {
-    if (t < t1)
-      W[(t / pad) * kp + kc4 + t % pad] = __float2bfloat16_rn(0.f);
-    else
+    if (t < t1) {
+      const int64_t row = t / (n_reg * pad), rem = t % (n_reg * pad);
+      W[row * kp + (rem / pad) * reg + kc4 + rem % pad] = __float2bfloat16_rn(0.f);
+    } else {
       W[rows_valid * kp + (t - t1)] = __float2bfloat16_rn(0.f);
+    }
   }
 }
 
@@ -197,51 +193,72 @@ int choose_ksplit(int64_t tiles, int64_t kp) {
 
 int bn_for(int64_t n) { return n % 256 == 0 ? 256 : n % 128 == 0 ? 128 : n % 64 == 0 ? 64 : n % 32 == 0 ? 32 : 16; }
 
+// plan layout: [per group g: S2_0 step-A operand, rowsA_a x (regA * |T_g|)] [S2_1 step-B operand, rowsB_a x (regB * G)]
+int64_t plan_bytes_for(const Geo& g1, const TermGroups& tg) {
+  int64_t b = 0;
+  for (auto& v : tg.terms) b += a256(g1.rowsA_a * g1.regA * (int64_t)v.size() * 2);
+  b += a256(g1.rowsB_a * g1.regB * (int64_t)tg.i1.size() * 2);
+  return b;
+}
+
 }  // namespace
 
-int64_t stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, int n0, int n1) {
+int64_t stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, const int32_t* terms, int n_terms) {
   S3 s;
   if (s3_shapes(s0_shape, s1_shape, 1, &s) != CARC_OK) return -1;
-  Geo g = geometry(s, 1);
-  return (int64_t)n0 * a256(g.rowsA_a * g.kpA * 2) + (int64_t)n1 * a256(g.rowsB_a * g.kpB * 2);
+  if (n_terms < 1) return 256;
+  return plan_bytes_for(geometry(s, 1), group_terms(terms, n_terms));
 }
 
 int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const void* const* s0_ptrs, int n0,
-                      const void* const* s1_ptrs, int n1, void* plan, int64_t plan_bytes, cudaStream_t stream) {
+                      const void* const* s1_ptrs, int n1, const int32_t* terms, int n_terms, void* plan,
+                      int64_t plan_bytes, cudaStream_t stream) {
   S3 s;
   CARC_RETURN_IF(s3_shapes(s0_shape, s1_shape, 1, &s));
-  if (plan_bytes < stage3_tc_plan_size(s0_shape, s1_shape, n0, n1)) return fail(CARC_BAD_ARG, "stage3 tc: plan too small");
-  Geo g = geometry(s, 1);
+  if (n_terms < 1) return CARC_OK;
+  for (int t = 0; t < n_terms; ++t)
+    if (terms[3 * t] < 0 || terms[3 * t] >= n0 || terms[3 * t + 1] < 0 || terms[3 * t + 1] >= n1)
+      return fail(CARC_BAD_ARG, "stage3 tc: term %d out of range", t);
+  const TermGroups tg = group_terms(terms, n_terms);
+  const Geo g = geometry(s, 1);
+  if (plan_bytes < plan_bytes_for(g, tg)) return fail(CARC_BAD_ARG, "stage3 tc: plan too small");
   char* p = static_cast<char*>(plan);
-  for (int i = 0; i < n0; ++i) {
-    CARC_RETURN_IF(pack_operand(view_s2_0_stepA(s, s0_ptrs[i]), 0, p, g.rowsA_a, g.kpA, stream));
-    p += a256(g.rowsA_a * g.kpA * 2);
+  for (size_t q = 0; q < tg.terms.size(); ++q) {
+    const int64_t kp = g.regA * (int64_t)tg.terms[q].size();
+    for (size_t j = 0; j < tg.terms[q].size(); ++j)
+      CARC_RETURN_IF(pack_operand_region(view_s2_0_stepA(s, s0_ptrs[terms[3 * tg.terms[q][j]]]), 0, p, g.rowsA_a, kp,
+                                         (int64_t)j * g.regA, g.regA, stream));
+    p += a256(g.rowsA_a * kp * 2);
   }
-  for (int i = 0; i < n1; ++i) {
-    CARC_RETURN_IF(pack_operand(view_s2_1_stepB(s, s1_ptrs[i]), 0, p, g.rowsB_a, g.kpB, stream));
-    p += a256(g.rowsB_a * g.kpB * 2);
-  }
+  const int64_t kpB = g.regB * (int64_t)tg.i1.size();
+  for (size_t q = 0; q < tg.i1.size(); ++q)
+    CARC_RETURN_IF(pack_operand_region(view_s2_1_stepB(s, s1_ptrs[tg.i1[q]]), 0, p, g.rowsB_a, kpB,
+                                       (int64_t)q * g.regB, g.regB, stream));
   return CARC_OK;
 }
 
 namespace {
 
 struct MvWs {
-  char* vop;      // n_ops x (nvec x nk4 x d) complex128
-  char* vin_pk;   // packed Vin (rowsA_b x kpA bf16)
-  float* pA;      // step A partials (rowsA_a x rowsA_b fp32)
-  char* w_pk;     // packed W (rowsB_b x kpB bf16)
-  float* pB;      // step B partials, n_terms * ksB planes (rowsB_a x rowsB_b)
+  char* vop;     // distinct operators applied to x, complex128
+  char* vin_pk;  // packed Vin regions of one group
+  char* w_pk;    // packed W of all groups (step-B operand)
+  float* pB;     // step-B split planes
+  char* red;     // reduction partial sums
   int ksB;
 };
 
-int64_t mv_layout(const S3& s, int nvec, int n_terms, MvWs* w, void* base) {
-  Geo g = geometry(s, nvec);
+int64_t mv_layout(const S3& s, int nvec, int n_terms, const TermGroups& tg, MvWs* w, void* base) {
+  const Geo g = geometry(s, nvec);
+  const int64_t kpB = g.regB * (int64_t)tg.i1.size();
   const int64_t tilesB = (g.rowsB_a / 128) * (g.rowsB_b / bn_for(g.rowsB_b));
-  const int ksB = gemm_effective_ksplit((int)g.kpB, choose_ksplit(tilesB, g.kpB));
+  const int ksB = gemm_effective_ksplit((int)kpB, choose_ksplit(tilesB, kpB));
   const int64_t nk4 = s.k0 * s.k1 * s.k2 * s.k3;
-  int64_t sizes[5] = {(int64_t)n_terms * nvec * nk4 * s.d * 16, g.rowsA_b * g.kpA * 2, g.rowsA_a * g.rowsA_b * 4,
-                      g.rowsB_b * g.kpB * 2, (int64_t)n_terms * ksB * g.rowsB_a * g.rowsB_b * 4};
+  const int64_t sizes[5] = {(int64_t)n_terms * nvec * nk4 * s.d * 16,
+                            g.rowsA_b * g.regA * (int64_t)tg.max_terms * 2,
+                            g.rowsB_b * kpB * 2,
+                            (int64_t)ksB * g.rowsB_a * g.rowsB_b * 4,
+                            reduce_partials2_workspace(s.l2 * s.l3, (int64_t)nvec * s.l0 * s.l1 * s.d, ksB)};
   char* p = static_cast<char*>(base);
   int64_t off = 0;
   char* ptrs[5];
@@ -252,9 +269,9 @@ int64_t mv_layout(const S3& s, int nvec, int n_terms, MvWs* w, void* base) {
   if (w) {
     w->vop = ptrs[0];
     w->vin_pk = ptrs[1];
-    w->pA = reinterpret_cast<float*>(ptrs[2]);
-    w->w_pk = ptrs[3];
-    w->pB = reinterpret_cast<float*>(ptrs[4]);
+    w->w_pk = ptrs[2];
+    w->pB = reinterpret_cast<float*>(ptrs[3]);
+    w->red = ptrs[4];
     w->ksB = ksB;
   }
   return off;
@@ -262,11 +279,12 @@ int64_t mv_layout(const S3& s, int nvec, int n_terms, MvWs* w, void* base) {
 
 }  // namespace
 
-int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int n_terms, int nvec) {
+int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const int32_t* terms,
+                            int n_terms, int nvec) {
   S3 s;
   if (s3_shapes(s0_shape, s1_shape, d, &s) != CARC_OK) return -1;
   if (n_terms < 1 || nvec < 1) return 0;
-  return mv_layout(s, nvec, n_terms, nullptr, nullptr);
+  return mv_layout(s, nvec, n_terms, group_terms(terms, n_terms), nullptr, nullptr);
 }
 
 int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int n0, int n1,
@@ -279,19 +297,20 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
     if (!accumulate) return fill_launch((int64_t)nvec * nl4 * d, make_double2(0, 0), y, stream);
     return CARC_OK;
   }
-  if (ws_bytes < stage3_matvec_tc_ws(s0_shape, s1_shape, d, n_terms, nvec))
-    return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
   for (int t = 0; t < n_terms; ++t) {
     int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
     if (i0 < 0 || i0 >= n0 || i1 < 0 || i1 >= n1 || io >= nop)
       return fail(CARC_BAD_ARG, "stage3 tc matvec: term %d out of range", t);
   }
-  Geo gA = geometry(s, 1);
-  Geo g = geometry(s, nvec);
+  const TermGroups tg = group_terms(terms, n_terms);
+  if (ws_bytes < mv_layout(s, nvec, n_terms, tg, nullptr, nullptr))
+    return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
+  const Geo g1 = geometry(s, 1);
+  const Geo g = geometry(s, nvec);
   MvWs w;
-  mv_layout(s, nvec, n_terms, &w, ws);
-  const char* planA = static_cast<const char*>(plan);
-  const char* planB = planA + (int64_t)n0 * a256(gA.rowsA_a * gA.kpA * 2);
+  mv_layout(s, nvec, n_terms, tg, &w, ws);
+  const int G = (int)tg.i1.size();
+  const int64_t kpB = g.regB * G;
   // operators applied to x (FP64, tiny): Vop_o[vec][k4][p] = sum_q O[p,q] x[vec][k4][q]
   std::map<int, int> op_slot;
   for (int t = 0; t < n_terms; ++t) {
@@ -312,43 +331,45 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
       CARC_RETURN_IF(gett_launch(dop, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, nullptr, 0, stream));
     }
   }
-  const int64_t MA = s.x0 * s.x1 * s.l0 * s.l1;
-  FoldParams fp;
-  fp.x0 = s.x0;
-  fp.x1 = s.x1;
-  fp.l0 = s.l0;
-  fp.l1 = s.l1;
-  fp.nvec = nvec;
-  fp.k2 = s.k2;
-  fp.k3 = s.k3;
-  fp.d = s.d;
-  fp.ld = g.rowsA_b;
-  fp.kcB = g.kcB;
-  fp.kpB = g.kpB;
-  fp.M = MA;
   const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
-  const int64_t planeB = g.rowsB_a * g.rowsB_b;
-  for (int t = 0; t < n_terms; ++t) {
-    const int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
-    const void* vin = io < 0 ? x : (const void*)(w.vop + (int64_t)op_slot[io] * nvec * nk4 * s.d * 16);
-    CARC_RETURN_IF(pack_operand(view_vin(s, nvec, vin), 1, w.vin_pk, g.rowsA_b, g.kpA, stream));
-    // step A: W = S2_0 . Vin  (single pass over K = k0 k1)
-    const char* a_op = planA + (int64_t)i0 * a256(gA.rowsA_a * gA.kpA * 2);
-    CARC_RETURN_IF(gemm_bf16_tn(a_op, (int)g.rowsA_a, w.vin_pk, (int)g.rowsA_b, (int)g.kpA, w.pA, g.rowsA_b, 1,
-                                status, stream));
-    clear_w_padding_kernel<<<grid_of(rows_valid_w * (g.kpB - 4 * g.kcB) + (g.rowsB_b - rows_valid_w) * g.kpB), 256, 0,
-                             stream>>>(reinterpret_cast<__nv_bfloat16*>(w.w_pk), rows_valid_w, g.rowsB_b, 4 * g.kcB,
-                                       g.kpB);
-    CARC_CHECK_LAUNCH();
-    fold_pack_w_kernel<<<grid_of(MA * nvec * s.k2 * s.k3 * s.d), 256, 0, stream>>>(
-        w.pA, reinterpret_cast<__nv_bfloat16*>(w.w_pk), fp);
-    CARC_CHECK_LAUNCH();
-    // step B: y^T += S2_1 . W   (split K over x0 x1 k2 k3)
-    const char* b_op = planB + (int64_t)i1 * a256(gA.rowsB_a * gA.kpB * 2);
-    CARC_RETURN_IF(gemm_bf16_tn(b_op, (int)g.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)g.kpB,
-                                w.pB + (int64_t)t * w.ksB * planeB, g.rowsB_b, w.ksB, status, stream));
+  clear_w_padding_kernel<<<grid_of(rows_valid_w * G * (g.regB - 4 * g.kcB) + (g.rowsB_b - rows_valid_w) * kpB), 256,
+                           0, stream>>>(reinterpret_cast<__nv_bfloat16*>(w.w_pk), rows_valid_w, g.rowsB_b,
+                                        4 * g.kcB, g.regB, G);
+  CARC_CHECK_LAUNCH();
+  // step A per group: W_g = sum_{t in g} S2_0[i0_t] . Vin_t, folded straight into region g of the step-B operand
+  const char* planA = static_cast<const char*>(plan);
+  for (int q = 0; q < G; ++q) {
+    const std::vector<int>& tl = tg.terms[q];
+    const int64_t kpA = g.regA * (int64_t)tl.size();
+    for (size_t j = 0; j < tl.size(); ++j) {
+      const int io = terms[3 * tl[j] + 2];
+      const void* vin = io < 0 ? x : (const void*)(w.vop + (int64_t)op_slot[io] * nvec * nk4 * s.d * 16);
+      CARC_RETURN_IF(pack_operand_region(view_vin(s, nvec, vin), 1, w.vin_pk, g.rowsA_b, kpA, (int64_t)j * g.regA,
+                                         g.regA, stream));
+    }
+    FoldEpi fe;
+    fe.x0 = s.x0;
+    fe.x1 = s.x1;
+    fe.l0 = s.l0;
+    fe.l1 = s.l1;
+    fe.nvec = nvec;
+    fe.k2 = s.k2;
+    fe.k3 = s.k3;
+    fe.d = s.d;
+    fe.M = g.MA;
+    fe.N = g.NA;
+    fe.kc = g.kcB;
+    fe.col_off = (int64_t)q * g.regB;
+    fe.pitch = kpB;
+    fe.dst = w.w_pk;
+    CARC_RETURN_IF(gemm_bf16_tn_fold(planA, (int)g1.rowsA_a, w.vin_pk, (int)g.rowsA_b, (int)kpA, fe, status, stream));
+    planA += a256(g1.rowsA_a * kpA * 2);
   }
-  // y[vec][l0][l1][l2][l3][p] (+)= sum over all term and split planes
+  // step B: y^T[(l2,l3),(vec,l0,l1,p)] = sum_g S2_1[i1_g] . W_g in one split-K GEMM
+  const char* planB = planA;
+  const int64_t planeB = g.rowsB_a * g.rowsB_b;
+  CARC_RETURN_IF(gemm_bf16_tn(planB, (int)g1.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)kpB, w.pB, g.rowsB_b, w.ksB,
+                              status, stream));
   ZOut o;
   memset(&o, 0, sizeof(o));
   o.base = y;
@@ -361,7 +382,8 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   o.n_ext[1] = s.l0; o.n_str[1] = yl0;
   o.n_ext[2] = s.l1; o.n_str[2] = yl1;
   o.n_ext[3] = s.d; o.n_str[3] = 1;
-  return reduce_partials(w.pB, g.rowsB_b, planeB, n_terms * w.ksB, o, make_double2(1, 0), accumulate, stream);
+  return reduce_partials2(w.pB, g.rowsB_b, planeB, w.ksB, o, make_double2(1, 0), accumulate, w.red,
+                          reduce_partials2_workspace(s.l2 * s.l3, rows_valid_w, w.ksB), stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -414,7 +436,12 @@ FormGeo form_geometry(const S3& s, int max_terms) {
   f.max_terms = max_terms;
   f.kp_max = f.region * max_terms;
   const int64_t tiles = (f.rows_a / 128) * (f.rows_b / bn_for(f.rows_b));
-  f.ks = gemm_effective_ksplit((int)f.kp_max, choose_ksplit(tiles, f.kp_max));
+  // the split count is not monotonic in K: size for the largest over all group sizes
+  f.ks = 1;
+  for (int nt = 1; nt <= max_terms; ++nt) {
+    const int64_t kp = f.region * nt;
+    f.ks = std::max(f.ks, gemm_effective_ksplit((int)kp, choose_ksplit(tiles, kp)));
+  }
   return f;
 }
 

@@ -42,12 +42,13 @@ constexpr int smem_bytes() {
   return 1024 + STAGES * (A_STAGE_BYTES + BN * BK * 2) + 256;
 }
 
-template <int BN>
+template <int BN, int EPI>
 __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                    const __grid_constant__ CUtensorMap tmB,
                                                                    float* __restrict__ out, int64_t ld_out,
                                                                    int64_t split_stride, int kb_per_split,
-                                                                   int kb_total, int* __restrict__ err) {
+                                                                   int kb_total, int* __restrict__ err,
+                                                                   const __grid_constant__ FoldEpi fe) {
   using namespace umma;
   constexpr int B_STAGE_BYTES = BN * BK * 2;
   constexpr uint32_t TMEM_COLS = tmem_cols_for(BN);
@@ -133,7 +134,48 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
     const int quad = warp & 3;
     const bool ok = mbar_wait(done, 0, abort_flag);
     tc_fence_after();
-    if (ok) {
+    if (ok && EPI == 1) {
+      // rows 4m + 2c + s: sum s (lane ^ 1), pair re/im (lane ^ 2), write W[m, n] split into the packed operand
+      const int row = m0 + quad * 32 + lane;
+      const int64_t m = row >> 2;
+      const bool writer = (lane & 3) == 0 && m < fe.M;
+      int64_t xx0 = 0, xx1 = 0, ll0 = 0, ll1 = 0;
+      if (writer) {
+        int64_t r = m;
+        ll1 = r % fe.l1; r /= fe.l1;
+        ll0 = r % fe.l0; r /= fe.l0;
+        xx1 = r % fe.x1; r /= fe.x1;
+        xx0 = r;
+      }
+      __nv_bfloat16* W = static_cast<__nv_bfloat16*>(fe.dst);
+#pragma unroll 1
+      for (int c0 = 0; c0 < BN; c0 += 32) {
+        uint32_t r[32];
+        tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const double v = (double)__uint_as_float(r[j]) + (double)__shfl_xor_sync(0xffffffffu, __uint_as_float(r[j]), 1);
+          const double im = __shfl_xor_sync(0xffffffffu, v, 2);
+          const int64_t n = n0 + c0 + j;
+          if (!writer || c0 + j >= BN || n >= fe.N) continue;
+          int64_t q = n;
+          const int64_t p = q % fe.d; q /= fe.d;
+          const int64_t k3 = q % fe.k3; q /= fe.k3;
+          const int64_t k2 = q % fe.k2; q /= fe.k2;
+          const int64_t vec = q;
+          const int64_t wrow = ((vec * fe.l0 + ll0) * fe.l1 + ll1) * fe.d + p;
+          const int64_t kk = ((xx0 * fe.x1 + xx1) * fe.k2 + k2) * fe.k3 + k3;
+          const float fr = (float)v, fi = (float)im;
+          const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hi = __float2bfloat16_rn(fi);
+          const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
+          const __nv_bfloat16 li = __float2bfloat16_rn(fi - __bfloat162float(hi));
+          __nv_bfloat16* rowp = W + wrow * fe.pitch + fe.col_off;
+          *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * kk) = __halves2bfloat162(hr, hi);
+          *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * fe.kc + 2 * kk) = __halves2bfloat162(lr, li);
+        }
+      }
+    } else if (ok) {
       const int row = m0 + quad * 32 + lane;
       float* dst = out + (int64_t)blockIdx.z * split_stride + (int64_t)row * ld_out + n0;
 #pragma unroll 1
@@ -191,20 +233,35 @@ int make_map(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, 
   return CARC_OK;
 }
 
-template <int BN>
+template <int BN, int EPI>
 int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, float* out, int64_t ld_out,
-              int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, cudaStream_t stream) {
+              int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, const FoldEpi& fe,
+              cudaStream_t stream) {
   constexpr int SMEM = smem_bytes<BN>();
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    attr_err = cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
   });
   if (attr_err != cudaSuccess) return fail(CARC_CUDA_ERROR, "tensor core GEMM: %s", cudaGetErrorString(attr_err));
   dim3 grid(M / BM, N / BN, ksplit);
-  gemm_bf16_tn_kernel<BN><<<grid, THREADS, SMEM, stream>>>(ma, mb, out, ld_out, split_stride, kb_per, kb_total, err);
+  gemm_bf16_tn_kernel<BN, EPI><<<grid, THREADS, SMEM, stream>>>(ma, mb, out, ld_out, split_stride, kb_per, kb_total,
+                                                                 err, fe);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
+}
+
+template <int EPI>
+int launch_any(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, float* out, int64_t ld_out,
+               int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, const FoldEpi& fe,
+               cudaStream_t stream) {
+  switch (bn) {
+    case 256: return launch_bn<256, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 128: return launch_bn<128, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 64: return launch_bn<64, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 32: return launch_bn<32, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    default: return launch_bn<16, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+  }
 }
 
 }  // namespace
@@ -223,13 +280,23 @@ int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, 
   CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, BM));
   CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
   const int64_t split_stride = (int64_t)M * ld_out;
-  switch (bn) {
-    case 256: return launch_bn<256>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream);
-    case 128: return launch_bn<128>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream);
-    case 64: return launch_bn<64>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream);
-    case 32: return launch_bn<32>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream);
-    default: return launch_bn<16>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream);
-  }
+  FoldEpi none;
+  memset(&none, 0, sizeof(none));
+  return launch_any<0>(bn, ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, none, stream);
+}
+
+int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
+                      cudaStream_t stream) {
+  if (M <= 0 || N <= 0 || K <= 0 || M % BM != 0 || K % BK != 0 || N % 16 != 0)
+    return fail(CARC_BAD_SHAPE, "tensor core GEMM: shape %d x %d x %d not tileable (M%%128, K%%64, N%%16)", M, N, K);
+  if (fe.M * 4 > M || fe.N > N || (fe.pitch & 1) || (fe.col_off & 1))
+    return fail(CARC_BAD_ARG, "tensor core GEMM: folding epilogue does not fit the tile grid");
+  const int kb_total = K / BK;
+  int bn = N % 256 == 0 ? 256 : N % 128 == 0 ? 128 : N % 64 == 0 ? 64 : N % 32 == 0 ? 32 : 16;
+  CUtensorMap ma, mb;
+  CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, BM));
+  CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
+  return launch_any<1>(bn, ma, mb, M, N, nullptr, N, 0, 1, kb_total, kb_total, err, fe, stream);
 }
 
 int gemm_effective_ksplit(int K, int ksplit) {
@@ -360,6 +427,39 @@ __global__ void reduce_kernel(const float* __restrict__ P, double2* __restrict__
   }
 }
 
+// partial[s][m][n] = sum over planes z = s, s+S, ... of the folded complex value
+__global__ void reduce_slices_kernel(const float* __restrict__ P, double2* __restrict__ part,
+                                     const __grid_constant__ ReduceParams p, int S) {
+  const int64_t total = (int64_t)S * p.Mc * p.Nc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t n = t % p.Nc;
+    const int64_t rest = t / p.Nc;
+    const int64_t m = rest % p.Mc;
+    const int s = (int)(rest / p.Mc);
+    double re = 0.0, im = 0.0;
+    for (int z = s; z < p.ksplit; z += S) {
+      const float* b = P + z * p.split_stride + (4 * m) * p.ld + n;
+      re += (double)b[0] + (double)b[p.ld];
+      im += (double)b[2 * p.ld] + (double)b[3 * p.ld];
+    }
+    part[t] = make_double2(re, im);
+  }
+}
+
+__global__ void reduce_finish_kernel(const double2* __restrict__ part, double2* __restrict__ C,
+                                     const __grid_constant__ ReduceParams p, int S) {
+  const int64_t total = p.Mc * p.Nc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    double2 v = make_double2(0.0, 0.0);
+    for (int s = 0; s < S; ++s) v = cadd(v, part[(int64_t)s * total + t]);
+    v = cmul(p.alpha, v);
+    const int64_t m = t / p.Nc, n = t % p.Nc;
+    const int64_t off = pdecomp(m, p.nm, p.m_ext, p.m_str) + pdecomp(n, p.nn, p.n_ext, p.n_str);
+    if (p.accumulate) v = cadd(v, C[off]);
+    C[off] = v;
+  }
+}
+
 inline int grid_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * 152)); }
 
 PackParams pack_params(const ZView& v, int64_t rows_out, int64_t kp_out, int64_t col_off) {
@@ -454,6 +554,45 @@ int reduce_partials(const float* P, int64_t ld, int64_t split_stride, int ksplit
   p.accumulate = accumulate;
   p.alpha = alpha;
   reduce_kernel<<<grid_of(p.Mc * p.Nc), 256, 0, stream>>>(P, static_cast<double2*>(o.base), p);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+static int reduce_slices_for(int ksplit) { return std::max(1, std::min(ksplit, 32)); }
+
+int64_t reduce_partials2_workspace(int64_t Mc, int64_t Nc, int ksplit) {
+  return (int64_t)reduce_slices_for(ksplit) * Mc * Nc * 16 + 256;
+}
+
+int reduce_partials2(const float* P, int64_t ld, int64_t split_stride, int ksplit, const ZOut& o, double2 alpha,
+                     int accumulate, void* ws, int64_t ws_bytes, cudaStream_t stream) {
+  ReduceParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.nm = o.nm;
+  p.nn = o.nn;
+  p.Mc = 1;
+  p.Nc = 1;
+  for (int i = 0; i < o.nm; ++i) {
+    p.m_ext[i] = o.m_ext[i];
+    p.m_str[i] = o.m_str[i];
+    p.Mc *= o.m_ext[i];
+  }
+  for (int i = 0; i < o.nn; ++i) {
+    p.n_ext[i] = o.n_ext[i];
+    p.n_str[i] = o.n_str[i];
+    p.Nc *= o.n_ext[i];
+  }
+  p.ld = ld;
+  p.split_stride = split_stride;
+  p.ksplit = ksplit;
+  p.accumulate = accumulate;
+  p.alpha = alpha;
+  const int S = reduce_slices_for(ksplit);
+  if (ws_bytes < reduce_partials2_workspace(p.Mc, p.Nc, ksplit)) return fail(CARC_BAD_ARG, "reduce: workspace too small");
+  double2* part = static_cast<double2*>(ws);
+  reduce_slices_kernel<<<grid_of((int64_t)S * p.Mc * p.Nc), 256, 0, stream>>>(P, part, p, S);
+  CARC_CHECK_LAUNCH();
+  reduce_finish_kernel<<<grid_of(p.Mc * p.Nc), 256, 0, stream>>>(part, static_cast<double2*>(o.base), p, S);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }

@@ -21,6 +21,19 @@ struct ZOut {
   int64_t n_ext[CARC_MAX_SUBDIMS], n_str[CARC_MAX_SUBDIMS];
 };
 
+// Epilogue that folds the GEMM rows (4m + 2c + s) into complex W[m, n] and
+// writes it split (hi | lo) into a region of a packed K-major operand:
+//   m -> (x0,x1,l0,l1), n -> (vec,k2,k3,p);  row (vec,l0,l1,p), k (x0,x1,k2,k3).
+struct FoldEpi {
+  int64_t x0, x1, l0, l1;
+  int64_t nvec, k2, k3, d;
+  int64_t M, N;      // valid complex rows / columns
+  int64_t kc;        // complex K of the destination region
+  int64_t col_off;   // first bf16 column of the region
+  int64_t pitch;     // destination row pitch in bf16 elements
+  void* dst;
+};
+
 int64_t zview_rows(const ZView& v);
 int64_t zview_k(const ZView& v);
 int64_t round_up(int64_t a, int64_t b);
@@ -30,6 +43,14 @@ int64_t round_up(int64_t a, int64_t b);
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
                  cudaStream_t stream);
 int gemm_effective_ksplit(int K, int ksplit);
+// The same GEMM (no K split) with the folding epilogue instead of FP32 planes.
+int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
+                      cudaStream_t stream);
+// Two-level deterministic reduction of split-K planes into a complex output
+// (coalesced over columns; the plane sum is spread over `slices` partial sums).
+int64_t reduce_partials2_workspace(int64_t Mc, int64_t Nc, int ksplit);
+int reduce_partials2(const float* P, int64_t ld, int64_t split_stride, int ksplit, const ZOut& o, double2 alpha,
+                     int accumulate, void* ws, int64_t ws_bytes, cudaStream_t stream);
 // role 0: A operand (rows (m, re/im, hi/lo)); role 1: B operand (row n, K = [hi | lo]).
 int pack_operand(const ZView& v, int role, void* out, int64_t rows_out, int64_t kp_out, cudaStream_t stream);
 // Pack into the K-column region [col_off, col_off + region) of rows of pitch kp_out (region >= 4K, rest zeroed).

@@ -296,12 +296,12 @@ class Stage3Operator:
         """Packed split-BF16 copies of this class's S2 tags (built once)."""
         if "plan" not in g:
             lib = _lib.load()
-            nbytes = lib.carc_stage3_tc_plan_size(g["s0"], g["s1"], g["n0"], g["n1"])
+            nbytes = lib.carc_stage3_tc_plan_size(g["s0"], g["s1"], g["pt"], len(g["terms"]))
             if nbytes < 0:
                 _lib.check(_lib.CARC_BAD_SHAPE)
             g["plan"] = torch.empty(max(nbytes, 256), dtype=torch.uint8, device=self.device)
-            _lib.call("carc_stage3_tc_prepare", g["s0"], g["s1"], g["p0"], g["n0"], g["p1"], g["n1"],
-                      ctypes.c_void_p(g["plan"].data_ptr()), nbytes, current_stream_handle())
+            _lib.call("carc_stage3_tc_prepare", g["s0"], g["s1"], g["p0"], g["n0"], g["p1"], g["n1"], g["pt"],
+                      len(g["terms"]), ctypes.c_void_p(g["plan"].data_ptr()), nbytes, current_stream_handle())
         return g["plan"]
 
     def _status(self):
@@ -327,7 +327,8 @@ class Stage3Operator:
         st = self._status()
         for gi, g in enumerate(self._groups):
             plan = self._tc_plan(g)
-            ws_bytes = lib.carc_stage3_matvec_tc_workspace_size(g["s0"], g["s1"], self.d, len(g["terms"]), nvec)
+            ws_bytes = lib.carc_stage3_matvec_tc_workspace_size(g["s0"], g["s1"], self.d, g["pt"], len(g["terms"]),
+                                                                nvec)
             if ws_bytes < 0:
                 _lib.check(_lib.CARC_BAD_SHAPE)
             ws = engine.Workspace.get(ws_bytes, x.device)

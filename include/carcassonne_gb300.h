@@ -158,25 +158,27 @@ int carc_gemm_bf16_tn(const void* A, int32_t M, const void* B, int32_t N, int32_
 /*
  * The stage-3 operator on the tensor cores (split-BF16 operands, FP32
  * accumulation in TMEM, FP64 reductions; relative error ~1e-5).
- * carc_stage3_tc_prepare packs the S2 tags once into a caller-provided plan
- * buffer of carc_stage3_tc_plan_size bytes (the many matvecs of a solve reuse
- * it); carc_stage3_matvec_tc then applies the operator exactly as
+ * carc_stage3_tc_prepare packs the S2 tags of a term table once into a
+ * caller-provided plan buffer of carc_stage3_tc_plan_size bytes (the many
+ * matvecs of a solve reuse it; the plan is valid for that term table only);
+ * carc_stage3_matvec_tc then applies the operator exactly as
  * carc_stage3_matvec_f64 does (same terms, x, y layout), and
  * carc_stage3_form_matrix_tc forms H as carc_stage3_form_matrix_f64 does.
  * *status (device int32) is nonzero if a pipeline wait timed out.
  * Replaces formDenseStage3 / formNormalizationStage3 multiply and formMatrix
  * (tensors/_2d/dense.py:114-203) where split-BF16 accuracy is accepted.
  */
-int64_t carc_stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, int32_t n0, int32_t n1);
+int64_t carc_stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, const int32_t* terms,
+                                 int32_t n_terms);
 int carc_stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape,
                            const void* const* s0_ptrs, int32_t n0, const void* const* s1_ptrs, int32_t n1,
-                           void* plan, int64_t plan_bytes, void* stream);
+                           const int32_t* terms, int32_t n_terms, void* plan, int64_t plan_bytes, void* stream);
 int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan,
                           int32_t n0, int32_t n1, const void* const* op_ptrs, int32_t nop,
                           const int32_t* terms, int32_t n_terms, const void* x, void* y, int32_t nvec,
                           int32_t accumulate, void* workspace, int64_t workspace_bytes, void* status, void* stream);
 int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
-                                             int32_t n_terms, int32_t nvec);
+                                             const int32_t* terms, int32_t n_terms, int32_t nvec);
 int carc_stage3_form_matrix_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
                                const void* const* s0_ptrs, int32_t n0, const void* const* s1_ptrs, int32_t n1,
                                const void* const* op_ptrs, int32_t nop, const int32_t* terms, int32_t n_terms,

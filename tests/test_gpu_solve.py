@@ -1,0 +1,40 @@
+"""Center-site solves: the plain FP64 solve and the mixed-precision solve
+(tensor-core split-BF16 H_eff/N_eff, FP64 Lanczos, FP64 Rayleigh-Ritz
+refinement) both reach the reference's ground-state energy on the golden
+trajectories to 1e-8 relative."""
+import json
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from tests.test_gpu_system import GOLD, _system_at, env  # noqa: F401  (fixture)
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("ti", s) for s in range(1, 6)] + [("heis", s) for s in range(5)] + [("ising_ud", s) for s in range(0, 8, 2)]
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_solve_center_energy(env, precision):
+    from carcassonne_gb300.solve import solve_center
+    with open(os.path.join(GOLD, "tables.json")) as f:
+        tables = json.load(f)
+    traj = np.load(os.path.join(GOLD, "trajectory.npz"))
+    for name, step in CASES:
+        system = _system_at(env, traj, tables[name]["records"][step], name, step)
+        H, N = system.formExpectationAndNormalizationMultipliers()
+        out = solve_center(H, N, precision=precision)
+        exact = traj[f"{name}_{step}_E"][0].real
+        err = abs(out["energy"] - exact) / max(1.0, abs(exact))
+        assert err <= 1e-8, (name, step, precision, out["energy"], exact, out["lanczos_eigenvalue"])
+        # the returned center is N-normalized and its FP64 Rayleigh quotient is the energy
+        x = out["center"]
+        hx = H.operator.apply(x._t)
+        nx = N.operator.apply(x._t)
+        xh = x._t.reshape(-1).conj()
+        nn = torch.dot(xh, nx.reshape(-1)).real.item()
+        ee = torch.dot(xh, hx.reshape(-1)).real.item() / nn
+        assert abs(nn - 1.0) < 1e-8
+        assert abs(ee - out["energy"]) <= 1e-10 * max(1.0, abs(exact))
