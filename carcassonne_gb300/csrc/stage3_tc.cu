@@ -149,23 +149,6 @@ ZView view_s2_1_stepB(const S3& s, const void* base) {
   return v;
 }
 
-// Vin[vec][k0][k1][k2][k3][p] as a B operand: rows (vec,k2,k3,p), k (k0,k1)
-ZView view_vin(const S3& s, int nvec, const void* base) {
-  const int64_t k3 = s.d, k2 = s.k3 * k3, k1 = s.k2 * k2, k0 = s.k1 * k1, vec = s.k0 * k0;
-  ZView v;
-  memset(&v, 0, sizeof(v));
-  v.base = base;
-  v.nr = 4;
-  v.r_ext[0] = nvec; v.r_str[0] = vec;
-  v.r_ext[1] = s.k2; v.r_str[1] = k2;
-  v.r_ext[2] = s.k3; v.r_str[2] = k3;
-  v.r_ext[3] = s.d; v.r_str[3] = 1;
-  v.nk = 2;
-  v.k_ext[0] = s.k0; v.k_str[0] = k0;
-  v.k_ext[1] = s.k1; v.k_str[1] = k1;
-  return v;
-}
-
 // zero the padding of the packed W: rows >= rows_valid, and per region the
 // columns [4 kc, reg) (the folding epilogue writes only the valid entries)
 __global__ void clear_w_padding_kernel(__nv_bfloat16* __restrict__ W, int64_t rows_valid, int64_t rows_total,
@@ -184,9 +167,10 @@ __global__ void clear_w_padding_kernel(__nv_bfloat16* __restrict__ W, int64_t ro
 
 inline int grid_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * 152)); }
 
+// split-K count that fills the 152 SMs (one CTA each) in a single wave
 int choose_ksplit(int64_t tiles, int64_t kp) {
   const int64_t kb = kp / 64;
-  int64_t ks = (2 * 148 + tiles - 1) / tiles;
+  int64_t ks = tiles >= 152 ? 1 : 152 / tiles;
   ks = std::max<int64_t>(1, std::min<int64_t>(ks, kb));
   return (int)ks;
 }
@@ -240,41 +224,98 @@ int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const vo
 namespace {
 
 struct MvWs {
-  char* vop;     // distinct operators applied to x, complex128
-  char* vin_pk;  // packed Vin regions of one group
+  char* vin;     // packed Vin operands of all groups (step-A B operands)
   char* w_pk;    // packed W of all groups (step-B operand)
   float* pB;     // step-B split planes
   char* red;     // reduction partial sums
   int ksB;
+  std::vector<int64_t> vin_off;  // byte offset of each group's Vin operand
 };
 
-int64_t mv_layout(const S3& s, int nvec, int n_terms, const TermGroups& tg, MvWs* w, void* base) {
+int64_t mv_layout(const S3& s, int nvec, const TermGroups& tg, MvWs* w, void* base) {
   const Geo g = geometry(s, nvec);
   const int64_t kpB = g.regB * (int64_t)tg.i1.size();
   const int64_t tilesB = (g.rowsB_a / 128) * (g.rowsB_b / bn_for(g.rowsB_b));
   const int ksB = gemm_effective_ksplit((int)kpB, choose_ksplit(tilesB, kpB));
-  const int64_t nk4 = s.k0 * s.k1 * s.k2 * s.k3;
-  const int64_t sizes[5] = {(int64_t)n_terms * nvec * nk4 * s.d * 16,
-                            g.rowsA_b * g.regA * (int64_t)tg.max_terms * 2,
-                            g.rowsB_b * kpB * 2,
-                            (int64_t)ksB * g.rowsB_a * g.rowsB_b * 4,
+  std::vector<int64_t> vin_off;
+  int64_t vin_bytes = 0;
+  for (auto& v : tg.terms) {
+    vin_off.push_back(vin_bytes);
+    vin_bytes += a256(g.rowsA_b * g.regA * (int64_t)v.size() * 2);
+  }
+  const int64_t sizes[4] = {vin_bytes, g.rowsB_b * kpB * 2, (int64_t)ksB * g.rowsB_a * g.rowsB_b * 4,
                             reduce_partials2_workspace(s.l2 * s.l3, (int64_t)nvec * s.l0 * s.l1 * s.d, ksB)};
   char* p = static_cast<char*>(base);
   int64_t off = 0;
-  char* ptrs[5];
-  for (int i = 0; i < 5; ++i) {
+  char* ptrs[4];
+  for (int i = 0; i < 4; ++i) {
     ptrs[i] = p ? p + off : nullptr;
     off += a256(sizes[i]);
   }
   if (w) {
-    w->vop = ptrs[0];
-    w->vin_pk = ptrs[1];
-    w->w_pk = ptrs[2];
-    w->pB = reinterpret_cast<float*>(ptrs[3]);
-    w->red = ptrs[4];
+    w->vin = ptrs[0];
+    w->w_pk = ptrs[1];
+    w->pB = reinterpret_cast<float*>(ptrs[2]);
+    w->red = ptrs[3];
     w->ksB = ksB;
+    w->vin_off = vin_off;
   }
   return off;
+}
+
+// Step A's B operands for every term in one launch: Vin_t = O[io_t] applied
+// to the physical index of x (x itself for identity terms), split into BF16
+// hi/lo and packed K-major as rows (vec,k2,k3,p) x [hi | lo] of (k0,k1, re/im)
+// into the term's K region of its group's operand; padding rows and columns
+// are written as zeros.
+constexpr int kVinTermsPerLaunch = 64;
+
+struct VinTerms {
+  int n;
+  int64_t rows_out, rows_valid, kc, reg4, k23, d;
+  const double2* op[kVinTermsPerLaunch];
+  int64_t dst[kVinTermsPerLaunch];    // uint32 (bf16 pair) offset of the term's region in row 0
+  int64_t pitch[kVinTermsPerLaunch];  // row pitch in bf16 pairs
+};
+
+__global__ void pack_vin_kernel(const double2* __restrict__ x, uint32_t* __restrict__ out,
+                                const __grid_constant__ VinTerms p) {
+  const int64_t per_term = p.rows_out * p.reg4;
+  const int64_t total = (int64_t)p.n * per_term;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int term = (int)(t / per_term);
+    const int64_t rem = t % per_term;
+    const int64_t n = rem / p.reg4, slot = rem % p.reg4;
+    uint32_t* row = out + p.dst[term] + n * p.pitch[term];
+    if (slot >= p.kc) {  // padding columns [4 kc, reg)
+      row[2 * slot] = 0u;
+      row[2 * slot + 1] = 0u;
+      continue;
+    }
+    uint32_t hi = 0u, lo = 0u;
+    if (n < p.rows_valid) {
+      const int64_t pp = n % p.d, q = n / p.d;
+      const int64_t k23 = q % p.k23, vec = q / p.k23;
+      const double2* xv = x + ((vec * p.kc + slot) * p.k23 + k23) * p.d;
+      double2 b;
+      const double2* O = p.op[term];
+      if (O == nullptr) {
+        b = xv[pp];
+      } else {
+        b = make_double2(0.0, 0.0);
+        for (int64_t qq = 0; qq < p.d; ++qq) b = cadd(b, cmul(O[pp * p.d + qq], xv[qq]));
+      }
+      const float fr = (float)b.x, fi = (float)b.y;
+      const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hm = __float2bfloat16_rn(fi);
+      const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
+      const __nv_bfloat16 lm = __float2bfloat16_rn(fi - __bfloat162float(hm));
+      const __nv_bfloat162 h2 = __halves2bfloat162(hr, hm), l2 = __halves2bfloat162(lr, lm);
+      hi = *reinterpret_cast<const uint32_t*>(&h2);
+      lo = *reinterpret_cast<const uint32_t*>(&l2);
+    }
+    row[slot] = hi;
+    row[p.kc + slot] = lo;
+  }
 }
 
 }  // namespace
@@ -284,7 +325,7 @@ int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, in
   S3 s;
   if (s3_shapes(s0_shape, s1_shape, d, &s) != CARC_OK) return -1;
   if (n_terms < 1 || nvec < 1) return 0;
-  return mv_layout(s, nvec, n_terms, group_terms(terms, n_terms), nullptr, nullptr);
+  return mv_layout(s, nvec, group_terms(terms, n_terms), nullptr, nullptr);
 }
 
 int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int n0, int n1,
@@ -303,50 +344,55 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
       return fail(CARC_BAD_ARG, "stage3 tc matvec: term %d out of range", t);
   }
   const TermGroups tg = group_terms(terms, n_terms);
-  if (ws_bytes < mv_layout(s, nvec, n_terms, tg, nullptr, nullptr))
+  if (ws_bytes < mv_layout(s, nvec, tg, nullptr, nullptr))
     return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
   const Geo g1 = geometry(s, 1);
   const Geo g = geometry(s, nvec);
   MvWs w;
-  mv_layout(s, nvec, n_terms, tg, &w, ws);
+  mv_layout(s, nvec, tg, &w, ws);
   const int G = (int)tg.i1.size();
   const int64_t kpB = g.regB * G;
-  // operators applied to x (FP64, tiny): Vop_o[vec][k4][p] = sum_q O[p,q] x[vec][k4][q]
-  std::map<int, int> op_slot;
-  for (int t = 0; t < n_terms; ++t) {
-    int io = terms[3 * t + 2];
-    if (io >= 0 && !op_slot.count(io)) {
-      int slot = (int)op_slot.size();
-      op_slot[io] = slot;
-      carc_contract_desc dop = DescBuilder()
-                                   .m(s.d, s.d, 1)
-                                   .n(nvec, nk4 * s.d, nk4 * s.d)
-                                   .n(nk4, s.d, s.d)
-                                   .k(s.d, 1, 1)
-                                   .d;
-      const void* pa[1] = {op_ptrs[io]};
-      const void* pb[1] = {x};
-      void* pc[1] = {w.vop + (int64_t)slot * nvec * nk4 * s.d * 16};
-      int32_t e[3] = {0, 0, 0};
-      CARC_RETURN_IF(gett_launch(dop, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, nullptr, 0, stream));
+  // Vin of every term, operator applied and packed, in launches of up to 64 terms
+  {
+    VinTerms vt;
+    memset(&vt, 0, sizeof(vt));
+    vt.rows_out = g.rowsA_b;
+    vt.rows_valid = g.NA;
+    vt.kc = s.k0 * s.k1;
+    vt.reg4 = g.regA / 4;
+    vt.k23 = s.k2 * s.k3;
+    vt.d = s.d;
+    auto flush = [&]() -> int {
+      if (vt.n == 0) return CARC_OK;
+      pack_vin_kernel<<<grid_of((int64_t)vt.n * vt.rows_out * vt.reg4), 256, 0, stream>>>(
+          static_cast<const double2*>(x), reinterpret_cast<uint32_t*>(w.vin), vt);
+      CARC_CHECK_LAUNCH();
+      vt.n = 0;
+      return CARC_OK;
+    };
+    for (int q = 0; q < G; ++q) {
+      const int nt = (int)tg.terms[q].size();
+      for (int j = 0; j < nt; ++j) {
+        const int io = terms[3 * tg.terms[q][j] + 2];
+        vt.op[vt.n] = io < 0 ? nullptr : static_cast<const double2*>(op_ptrs[io]);
+        vt.dst[vt.n] = w.vin_off[q] / 4 + (int64_t)j * g.regA / 2;
+        vt.pitch[vt.n] = g.regA * nt / 2;
+        if (++vt.n == kVinTermsPerLaunch) CARC_RETURN_IF(flush());
+      }
     }
+    CARC_RETURN_IF(flush());
   }
   const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
-  clear_w_padding_kernel<<<grid_of(rows_valid_w * G * (g.regB - 4 * g.kcB) + (g.rowsB_b - rows_valid_w) * kpB), 256,
-                           0, stream>>>(reinterpret_cast<__nv_bfloat16*>(w.w_pk), rows_valid_w, g.rowsB_b,
-                                        4 * g.kcB, g.regB, G);
-  CARC_CHECK_LAUNCH();
+  const int64_t pad_w = rows_valid_w * G * (g.regB - 4 * g.kcB) + (g.rowsB_b - rows_valid_w) * kpB;
+  if (pad_w > 0) {
+    clear_w_padding_kernel<<<grid_of(pad_w), 256, 0, stream>>>(reinterpret_cast<__nv_bfloat16*>(w.w_pk), rows_valid_w,
+                                                              g.rowsB_b, 4 * g.kcB, g.regB, G);
+    CARC_CHECK_LAUNCH();
+  }
   // step A per group: W_g = sum_{t in g} S2_0[i0_t] . Vin_t, folded straight into region g of the step-B operand
   const char* planA = static_cast<const char*>(plan);
   for (int q = 0; q < G; ++q) {
-    const std::vector<int>& tl = tg.terms[q];
-    const int64_t kpA = g.regA * (int64_t)tl.size();
-    for (size_t j = 0; j < tl.size(); ++j) {
-      const int io = terms[3 * tl[j] + 2];
-      const void* vin = io < 0 ? x : (const void*)(w.vop + (int64_t)op_slot[io] * nvec * nk4 * s.d * 16);
-      CARC_RETURN_IF(pack_operand_region(view_vin(s, nvec, vin), 1, w.vin_pk, g.rowsA_b, kpA, (int64_t)j * g.regA,
-                                         g.regA, stream));
-    }
+    const int64_t kpA = g.regA * (int64_t)tg.terms[q].size();
     FoldEpi fe;
     fe.x0 = s.x0;
     fe.x1 = s.x1;
@@ -362,7 +408,8 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
     fe.col_off = (int64_t)q * g.regB;
     fe.pitch = kpB;
     fe.dst = w.w_pk;
-    CARC_RETURN_IF(gemm_bf16_tn_fold(planA, (int)g1.rowsA_a, w.vin_pk, (int)g.rowsA_b, (int)kpA, fe, status, stream));
+    CARC_RETURN_IF(gemm_bf16_tn_fold(planA, (int)g1.rowsA_a, w.vin + w.vin_off[q], (int)g.rowsA_b, (int)kpA, fe,
+                                     status, stream));
     planA += a256(g1.rowsA_a * kpA * 2);
   }
   // step B: y^T[(l2,l3),(vec,l0,l1,p)] = sum_g S2_1[i1_g] . W_g in one split-K GEMM

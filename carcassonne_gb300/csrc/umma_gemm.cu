@@ -42,6 +42,80 @@ constexpr int smem_bytes() {
   return 1024 + STAGES * (A_STAGE_BYTES + BN * BK * 2) + 256;
 }
 
+// ---- folding epilogue --------------------------------------------------------
+// The tile's accumulator is 128 rows (4m + 2c + s: complex row m, re/im c,
+// hi/lo s) x BN columns n, staged as FP32 with a row pitch of BN + 4 floats
+// (conflict-free float4 stores).  After it come two index tables: per complex
+// row m of the tile {row part, k part} of the destination (or -1), and per
+// slot q {n_local, row part, k part, valid}, slots in p-major order so that
+// consecutive slots walk (vec, k2, k3), i.e. consecutive destination k.
+template <int BN>
+__host__ __device__ constexpr int FOLD_PITCH() { return BN + 4; }
+
+template <int BN>
+__host__ __device__ constexpr int fold_smem_bytes() { return 128 * FOLD_PITCH<BN>() * 4 + 32 * 8 + BN * 16; }
+
+template <int BN>
+__device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0, int n0, int tid, int nthreads) {
+  int2* tabM = reinterpret_cast<int2*>(sP + 128 * FOLD_PITCH<BN>());
+  int4* tabN = reinterpret_cast<int4*>(tabM + 32);
+  const int L0 = (int)fe.l0, L1 = (int)fe.l1, X1 = (int)fe.x1, K2 = (int)fe.k2, K3 = (int)fe.k3, Dp = (int)fe.d;
+  for (int i = tid; i < 32; i += nthreads) {
+    const int64_t m = (int64_t)(m0 >> 2) + i;
+    int2 t = make_int2(-1, 0);
+    if (m < fe.M) {
+      int r = (int)m;
+      const int ll1 = r % L1; r /= L1;
+      const int ll0 = r % L0; r /= L0;
+      const int xx1 = r % X1; r /= X1;
+      t = make_int2((ll0 * L1 + ll1) * Dp, (r * X1 + xx1) * K2 * K3);
+    }
+    tabM[i] = t;
+  }
+  const bool pmajor = (BN % Dp) == 0;
+  for (int q = tid; q < BN; q += nthreads) {
+    const int nl = pmajor ? (q % (BN / Dp)) * Dp + q / (BN / Dp) : q;
+    const int64_t n = (int64_t)n0 + nl;
+    int4 t = make_int4(nl, 0, 0, 0);
+    if (n < fe.N) {
+      int r = (int)n;
+      const int p = r % Dp; r /= Dp;
+      const int k3 = r % K3; r /= K3;
+      const int k2 = r % K2; r /= K2;
+      t = make_int4(nl, r * L0 * L1 * Dp + p, k2 * K3 + k3, 1);
+    }
+    tabN[q] = t;
+  }
+}
+
+// Phase 2 (all threads): W[m, n] = (P[4m] + P[4m+1]) + i (P[4m+2] + P[4m+3]),
+// split into bf16 hi/lo pairs; consecutive threads store consecutive k of
+// one destination row.
+template <int BN>
+__device__ __forceinline__ void fold_write(const float* sP, const FoldEpi& fe) {
+  const int2* tabM = reinterpret_cast<const int2*>(sP + 128 * FOLD_PITCH<BN>());
+  const int4* tabN = reinterpret_cast<const int4*>(tabM + 32);
+  uint32_t* W = static_cast<uint32_t*>(fe.dst);  // bf16 pairs; pitch, col_off and kc are even
+  const int64_t pitch2 = fe.pitch >> 1, off2 = fe.col_off >> 1;
+  const int kc = (int)fe.kc;
+#pragma unroll 4
+  for (int e = threadIdx.x; e < 32 * BN; e += blockDim.x) {
+    const int ml = e / BN;
+    const int2 tm = tabM[ml];
+    const int4 tn = tabN[e % BN];
+    if (tm.x < 0 || tn.w == 0) continue;
+    const float* col = sP + 4 * ml * FOLD_PITCH<BN>() + tn.x;
+    const float re = col[0] + col[FOLD_PITCH<BN>()];
+    const float im = col[2 * FOLD_PITCH<BN>()] + col[3 * FOLD_PITCH<BN>()];
+    const __nv_bfloat162 h2 = __floats2bfloat162_rn(re, im);
+    const float2 hf = __bfloat1622float2(h2);
+    const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+    uint32_t* rowp = W + (int64_t)(tn.y + tm.x) * pitch2 + off2 + (tm.y + tn.z);
+    rowp[0] = *reinterpret_cast<const uint32_t*>(&h2);
+    rowp[kc] = *reinterpret_cast<const uint32_t*>(&l2);
+  }
+}
+
 template <int BN, int EPI>
 __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                    const __grid_constant__ CUtensorMap tmB,
@@ -52,6 +126,8 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
   using namespace umma;
   constexpr int B_STAGE_BYTES = BN * BK * 2;
   constexpr uint32_t TMEM_COLS = tmem_cols_for(BN);
+  static_assert(EPI == 0 || fold_smem_bytes<BN>() <= STAGES * (A_STAGE_BYTES + B_STAGE_BYTES),
+                "the staged tile must fit in the pipeline stages");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
@@ -134,47 +210,28 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
     const int quad = warp & 3;
     const bool ok = mbar_wait(done, 0, abort_flag);
     tc_fence_after();
-    if (ok && EPI == 1) {
-      // rows 4m + 2c + s: sum s (lane ^ 1), pair re/im (lane ^ 2), write W[m, n] split into the packed operand
-      const int row = m0 + quad * 32 + lane;
-      const int64_t m = row >> 2;
-      const bool writer = (lane & 3) == 0 && m < fe.M;
-      int64_t xx0 = 0, xx1 = 0, ll0 = 0, ll1 = 0;
-      if (writer) {
-        int64_t r = m;
-        ll1 = r % fe.l1; r /= fe.l1;
-        ll0 = r % fe.l0; r /= fe.l0;
-        xx1 = r % fe.x1; r /= fe.x1;
-        xx0 = r;
-      }
-      __nv_bfloat16* W = static_cast<__nv_bfloat16*>(fe.dst);
+    if (EPI == 1) {
+      // Folding epilogue, phase 1: the raw FP32 accumulator rows go to shared
+      // memory (reusing the pipeline stages: once `done` has fired every load
+      // has landed and every MMA has read its operands); phase 2 below, with
+      // all threads of the CTA, folds and writes them.
+      float* sP = reinterpret_cast<float*>(smem);
+      if (ok) {
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t r[32];
-        tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
-        tmem_ld_wait();
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
+          tmem_ld_wait();
+          float4* dst = reinterpret_cast<float4*>(sP + (quad * 32 + lane) * FOLD_PITCH<BN>() + c0);
 #pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          const double v = (double)__uint_as_float(r[j]) + (double)__shfl_xor_sync(0xffffffffu, __uint_as_float(r[j]), 1);
-          const double im = __shfl_xor_sync(0xffffffffu, v, 2);
-          const int64_t n = n0 + c0 + j;
-          if (!writer || c0 + j >= BN || n >= fe.N) continue;
-          int64_t q = n;
-          const int64_t p = q % fe.d; q /= fe.d;
-          const int64_t k3 = q % fe.k3; q /= fe.k3;
-          const int64_t k2 = q % fe.k2; q /= fe.k2;
-          const int64_t vec = q;
-          const int64_t wrow = ((vec * fe.l0 + ll0) * fe.l1 + ll1) * fe.d + p;
-          const int64_t kk = ((xx0 * fe.x1 + xx1) * fe.k2 + k2) * fe.k3 + k3;
-          const float fr = (float)v, fi = (float)im;
-          const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hi = __float2bfloat16_rn(fi);
-          const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
-          const __nv_bfloat16 li = __float2bfloat16_rn(fi - __bfloat162float(hi));
-          __nv_bfloat16* rowp = W + wrow * fe.pitch + fe.col_off;
-          *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * kk) = __halves2bfloat162(hr, hi);
-          *reinterpret_cast<__nv_bfloat162*>(rowp + 2 * fe.kc + 2 * kk) = __halves2bfloat162(lr, li);
+          for (int j = 0; j < 32; j += 4) {
+            if (c0 + j >= BN) break;
+            dst[j / 4] = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
+                                     __uint_as_float(r[j + 3]));
+          }
         }
       }
+      fold_tables<BN>(sP, fe, m0, n0, threadIdx.x - 64, 128);
     } else if (ok) {
       const int row = m0 + quad * 32 + lane;
       float* dst = out + (int64_t)blockIdx.z * split_stride + (int64_t)row * ld_out + n0;
@@ -197,6 +254,7 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
   }
   tc_fence_before();
   __syncthreads();
+  if (EPI == 1 && !*abort_flag) fold_write<BN>(reinterpret_cast<const float*>(smem), fe);
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, CARC_NOT_CONVERGED);
   if (warp == 1) {
     tc_fence_after();

@@ -84,9 +84,17 @@ def _refine(Hop, Nop, x):
 
 def solve_center(H, N, x0=None, precision="plain", refine_steps=1, tol=1e-13):
     """Lowest eigenpair of (H_eff, N_eff) given the two stage-3 Multipliers."""
-    Hop, Nop = H.operator, N.operator
+    Hop, Nop = getattr(H, "operator", None), N.operator
     timer = _Timer()
     timer.mark("start")
+    if Hop is None:
+        # H_eff = 0: every vector is an eigenvector with eigenvalue 0
+        xt = (x0._t if isinstance(x0, TorchData) else torch.ones(Nop.in_shape, dtype=CDT, device="cuda"))
+        xt = xt.reshape(Nop.in_shape)
+        nrm = abs(_dot(xt.reshape(-1), Nop.apply(xt).reshape(-1))) ** 0.5
+        timer.mark("eigensolve")
+        return dict(energy=0.0, center=TorchData(_lin(1.0 / nrm, xt, 0.0, xt)), iterations=0,
+                    timing_ms=timer.breakdown(), lanczos_eigenvalue=0.0)
     if precision == "plain":
         Hm = Hop.form_matrix()
         Nm = Nop.form_matrix()
@@ -106,6 +114,10 @@ def solve_center(H, N, x0=None, precision="plain", refine_steps=1, tol=1e-13):
         for _ in range(refine_steps):
             e, xt = _refine(Hop, Nop, xt)
             energy = float(e)
+        # N-normalize with the FP64 operator (the Rayleigh quotient is unchanged)
+        xf = xt.reshape(-1)
+        nrm = abs(_dot(xf, Nop.apply(xt.reshape(Hop.in_shape)).reshape(-1))) ** 0.5
+        xt = _lin(1.0 / nrm, xf, 0.0, xf)
         timer.mark("refine")
     out = TorchData(xt.reshape(Hop.in_shape))
     return dict(energy=float(energy), center=out, iterations=iters, timing_ms=timer.breakdown(),

@@ -180,12 +180,14 @@ def formExpectationStage3(stage2_0, stage2_1, operator_center):
     i0, i1 = k0.index(Identity()), k1.index(Identity())
     normalization_op = Stage3Operator([stage2_0[Identity()]], [stage2_1[Identity()]], [], [(0, 0, -1)], d)
     normalization = normalization_op.multiplier()
+    normalization.operator = normalization_op
     if expectation is None:
         zero = _ZeroOperator(normalization_op)
-        return Multiplier(normalization.shape, zero, 0, zero.formMatrix, 0), normalization
+        em = Multiplier(normalization.shape, zero, 0, zero.formMatrix, 0)
+        em.operator = None  # no term of the operator reaches the center: H_eff = 0
+        return em, normalization
     em = expectation.multiplier()
     em.operator = expectation
-    normalization.operator = normalization_op
     return em, normalization
 
 

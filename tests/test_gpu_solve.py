@@ -31,8 +31,7 @@ def test_solve_center_energy(env, precision):
         assert err <= 1e-8, (name, step, precision, out["energy"], exact, out["lanczos_eigenvalue"])
         # the returned center is N-normalized and its FP64 Rayleigh quotient is the energy
         x = out["center"]
-        hx = H.operator.apply(x._t)
-        nx = N.operator.apply(x._t)
+        hx, nx = H(x)._t, N(x)._t
         xh = x._t.reshape(-1).conj()
         nn = torch.dot(xh, nx.reshape(-1)).real.item()
         ee = torch.dot(xh, hx.reshape(-1)).real.item() / nn
