@@ -416,7 +416,7 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   const char* planB = planA;
   const int64_t planeB = g.rowsB_a * g.rowsB_b;
   CARC_RETURN_IF(gemm_bf16_tn(planB, (int)g1.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)kpB, w.pB, g.rowsB_b, w.ksB,
-                              status, stream));
+                              status, stream, (int)(4 * s.l2 * s.l3)));
   ZOut o;
   memset(&o, 0, sizeof(o));
   o.base = y;

@@ -31,32 +31,42 @@ namespace {
 
 constexpr int BM = 128;
 constexpr int BK = 64;  // bf16 elements per K block (128 bytes)
-constexpr int STAGES = 4;
 constexpr int THREADS = 192;
 constexpr int A_STAGE_BYTES = BM * BK * 2;
 
 __host__ __device__ constexpr int tmem_cols_for(int bn) { return bn <= 32 ? 32 : (bn <= 64 ? 64 : (bn <= 128 ? 128 : 256)); }
 
-template <int BN>
+// Pipeline depth: the plain GEMM streams long K ranges (4 stages, one CTA
+// per SM); the folding GEMM has short K and a long epilogue, so it keeps two
+// stages and fits two CTAs per SM, one CTA's epilogue overlapping the other's
+// loads and MMAs.
+__host__ __device__ constexpr int stages_for(int epi) { return epi ? 2 : 4; }
+
+template <int BN, int EPI>
 constexpr int smem_bytes() {
-  return 1024 + STAGES * (A_STAGE_BYTES + BN * BK * 2) + 256;
+  return 1024 + stages_for(EPI) * (A_STAGE_BYTES + BN * BK * 2) + 256;
 }
 
 // ---- folding epilogue --------------------------------------------------------
 // The tile's accumulator is 128 rows (4m + 2c + s: complex row m, re/im c,
-// hi/lo s) x BN columns n, staged as FP32 with a row pitch of BN + 4 floats
-// (conflict-free float4 stores).  After it come two index tables: per complex
-// row m of the tile {row part, k part} of the destination (or -1), and per
-// slot q {n_local, row part, k part, valid}, slots in p-major order so that
-// consecutive slots walk (vec, k2, k3), i.e. consecutive destination k.
+// hi/lo s) x BN columns n.  It is staged HC columns at a time as FP32 with a
+// row pitch of HC + 4 floats (conflict-free float4 stores).  After the staged
+// block come two index tables: per complex row m of the tile {row part, k part}
+// of the destination (or -1), and per slot q {n_local, row part, k part,
+// valid}, slots in p-major order so that consecutive slots walk (vec, k2, k3),
+// i.e. consecutive destination k.
 template <int BN>
-__host__ __device__ constexpr int FOLD_PITCH() { return BN + 4; }
+__host__ __device__ constexpr int FOLD_HC() { return BN == 256 ? 128 : (BN == 128 ? 64 : BN); }
 
 template <int BN>
-__host__ __device__ constexpr int fold_smem_bytes() { return 128 * FOLD_PITCH<BN>() * 4 + 32 * 8 + BN * 16; }
+__host__ __device__ constexpr int FOLD_PITCH() { return FOLD_HC<BN>() + 4; }
 
 template <int BN>
-__device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0, int n0, int tid, int nthreads) {
+__host__ __device__ constexpr int fold_smem_bytes() { return 128 * FOLD_PITCH<BN>() * 4 + 32 * 8 + FOLD_HC<BN>() * 16; }
+
+template <int BN>
+__device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0, int nb, int tid, int nthreads) {
+  constexpr int HC = FOLD_HC<BN>();
   int2* tabM = reinterpret_cast<int2*>(sP + 128 * FOLD_PITCH<BN>());
   int4* tabN = reinterpret_cast<int4*>(tabM + 32);
   const int L0 = (int)fe.l0, L1 = (int)fe.l1, X1 = (int)fe.x1, K2 = (int)fe.k2, K3 = (int)fe.k3, Dp = (int)fe.d;
@@ -72,10 +82,10 @@ __device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0
     }
     tabM[i] = t;
   }
-  const bool pmajor = (BN % Dp) == 0;
-  for (int q = tid; q < BN; q += nthreads) {
-    const int nl = pmajor ? (q % (BN / Dp)) * Dp + q / (BN / Dp) : q;
-    const int64_t n = (int64_t)n0 + nl;
+  const bool pmajor = (HC % Dp) == 0 && (nb % Dp) == 0;
+  for (int q = tid; q < HC; q += nthreads) {
+    const int nl = pmajor ? (q % (HC / Dp)) * Dp + q / (HC / Dp) : q;
+    const int64_t n = (int64_t)nb + nl;
     int4 t = make_int4(nl, 0, 0, 0);
     if (n < fe.N) {
       int r = (int)n;
@@ -88,21 +98,21 @@ __device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0
   }
 }
 
-// Phase 2 (all threads): W[m, n] = (P[4m] + P[4m+1]) + i (P[4m+2] + P[4m+3]),
-// split into bf16 hi/lo pairs; consecutive threads store consecutive k of
-// one destination row.
+// W[m, n] = (P[4m] + P[4m+1]) + i (P[4m+2] + P[4m+3]), split into bf16 hi/lo
+// pairs; consecutive threads store consecutive k of one destination row.
 template <int BN>
 __device__ __forceinline__ void fold_write(const float* sP, const FoldEpi& fe) {
+  constexpr int HC = FOLD_HC<BN>();
   const int2* tabM = reinterpret_cast<const int2*>(sP + 128 * FOLD_PITCH<BN>());
   const int4* tabN = reinterpret_cast<const int4*>(tabM + 32);
   uint32_t* W = static_cast<uint32_t*>(fe.dst);  // bf16 pairs; pitch, col_off and kc are even
   const int64_t pitch2 = fe.pitch >> 1, off2 = fe.col_off >> 1;
   const int kc = (int)fe.kc;
 #pragma unroll 4
-  for (int e = threadIdx.x; e < 32 * BN; e += blockDim.x) {
-    const int ml = e / BN;
+  for (int e = threadIdx.x; e < 32 * HC; e += blockDim.x) {
+    const int ml = e / HC;
     const int2 tm = tabM[ml];
-    const int4 tn = tabN[e % BN];
+    const int4 tn = tabN[e % HC];
     if (tm.x < 0 || tn.w == 0) continue;
     const float* col = sP + 4 * ml * FOLD_PITCH<BN>() + tn.x;
     const float re = col[0] + col[FOLD_PITCH<BN>()];
@@ -117,15 +127,16 @@ __device__ __forceinline__ void fold_write(const float* sP, const FoldEpi& fe) {
 }
 
 template <int BN, int EPI>
-__global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
+__global__ __launch_bounds__(THREADS, EPI ? 2 : 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                    const __grid_constant__ CUtensorMap tmB,
                                                                    float* __restrict__ out, int64_t ld_out,
                                                                    int64_t split_stride, int kb_per_split,
-                                                                   int kb_total, int* __restrict__ err,
+                                                                   int kb_total, int a_rows, int* __restrict__ err,
                                                                    const __grid_constant__ FoldEpi fe) {
   using namespace umma;
   constexpr int B_STAGE_BYTES = BN * BK * 2;
   constexpr uint32_t TMEM_COLS = tmem_cols_for(BN);
+  constexpr int STAGES = stages_for(EPI);
   static_assert(EPI == 0 || fold_smem_bytes<BN>() <= STAGES * (A_STAGE_BYTES + B_STAGE_BYTES),
                 "the staged tile must fit in the pipeline stages");
   extern __shared__ uint8_t smem_raw[];
@@ -153,6 +164,15 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
     *abort_flag = 0;
     fence_barrier_init();
   }
+  if (a_rows < BM) {
+    // the TMA fills only rows [0, a_rows) of each A stage: the rest is zero
+    // (the operand's padding rows), so they need not be read from memory
+    for (int s = 0; s < STAGES; ++s) {
+      uint4* z = reinterpret_cast<uint4*>(sA + s * A_STAGE_BYTES + a_rows * BK * 2);
+      for (int i = threadIdx.x; i < (BM - a_rows) * BK * 2 / 16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    fence_proxy_async();
+  }
   if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
   tc_fence_before();
   __syncthreads();
@@ -169,7 +189,7 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)((i / STAGES) & 1);
         if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag)) break;
-        mbar_arrive_expect_tx(&full[s], (uint32_t)(A_STAGE_BYTES + B_STAGE_BYTES));
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(a_rows * BK * 2 + B_STAGE_BYTES));
         const int kx = (kb0 + i) * BK;
         tma_load_2d(sA + s * A_STAGE_BYTES, &tmA, kx, m0, &full[s]);
         tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, kx, n0, &full[s]);
@@ -211,27 +231,7 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
     const bool ok = mbar_wait(done, 0, abort_flag);
     tc_fence_after();
     if (EPI == 1) {
-      // Folding epilogue, phase 1: the raw FP32 accumulator rows go to shared
-      // memory (reusing the pipeline stages: once `done` has fired every load
-      // has landed and every MMA has read its operands); phase 2 below, with
-      // all threads of the CTA, folds and writes them.
-      float* sP = reinterpret_cast<float*>(smem);
-      if (ok) {
-#pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 32) {
-          uint32_t r[32];
-          tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
-          tmem_ld_wait();
-          float4* dst = reinterpret_cast<float4*>(sP + (quad * 32 + lane) * FOLD_PITCH<BN>() + c0);
-#pragma unroll
-          for (int j = 0; j < 32; j += 4) {
-            if (c0 + j >= BN) break;
-            dst[j / 4] = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
-                                     __uint_as_float(r[j + 3]));
-          }
-        }
-      }
-      fold_tables<BN>(sP, fe, m0, n0, threadIdx.x - 64, 128);
+      // the folding epilogue runs below, after the CTA-wide barrier
     } else if (ok) {
       const int row = m0 + quad * 32 + lane;
       float* dst = out + (int64_t)blockIdx.z * split_stride + (int64_t)row * ld_out + n0;
@@ -254,7 +254,41 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
   }
   tc_fence_before();
   __syncthreads();
-  if (EPI == 1 && !*abort_flag) fold_write<BN>(reinterpret_cast<const float*>(smem), fe);
+  if (EPI == 1) {
+    // Folding epilogue, HC columns at a time: warps 2..5 move the raw FP32
+    // accumulator rows of their TMEM lane quadrant to shared memory (reusing
+    // the pipeline stages: once `done` has fired every load has landed and
+    // every MMA has read its operands), then all threads fold and write them.
+    constexpr int HC = FOLD_HC<BN>();
+    float* sP = reinterpret_cast<float*>(smem);
+    const bool ok = !*abort_flag;
+    tc_fence_after();
+#pragma unroll 1
+    for (int h0 = 0; h0 < BN; h0 += HC) {
+      if (ok && warp >= 2) {
+        const int quad = warp & 3;
+#pragma unroll 1
+        for (int c0 = 0; c0 < HC; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(h0 + c0), r);
+          tmem_ld_wait();
+          float4* dst = reinterpret_cast<float4*>(sP + (quad * 32 + lane) * FOLD_PITCH<BN>() + c0);
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) {
+            if (c0 + j >= HC) break;
+            dst[j / 4] = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
+                                     __uint_as_float(r[j + 3]));
+          }
+        }
+      }
+      tc_fence_before();
+      fold_tables<BN>(sP, fe, m0, n0 + h0, threadIdx.x, blockDim.x);
+      __syncthreads();
+      if (ok) fold_write<BN>(sP, fe);
+      __syncthreads();
+      tc_fence_after();
+    }
+  }
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, CARC_NOT_CONVERGED);
   if (warp == 1) {
     tc_fence_after();
@@ -292,10 +326,10 @@ int make_map(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, 
 }
 
 template <int BN, int EPI>
-int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, float* out, int64_t ld_out,
+int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_rows, float* out, int64_t ld_out,
               int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, const FoldEpi& fe,
               cudaStream_t stream) {
-  constexpr int SMEM = smem_bytes<BN>();
+  constexpr int SMEM = smem_bytes<BN, EPI>();
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
@@ -303,29 +337,30 @@ int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, float*
   });
   if (attr_err != cudaSuccess) return fail(CARC_CUDA_ERROR, "tensor core GEMM: %s", cudaGetErrorString(attr_err));
   dim3 grid(M / BM, N / BN, ksplit);
-  gemm_bf16_tn_kernel<BN, EPI><<<grid, THREADS, SMEM, stream>>>(ma, mb, out, ld_out, split_stride, kb_per, kb_total,
+  gemm_bf16_tn_kernel<BN, EPI><<<grid, THREADS, SMEM, stream>>>(ma, mb, out, ld_out, split_stride, kb_per, kb_total, a_rows,
                                                                  err, fe);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }
 
 template <int EPI>
-int launch_any(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, float* out, int64_t ld_out,
+int launch_any(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_rows, float* out,
+               int64_t ld_out,
                int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, const FoldEpi& fe,
                cudaStream_t stream) {
   switch (bn) {
-    case 256: return launch_bn<256, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    case 128: return launch_bn<128, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    case 64: return launch_bn<64, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    case 32: return launch_bn<32, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    default: return launch_bn<16, EPI>(ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 256: return launch_bn<256, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 128: return launch_bn<128, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 64: return launch_bn<64, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 32: return launch_bn<32, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    default: return launch_bn<16, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
   }
 }
 
 }  // namespace
 
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
-                 cudaStream_t stream) {
+                 cudaStream_t stream, int m_live) {
   if (M <= 0 || N <= 0 || K <= 0 || M % BM != 0 || K % BK != 0 || N % 16 != 0)
     return fail(CARC_BAD_SHAPE, "tensor core GEMM: shape %d x %d x %d not tileable (M%%128, K%%64, N%%16)", M, N, K);
   if (ld_out < N || ld_out % 4 != 0) return fail(CARC_BAD_ARG, "tensor core GEMM: ld_out %lld", (long long)ld_out);
@@ -334,13 +369,16 @@ int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, 
   const int kb_per = (kb_total + ksplit - 1) / ksplit;
   ksplit = (kb_total + kb_per - 1) / kb_per;
   int bn = N % 256 == 0 ? 256 : N % 128 == 0 ? 128 : N % 64 == 0 ? 64 : N % 32 == 0 ? 32 : 16;
+  // one 128-row tile whose rows >= 64 are zero padding: load only the live half
+  const int a_rows = (M == BM && m_live > 0 && m_live <= 64) ? 64 : BM;
   CUtensorMap ma, mb;
-  CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, BM));
+  CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, (uint32_t)a_rows));
   CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
   const int64_t split_stride = (int64_t)M * ld_out;
   FoldEpi none;
   memset(&none, 0, sizeof(none));
-  return launch_any<0>(bn, ma, mb, M, N, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, none, stream);
+  return launch_any<0>(bn, ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, none,
+                       stream);
 }
 
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
@@ -354,7 +392,7 @@ int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const F
   CUtensorMap ma, mb;
   CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, BM));
   CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
-  return launch_any<1>(bn, ma, mb, M, N, nullptr, N, 0, 1, kb_total, kb_total, err, fe, stream);
+  return launch_any<1>(bn, ma, mb, M, N, BM, nullptr, N, 0, 1, kb_total, kb_total, err, fe, stream);
 }
 
 int gemm_effective_ksplit(int K, int ksplit) {

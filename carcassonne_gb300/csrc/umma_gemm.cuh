@@ -40,8 +40,10 @@ int64_t round_up(int64_t a, int64_t b);
 
 // Raw GEMM: out[z][m][n] (fp32, ld_out) = sum over split z's K range of A[m,:] . B[n,:]
 // (A: M x K, B: N x K, BF16 K-major; M % 128 == 0, K % 64 == 0, N % 16 == 0).
+// m_live (optional): when M == 128 and only rows [0, m_live <= 64) of A can be
+// nonzero, the zero rows are not read from memory.
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
-                 cudaStream_t stream);
+                 cudaStream_t stream, int m_live = 0);
 int gemm_effective_ksplit(int K, int ksplit);
 // The same GEMM (no K split) with the folding epilogue instead of FP32 planes.
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
