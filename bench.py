@@ -19,6 +19,7 @@ available on the GPU host).
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -36,6 +37,94 @@ METRIC = "center-site matvec GFLOP/s (CostTracker algorithmic flops), 1 GB300"
 UNIT = "GFLOP/s"
 L2_FLUSH_BYTES = 512 << 20
 
+# full center-site solve, mixed vs plain FP64 (Heisenberg XXX term structure,
+# D=4, chi=64 = 8x8, Hermitian-definite synthetic boundaries, seed 2)
+SOLVE = dict(workload="center-site solve, Heisenberg XXX d=2, D=4, chi=64 (8x8)", D=4, c=8, seed=2, reps=3)
+
+# phases of the tensor-core operator, as numbered by carc_phase_timing_read
+PHASE_NAMES = ("pack", "step_a", "step_b", "reduce")
+KERNEL_OF_PHASE = dict(pack="pack_vin_kernel", step_a="gemm_bf16_tn_kernel<256,1> (folding epilogue)",
+                       step_b="gemm_bf16_tn_kernel<256,0> (split-K)", reduce="reduce_slices/finish_kernel")
+# DRAM bytes (read + write) per launch from one ncu capture of this workload
+# (profiles/ holds the summary and the command that produced it)
+NCU_TRAFFIC = {
+    ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "step_a"): dict(
+        bytes_per_launch=8.97e6,
+        source="profiles/stage3_tc_matvec_D4_chi32_nvec8.md: one step-A launch (1-term group, 41.9 MB "
+               "algorithmic), dram read 8.46 MB + write 0.51 MB; the W it writes is still in L2 at kernel exit"),
+}
+
+
+def _round_up(a, b):
+    return (a + b - 1) // b * b
+
+
+def tc_bytes_per_step(opr, nvec):
+    """Algorithmic bytes each tensor-core phase must move per operator
+    application, from the packed split-BF16 operand geometry: step A reads
+    the packed S2_0 tags of its terms (4 bf16 rows x 4K columns per complex
+    row, 2 bytes each) and the packed Vin, and writes W; step B reads the live
+    rows of the packed S2_1 tags and W and writes its FP32 split planes."""
+    out = dict(step_a=0, step_b=0, launches=dict(step_a=0, step_b=0))
+    for g in opr._groups:
+        x0, x1, k0, k1, l0, l1 = g["shape0"]
+        _, _, k2, k3, l2, l3 = g["shape1"]
+        d = opr.d
+        terms = g["terms"]
+        groups = sorted({t[1] for t in terms})
+        nt = len(terms)
+        rows_a = _round_up(4 * x0 * x1 * l0 * l1, 128)
+        reg_a = _round_up(4 * k0 * k1, 64)
+        rows_vin = _round_up(nvec * k2 * k3 * d, 16)
+        reg_b = _round_up(4 * x0 * x1 * k2 * k3, 64)
+        rows_w = _round_up(nvec * l0 * l1 * d, 16)
+        kp_b = reg_b * len(groups)
+        out["step_a"] += 2 * (rows_a * reg_a * nt + rows_vin * reg_a * nt + rows_w * kp_b)
+        out["launches"]["step_a"] += len(groups)
+        live_b = 4 * l2 * l3
+        rows_sb = _round_up(live_b, 128)
+        bn = next(b for b in (256, 128, 64, 32, 16) if rows_w % b == 0)
+        tiles = (rows_sb // 128) * (rows_w // bn)
+        kb = kp_b // 64
+        ks_b = max(1, min(1 if tiles >= 152 else 152 // tiles, kb))
+        kb_per = -(-kb // ks_b)
+        ks_b = -(-kb // kb_per)
+        live_rows = live_b if rows_sb == 128 and live_b <= 64 else rows_sb
+        out["step_b"] += 2 * (live_rows * kp_b + rows_w * kp_b) + 4 * ks_b * rows_sb * rows_w
+        out["launches"]["step_b"] += 1
+    return out
+
+
+def solve_section():
+    """Time-to-energy of one center-site solve: plain FP64 (H_eff, N_eff formed
+    on the CUDA cores, Lanczos) against mixed (formed on the tensor cores from
+    split-BF16 operands, the same Lanczos, FP64 Rayleigh quotient)."""
+    import numpy as np
+    import torch
+    from carcassonne_gb300 import workloads
+    from carcassonne_gb300.solve import solve_center
+    from carcassonne_gb300.tensors._2d import sparse as tsp
+    cc, ss, oo = workloads.hermitian_problem_arrays(D=SOLVE["D"], c=SOLVE["c"], seed=SOLVE["seed"])
+    corners, sides, op = workloads.to_device(cc, ss, oo)
+    H, N = tsp.formExpectationAndNormalizationMultipliers(corners, sides, op)
+    res = {}
+    for prec in ("plain", "mixed"):
+        solve_center(H, N, precision=prec)
+        times = []
+        for _ in range(SOLVE["reps"]):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = solve_center(H, N, precision=prec)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+        res[prec] = dict(seconds=statistics.median(times), energy=out["energy"], lanczos_iterations=out["iterations"],
+                         breakdown_ms={k: round(v, 3) for k, v in out["timing_ms"].items()})
+    e0 = res["plain"]["energy"]
+    return dict(config=dict(SOLVE, n=int(np.prod(H.operator.in_shape)), terms=len(H.operator.terms)),
+                plain=res["plain"], mixed=res["mixed"],
+                rel_energy_diff=abs(res["mixed"]["energy"] - e0) / abs(e0),
+                speedup=res["plain"]["seconds"] / res["mixed"]["seconds"])
+
 
 def parse_args():
     p = argparse.ArgumentParser()
@@ -47,6 +136,8 @@ def parse_args():
     p.add_argument("--mode", default="tc", choices=["tc", "fp64"],
                    help="tc: split-BF16 tensor-core matvec (headline); fp64: plain FP64 CUDA-core matvec")
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-solve", dest="solve", action="store_false",
+                   help="skip the mixed-vs-plain center-site solve comparison")
     return p.parse_args()
 
 
@@ -84,6 +175,9 @@ class ClockSampler:
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
+
+    def samples(self):
+        return len(self.lines)
 
     def stop(self):
         if self.proc is None:
@@ -215,6 +309,19 @@ def main():
         dist.barrier()
     sampler = ClockSampler(local_rank)
     sampler.start()
+
+    def load_until(pred, limit_s):
+        # untimed steps keep the GPU under the same load while nvidia-smi samples
+        t0 = time.perf_counter()
+        while not pred() and time.perf_counter() - t0 < limit_s:
+            for _ in range(20):
+                step()
+            torch.cuda.synchronize()
+
+    # the timed region is milliseconds long; the clock samples (every 100 ms)
+    # bracket it under the same load: at least two before, two after
+    n0 = sampler.samples() if sampler.proc else 0
+    load_until(lambda: sampler.proc is None or sampler.samples() >= n0 + 2, 5.0)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     launches0 = lib.carc_launch_counter()
@@ -228,12 +335,30 @@ def main():
         launches_in_steps += lib.carc_launch_counter() - c0
         ends[i].record()
     torch.cuda.synchronize()
+    n1 = sampler.samples() if sampler.proc else 0
+    load_until(lambda: sampler.proc is None or sampler.samples() >= n1 + 2, 5.0)
     if dist:
         dist.barrier()
     clocks = sampler.stop()
     times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = sum(times) / len(times)
     del launches0
+
+    # per-phase device times of the tensor-core operator (CUDA event pairs
+    # around each phase's launches on the launching stream), same workload
+    phases = None
+    if args.mode == "tc":
+        lib.carc_phase_timing_enable(1)
+        for i in range(args.steps):
+            flush_l2()
+            step()
+        torch.cuda.synchronize()
+        lib.carc_phase_timing_enable(0)
+        phases = {}
+        for pid, pname in enumerate(PHASE_NAMES):
+            tot, cnt = ctypes.c_double(0.0), ctypes.c_int64(0)
+            _lib.check(lib.carc_phase_timing_read(pid, ctypes.byref(tot), ctypes.byref(cnt)))
+            phases[pname] = dict(ms_per_step=tot.value / args.steps, intervals_per_step=cnt.value / args.steps)
 
     # the plain FP64 path on the same workload, for reference
     fp64_ms = None
@@ -286,7 +411,32 @@ def main():
         return
     peaks = measured_peaks()
     achieved_tflops = flops_per_step / (ms * 1e-3) / 1e12
+    roofline = dict(bound="tensor", achieved=achieved_tflops, peak=peaks["bf16_tflops"], unit="TFLOP/s",
+                    frac=achieved_tflops / peaks["bf16_tflops"], traffic=None,
+                    peak_source=peaks["source"] + " bf16 dense",
+                    note="whole operator: algorithmic (CostTracker) flops per step / step time")
+    if phases:
+        geo = tc_bytes_per_step(opr, nvec)
+        for pname, ph in phases.items():
+            ph["share"] = ph["ms_per_step"] / ms
+            if pname in geo:
+                ph["algorithmic_bytes_per_step"] = geo[pname]
+                ph["achieved_gbs"] = geo[pname] / (ph["ms_per_step"] * 1e-3) / 1e9 if ph["ms_per_step"] else None
+        top = max((p for p in phases if p in geo), key=lambda p: phases[p]["ms_per_step"])
+        ph = phases[top]
+        launches = geo["launches"][top]
+        traffic = NCU_TRAFFIC.get((WORKLOAD["workload"], top))
+        roofline = dict(bound="hbm", kernel=KERNEL_OF_PHASE[top], achieved=ph["achieved_gbs"],
+                        peak=peaks["hbm_gbs"], unit="GB/s", frac=ph["achieved_gbs"] / peaks["hbm_gbs"],
+                        traffic=None if traffic is None else traffic["bytes_per_launch"],
+                        algorithmic_bytes_per_launch=geo[top] / launches,
+                        launch_ms=ph["ms_per_step"] / launches, launches_per_step=launches,
+                        peak_source=peaks["source"] + " HBM copy",
+                        traffic_source=None if traffic is None else traffic["source"],
+                        whole_operator_tflops=achieved_tflops,
+                        whole_operator_frac_of_bf16=achieved_tflops / peaks["bf16_tflops"])
     cpu = cpu_reference(args, args.cpu_seconds) if world == 1 else None
+    solve = solve_section() if args.solve else None
     line = dict(
         metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
         ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None,
@@ -301,11 +451,7 @@ def main():
         e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=int(xh.numel() * 16),
                  d2h_bytes_per_step=int(yh.numel() * 16)),
         gpu_launches=int(launches_in_steps),
-        roofline=dict(bound="tensor", achieved=achieved_tflops, peak=peaks["bf16_tflops"], unit="TFLOP/s",
-                      frac=achieved_tflops / peaks["bf16_tflops"], traffic=None,
-                      peak_source=peaks["source"] + " bf16 dense",
-                      note="achieved = algorithmic (CostTracker) flops per step / step time; the split-BF16 "
-                           "path executes 16 real tensor MACs per complex MAC"),
+        roofline=roofline, phases=phases, solve=solve,
         cpu_baseline=None if cpu is None else dict(value=cpu["value"], unit=UNIT, cores=cpu["cores"],
                                                    kind=cpu["kind"], sample=cpu["sample"]),
         clocks=clocks, step_ms=dict(min=min(times), max=max(times)),

@@ -47,6 +47,8 @@ SIGNATURES = {
     "carc_last_error_string": (ctypes.c_char_p, []),
     "carc_version": (ctypes.c_int, []),
     "carc_launch_counter": (_i64, []),
+    "carc_phase_timing_enable": (_i32, [_i32]),
+    "carc_phase_timing_read": (_i32, [_i32, ctypes.POINTER(ctypes.c_double), _pi64]),
     "carc_zcontract_grouped": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _pvp, _i32, _pvp, _i32, _pvp, _i32,
                                               _pi32, _i32, _dbl, _dbl, _i32, _vp, _i64, _vp]),
     "carc_zcontract_workspace_size": (_i64, [ctypes.POINTER(ContractDesc), _i32]),

@@ -16,6 +16,13 @@ int carc_version(void) { return 100; }
 
 int64_t carc_launch_counter(void) { return (int64_t)launch_count(); }
 
+int carc_phase_timing_enable(int32_t on) { return phase_timing_enable(on); }
+
+int carc_phase_timing_read(int32_t phase, double* total_ms, int64_t* count) {
+  if (phase < 0 || phase >= PH_COUNT) return fail(CARC_BAD_ARG, "phase timing: phase %d", phase);
+  return phase_timing_read(phase, total_ms, count);
+}
+
 int carc_zcontract_grouped(const carc_contract_desc* desc, const void* const* a_ptrs, int32_t n_a,
                            const void* const* b_ptrs, int32_t n_b, void* const* c_ptrs, int32_t n_c,
                            const int32_t* entries, int32_t n_entries, double alpha_re, double alpha_im,

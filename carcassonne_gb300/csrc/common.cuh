@@ -33,6 +33,25 @@ void count_launch();
                           cudaGetErrorString(_e), __FILE__, __LINE__);            \
   } while (0)
 
+// Optional per-phase device timing: when enabled (carc_phase_timing_enable),
+// a PhaseScope records a CUDA event pair on the launching stream around the
+// launches of one phase; carc_phase_timing_read sums the elapsed times.
+enum Phase { PH_TC_PACK = 0, PH_TC_STEP_A = 1, PH_TC_STEP_B = 2, PH_TC_REDUCE = 3, PH_COUNT = 8 };
+bool phase_timing_on();
+void phase_record(int phase, cudaStream_t stream, bool start);
+
+struct PhaseScope {
+  int phase;
+  cudaStream_t stream;
+  bool on;
+  PhaseScope(int ph, cudaStream_t s) : phase(ph), stream(s), on(phase_timing_on()) {
+    if (on) phase_record(phase, stream, true);
+  }
+  ~PhaseScope() {
+    if (on) phase_record(phase, stream, false);
+  }
+};
+
 #define CARC_RETURN_IF(status_expr)                                               \
   do {                                                                            \
     int _s = (status_expr);                                                       \

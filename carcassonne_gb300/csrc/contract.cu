@@ -20,6 +20,65 @@ static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
+// ---- per-phase timing ----------------------------------------------------------
+static std::atomic<bool> g_phase_on{false};
+static std::mutex g_phase_mu;
+struct PhaseRec {
+  int phase;
+  cudaEvent_t start, stop;
+};
+static std::vector<PhaseRec> g_phase_recs;
+
+bool phase_timing_on() { return g_phase_on.load(std::memory_order_relaxed); }
+
+void phase_record(int phase, cudaStream_t stream, bool start) {
+  std::lock_guard<std::mutex> lk(g_phase_mu);
+  if (start) {
+    PhaseRec r{phase, nullptr, nullptr};
+    if (cudaEventCreate(&r.start) != cudaSuccess || cudaEventCreate(&r.stop) != cudaSuccess) return;
+    cudaEventRecord(r.start, stream);
+    g_phase_recs.push_back(r);
+  } else {
+    for (auto it = g_phase_recs.rbegin(); it != g_phase_recs.rend(); ++it)
+      if (it->phase == phase) {
+        cudaEventRecord(it->stop, stream);
+        break;
+      }
+  }
+}
+
+int phase_timing_enable(int on) {
+  g_phase_on.store(on != 0, std::memory_order_relaxed);
+  return CARC_OK;
+}
+
+int phase_timing_read(int phase, double* total_ms, int64_t* count) {
+  std::lock_guard<std::mutex> lk(g_phase_mu);
+  double t = 0.0;
+  int64_t n = 0;
+  std::vector<PhaseRec> keep;
+  for (auto& r : g_phase_recs) {
+    if (r.phase != phase) {
+      keep.push_back(r);
+      continue;
+    }
+    float ms = 0.f;
+    cudaError_t e = cudaEventElapsedTime(&ms, r.start, r.stop);
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.stop);
+    if (e != cudaSuccess) {
+      g_phase_recs.swap(keep);
+      return fail(CARC_CUDA_ERROR, "phase timing: %s (synchronize the stream first)", cudaGetErrorString(e));
+    }
+    t += ms;
+    ++n;
+  }
+  g_phase_recs.swap(keep);
+  if (total_ms) *total_ms = t;
+  if (count) *count = n;
+  return CARC_OK;
+}
+
 void set_error(const char* fmt, ...) {
   char buf[1024];
   va_list ap;

@@ -33,6 +33,8 @@ struct GettParams {
 
 const char* last_error();
 long long launch_count();
+int phase_timing_enable(int on);
+int phase_timing_read(int phase, double* total_ms, int64_t* count);
 int validate_desc(const carc_contract_desc& d);
 int64_t gett_workspace_size(const carc_contract_desc& d, int n_out);
 int gett_launch(const carc_contract_desc& d, const void* const* a_ptrs, int n_a, const void* const* b_ptrs, int n_b,

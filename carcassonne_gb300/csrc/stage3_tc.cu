@@ -354,6 +354,7 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   const int64_t kpB = g.regB * G;
   // Vin of every term, operator applied and packed, in launches of up to 64 terms
   {
+    PhaseScope ph(PH_TC_PACK, stream);
     VinTerms vt;
     memset(&vt, 0, sizeof(vt));
     vt.rows_out = g.rowsA_b;
@@ -391,32 +392,38 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   }
   // step A per group: W_g = sum_{t in g} S2_0[i0_t] . Vin_t, folded straight into region g of the step-B operand
   const char* planA = static_cast<const char*>(plan);
-  for (int q = 0; q < G; ++q) {
-    const int64_t kpA = g.regA * (int64_t)tg.terms[q].size();
-    FoldEpi fe;
-    fe.x0 = s.x0;
-    fe.x1 = s.x1;
-    fe.l0 = s.l0;
-    fe.l1 = s.l1;
-    fe.nvec = nvec;
-    fe.k2 = s.k2;
-    fe.k3 = s.k3;
-    fe.d = s.d;
-    fe.M = g.MA;
-    fe.N = g.NA;
-    fe.kc = g.kcB;
-    fe.col_off = (int64_t)q * g.regB;
-    fe.pitch = kpB;
-    fe.dst = w.w_pk;
-    CARC_RETURN_IF(gemm_bf16_tn_fold(planA, (int)g1.rowsA_a, w.vin + w.vin_off[q], (int)g.rowsA_b, (int)kpA, fe,
-                                     status, stream));
-    planA += a256(g1.rowsA_a * kpA * 2);
+  {
+    PhaseScope ph(PH_TC_STEP_A, stream);
+    for (int q = 0; q < G; ++q) {
+      const int64_t kpA = g.regA * (int64_t)tg.terms[q].size();
+      FoldEpi fe;
+      fe.x0 = s.x0;
+      fe.x1 = s.x1;
+      fe.l0 = s.l0;
+      fe.l1 = s.l1;
+      fe.nvec = nvec;
+      fe.k2 = s.k2;
+      fe.k3 = s.k3;
+      fe.d = s.d;
+      fe.M = g.MA;
+      fe.N = g.NA;
+      fe.kc = g.kcB;
+      fe.col_off = (int64_t)q * g.regB;
+      fe.pitch = kpB;
+      fe.dst = w.w_pk;
+      CARC_RETURN_IF(gemm_bf16_tn_fold(planA, (int)g1.rowsA_a, w.vin + w.vin_off[q], (int)g.rowsA_b, (int)kpA, fe,
+                                       status, stream));
+      planA += a256(g1.rowsA_a * kpA * 2);
+    }
   }
   // step B: y^T[(l2,l3),(vec,l0,l1,p)] = sum_g S2_1[i1_g] . W_g in one split-K GEMM
   const char* planB = planA;
   const int64_t planeB = g.rowsB_a * g.rowsB_b;
-  CARC_RETURN_IF(gemm_bf16_tn(planB, (int)g1.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)kpB, w.pB, g.rowsB_b, w.ksB,
-                              status, stream, (int)(4 * s.l2 * s.l3)));
+  {
+    PhaseScope ph(PH_TC_STEP_B, stream);
+    CARC_RETURN_IF(gemm_bf16_tn(planB, (int)g1.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)kpB, w.pB, g.rowsB_b, w.ksB,
+                                status, stream, (int)(4 * s.l2 * s.l3)));
+  }
   ZOut o;
   memset(&o, 0, sizeof(o));
   o.base = y;
@@ -429,6 +436,7 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   o.n_ext[1] = s.l0; o.n_str[1] = yl0;
   o.n_ext[2] = s.l1; o.n_str[2] = yl1;
   o.n_ext[3] = s.d; o.n_str[3] = 1;
+  PhaseScope ph(PH_TC_REDUCE, stream);
   return reduce_partials2(w.pB, g.rowsB_b, planeB, w.ksB, o, make_double2(1, 0), accumulate, w.red,
                           reduce_partials2_workspace(s.l2 * s.l3, rows_valid_w, w.ksB), stream);
 }

@@ -3,10 +3,11 @@
 plain  : H_eff and N_eff formed in FP64 on the CUDA cores, lowest generalized
          eigenpair by the Cholesky-reduced restarted Lanczos (linalg.hegv_lowest).
 mixed  : H_eff and N_eff formed on the tensor cores from split-BF16 operands
-         (~1e-5 relative), the same eigensolver on them, then the eigenvector is
-         refined against the exact (FP64) operators: a Rayleigh-Ritz step on
-         span{x, t}, t = the FP64 residual H x - E N x, and the energy is the
-         FP64 Rayleigh quotient, whose error is quadratic in the eigenvector's.
+         (~1e-5 relative), the same eigensolver on them; the energy is the FP64
+         Rayleigh quotient of that eigenvector with the exact operators (one
+         FP64 application of each), whose error is quadratic in the
+         eigenvector's; optional Rayleigh-Ritz steps on span{x, t}, t the FP64
+         residual H x - E N x, also refine the vector.
 
 Both return the energy, the N-normalized center and a breakdown of where the
 time went (CUDA events on the current stream).
@@ -82,8 +83,24 @@ def _refine(Hop, Nop, x):
     return e2, _lin(1.0 / nrm, y, 0.0, y)
 
 
-def solve_center(H, N, x0=None, precision="plain", refine_steps=1, tol=1e-13):
-    """Lowest eigenpair of (H_eff, N_eff) given the two stage-3 Multipliers."""
+def _rayleigh(Hop, Nop, x):
+    """FP64 Rayleigh quotient of x and x N-normalized with the FP64 operators."""
+    shp = Hop.in_shape
+    xf = x.reshape(-1)
+    hx = Hop.apply(x.reshape(shp)).reshape(-1)
+    nx = Nop.apply(x.reshape(shp)).reshape(-1)
+    nn = _dot(xf, nx).real
+    e = _dot(xf, hx).real / nn
+    return e, _lin(1.0 / abs(nn) ** 0.5, xf, 0.0, xf)
+
+
+def solve_center(H, N, x0=None, precision="plain", refine_steps=0, tol=1e-13):
+    """Lowest eigenpair of (H_eff, N_eff) given the two stage-3 Multipliers.
+
+    mixed: the eigenvector of the tensor-core pencil is accurate to about the
+    operands' 1e-5, so the FP64 Rayleigh quotient of it is accurate to about
+    1e-10 (quadratic); ``refine_steps`` > 0 adds Rayleigh-Ritz steps with the
+    FP64 residual that also improve the vector."""
     Hop, Nop = getattr(H, "operator", None), N.operator
     timer = _Timer()
     timer.mark("start")
@@ -113,11 +130,9 @@ def solve_center(H, N, x0=None, precision="plain", refine_steps=1, tol=1e-13):
         Nop.check_status()
         for _ in range(refine_steps):
             e, xt = _refine(Hop, Nop, xt)
-            energy = float(e)
-        # N-normalize with the FP64 operator (the Rayleigh quotient is unchanged)
-        xf = xt.reshape(-1)
-        nrm = abs(_dot(xf, Nop.apply(xt.reshape(Hop.in_shape)).reshape(-1))) ** 0.5
-        xt = _lin(1.0 / nrm, xf, 0.0, xf)
+        # FP64 Rayleigh quotient and N-normalization with the exact operators
+        energy, xt = _rayleigh(Hop, Nop, xt)
+        energy = float(energy)
         timer.mark("refine")
     out = TorchData(xt.reshape(Hop.in_shape))
     return dict(energy=float(energy), center=out, iterations=iters, timing_ms=timer.breakdown(),

@@ -79,6 +79,36 @@ def matvec_problem_arrays(D=4, c_ket=8, c_bra=4, seed=1, op_arrays=None, rounds=
     return corners, sides, op_arrays
 
 
+def _ket_bra(rng, ket_shape, rank):
+    """sum_r A_r (x) conj(A_r) with the ket and bra axes interleaved as the
+    boundaries store them: (k_l, b_l, 1, k_r, b_r, 1[, D_k, D_b])."""
+    a = rng.standard_normal((rank,) + ket_shape) + 1j * rng.standard_normal((rank,) + ket_shape)
+    if len(ket_shape) == 2:
+        t = np.einsum("rij,rkl->ikjl", a, a.conj())
+        t = t.reshape(ket_shape[0], ket_shape[0], 1, ket_shape[1], ket_shape[1], 1)
+    else:
+        t = np.einsum("rijp,rklq->ikjlpq", a, a.conj())
+        c0, c1, dd = ket_shape
+        t = t.reshape(c0, c0, 1, c1, c1, 1, dd, dd)
+    return t / np.linalg.norm(t)
+
+
+def hermitian_problem_arrays(D=4, c=8, seed=2, op_arrays=None, rounds=1, rank=None):
+    """A center-site problem whose pencil (H_eff, N_eff) is Hermitian with N_eff
+    positive definite: every boundary tag is a sum of ket (x) conj(ket)
+    products (c_ket = c_bra = c, chi = c^2), so every term is a tensor product
+    of Hermitian factors with a Hermitian site operator.  The tag structure is
+    the operator's after ``rounds`` absorption rounds (Heisenberg by default)."""
+    rng = np.random.default_rng(seed)
+    op_arrays = heisenberg_operator_arrays() if op_arrays is None else op_arrays
+    rank = max(2, c) if rank is None else rank
+    op_tags = [t for t, _ in op_arrays]
+    corners_t, sides_t = simulate_tags(op_tags, list(range(4)) * rounds)
+    corners = [[(t, _ket_bra(rng, (c, c), rank)) for t in ct] for ct in corners_t]
+    sides = [[(t, _ket_bra(rng, (c, c, D), rank * D)) for t in st] for st in sides_t]
+    return corners, sides, op_arrays
+
+
 def to_device(corners, sides, op_arrays):
     from .data import TorchData
     c = [{t: TorchData(a) for t, a in lst} for lst in corners]

@@ -46,6 +46,15 @@ int carc_version(void);
 /* Kernels launched by this library so far, over all threads (a monotone
  * counter for instrumentation; no counterpart in the reference). */
 int64_t carc_launch_counter(void);
+/* Per-phase device timing of the tensor-core stage-3 operator (no counterpart
+ * in the reference; instrumentation for benchmarks).  While enabled, each
+ * phase's launches are bracketed by a CUDA event pair on the launching stream.
+ * Phases: 0 operand packing, 1 step-A GEMMs (folding epilogue), 2 step-B
+ * GEMM, 3 split-K reductions.  carc_phase_timing_read, called after the
+ * stream is synchronized, returns the summed milliseconds and the number of
+ * bracketed intervals of one phase and drops its records. */
+int carc_phase_timing_enable(int32_t on);
+int carc_phase_timing_read(int32_t phase, double* total_ms, int64_t* count);
 
 /*
  * A strided complex contraction  C[m; n] (+)= alpha * sum_k op(A)[m; k] op(B)[k; n]

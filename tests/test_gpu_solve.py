@@ -37,3 +37,27 @@ def test_solve_center_energy(env, precision):
         ee = torch.dot(xh, hx.reshape(-1)).real.item() / nn
         assert abs(nn - 1.0) < 1e-8
         assert abs(ee - out["energy"]) <= 1e-10 * max(1.0, abs(exact))
+
+
+@pytest.mark.parametrize("D,c", [(2, 3), (3, 2)])
+def test_solve_center_hermitian_workload(env, D, c):
+    """Synthetic Hermitian-definite pencils with the Heisenberg term structure:
+    plain and mixed solves both land on the oracle's lowest generalized
+    eigenvalue (dense scipy eigh of the oracle's H_eff, N_eff) to 1e-8."""
+    import scipy.linalg as sl
+    from carcassonne_gb300 import workloads
+    from carcassonne_gb300.solve import solve_center
+    from carcassonne_gb300.tensors._2d import sparse as tsp
+    from oracle import carc_oracle as orc
+    from tests.tagrepr import parse_tag
+    cc, ss, oo = workloads.hermitian_problem_arrays(D=D, c=c, seed=2)
+    conv = lambda t: parse_tag(repr(t))  # noqa: E731
+    H_o, N_o, _ = orc.expectation_and_normalization_multipliers(
+        [{conv(t): a for t, a in lst} for lst in cc], [{conv(t): a for t, a in lst} for lst in ss],
+        {conv(t): a for t, a in oo})
+    exact = sl.eigh(H_o.formMatrix(), N_o.formMatrix(), eigvals_only=True)[0]
+    corners, sides, op = workloads.to_device(cc, ss, oo)
+    H, N = tsp.formExpectationAndNormalizationMultipliers(corners, sides, op)
+    for precision in ("plain", "mixed"):
+        out = solve_center(H, N, precision=precision)
+        assert abs(out["energy"] - exact) <= 1e-8 * abs(exact), (precision, out["energy"], exact)
