@@ -105,7 +105,7 @@ const char* last_error() { return g_last_error.c_str(); }
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 8, NT = 256;
+constexpr int NT = 256;
 
 __device__ __forceinline__ int64_t decompose(int64_t idx, int n, const int64_t* ext, const int64_t* str) {
   int64_t off = 0;
@@ -118,21 +118,39 @@ __device__ __forceinline__ int64_t decompose(int64_t idx, int n, const int64_t* 
   return off;
 }
 
+// Output tile TBM x TBN, a 4 x 4 register tile per thread; when the tile needs
+// fewer than 256 threads the block splits K into KS slices (each thread group
+// takes TBK consecutive k of every KSTEP) and sums the slices in shared memory.
+template <int TBM, int TBN>
+struct GettCfg {
+  static constexpr int TX = TBN / 4, TY = TBM / 4, TPS = TX * TY;
+  static constexpr int KS = NT / TPS;
+  static constexpr int TBK = KS >= 4 ? 4 : 8;
+  static constexpr int KSTEP = KS * TBK;
+  static constexpr int STAGE = KSTEP * (TBM + TBN);
+  static constexpr int SMEM_ELEMS = (KS > 1 && TBM * TBN > STAGE) ? TBM * TBN : STAGE;
+};
+
+template <int TBM, int TBN>
 __global__ __launch_bounds__(NT) void gett_kernel(const __grid_constant__ GettParams p) {
+  using Cfg = GettCfg<TBM, TBN>;
+  static_assert(Cfg::TPS * Cfg::KS == NT, "tile must divide the block");
   const int out = blockIdx.z;
   const int ks = blockIdx.y;
-  const int64_t tiles_n = (p.N + BN - 1) / BN;
+  const int64_t tiles_n = (p.N + TBN - 1) / TBN;
   const int64_t tm = blockIdx.x / tiles_n, tn = blockIdx.x % tiles_n;
   const int tid = threadIdx.x;
-  const int tx = tid & 15, ty = tid >> 4;
+  const int slice = tid / Cfg::TPS, lt = tid % Cfg::TPS;
+  const int tx = lt % Cfg::TX, ty = lt / Cfg::TX;
 
-  __shared__ int64_t s_arow[BM], s_crow[BM], s_bcol[BN], s_ccol[BN];
-  __shared__ int64_t s_ak[BK], s_bk[BK];
-  __shared__ double2 As[BK][BM];
-  __shared__ double2 Bs[BK][BN];
+  __shared__ int64_t s_arow[TBM], s_crow[TBM], s_bcol[TBN], s_ccol[TBN];
+  __shared__ int64_t s_ak[Cfg::KSTEP], s_bk[Cfg::KSTEP];
+  __shared__ double2 sbuf[Cfg::SMEM_ELEMS];  // operand stage, then the slice reduction
+  double2(*As)[TBM] = reinterpret_cast<double2(*)[TBM]>(sbuf);
+  double2(*Bs)[TBN] = reinterpret_cast<double2(*)[TBN]>(sbuf + Cfg::KSTEP * TBM);
 
-  for (int i = tid; i < BM; i += NT) {
-    int64_t m = tm * BM + i;
+  for (int i = tid; i < TBM; i += NT) {
+    int64_t m = tm * TBM + i;
     if (m < p.M) {
       s_arow[i] = decompose(m, p.nm, p.m_ext, p.a_m);
       s_crow[i] = decompose(m, p.nm, p.m_ext, p.c_m);
@@ -141,8 +159,8 @@ __global__ __launch_bounds__(NT) void gett_kernel(const __grid_constant__ GettPa
       s_crow[i] = -1;
     }
   }
-  for (int i = tid; i < BN; i += NT) {
-    int64_t n = tn * BN + i;
+  for (int i = tid; i < TBN; i += NT) {
+    int64_t n = tn * TBN + i;
     if (n < p.N) {
       s_bcol[i] = decompose(n, p.nn, p.n_ext, p.b_n);
       s_ccol[i] = decompose(n, p.nn, p.n_ext, p.c_n);
@@ -165,18 +183,19 @@ __global__ __launch_bounds__(NT) void gett_kernel(const __grid_constant__ GettPa
   for (int e = e_begin; e < e_end; ++e) {
     const double2* __restrict__ A = p.a[p.ea[e]];
     const double2* __restrict__ B = p.b[p.eb[e]];
-    for (int64_t k0 = k_begin; k0 < k_end; k0 += BK) {
+    for (int64_t k0 = k_begin; k0 < k_end; k0 += Cfg::KSTEP) {
       __syncthreads();
-      if (tid < BK) {
-        int64_t k = k0 + tid;
-        s_ak[tid] = k < k_end ? decompose(k, p.nk, p.k_ext, p.a_k) : -1;
-      } else if (tid >= 32 && tid < 32 + BK) {
-        int64_t k = k0 + tid - 32;
-        s_bk[tid - 32] = k < k_end ? decompose(k, p.nk, p.k_ext, p.b_k) : -1;
+      for (int i = tid; i < 2 * Cfg::KSTEP; i += NT) {
+        const int kk = i % Cfg::KSTEP;
+        const int64_t k = k0 + kk;
+        if (i < Cfg::KSTEP)
+          s_ak[kk] = k < k_end ? decompose(k, p.nk, p.k_ext, p.a_k) : -1;
+        else
+          s_bk[kk] = k < k_end ? decompose(k, p.nk, p.k_ext, p.b_k) : -1;
       }
       __syncthreads();
-      for (int idx = tid; idx < BK * BM; idx += NT) {
-        int kk = idx / BM, mm = idx % BM;
+      for (int idx = tid; idx < Cfg::KSTEP * TBM; idx += NT) {
+        int kk = idx / TBM, mm = idx % TBM;
         double2 v = make_double2(0.0, 0.0);
         int64_t ro = s_arow[mm], ko = s_ak[kk];
         if (ro >= 0 && ko >= 0) {
@@ -185,8 +204,8 @@ __global__ __launch_bounds__(NT) void gett_kernel(const __grid_constant__ GettPa
         }
         As[kk][mm] = v;
       }
-      for (int idx = tid; idx < BK * BN; idx += NT) {
-        int kk = idx / BN, nn = idx % BN;
+      for (int idx = tid; idx < Cfg::KSTEP * TBN; idx += NT) {
+        int kk = idx / TBN, nn = idx % TBN;
         double2 v = make_double2(0.0, 0.0);
         int64_t co = s_bcol[nn], ko = s_bk[kk];
         if (co >= 0 && ko >= 0) {
@@ -197,18 +216,42 @@ __global__ __launch_bounds__(NT) void gett_kernel(const __grid_constant__ GettPa
       }
       __syncthreads();
 #pragma unroll
-      for (int kk = 0; kk < BK; ++kk) {
+      for (int kk = 0; kk < Cfg::TBK; ++kk) {
+        const int kq = slice * Cfg::TBK + kk;
         double2 a[4], b[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+        for (int i = 0; i < 4; ++i) a[i] = As[kq][ty * 4 + i];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx * 4 + j];
+        for (int j = 0; j < 4; ++j) b[j] = Bs[kq][tx * 4 + j];
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
       }
     }
+  }
+
+  if (Cfg::KS > 1) {
+    // sum the K slices into slice 0 (in slice order: deterministic)
+    double2* red = sbuf;
+    for (int r = 0; r < Cfg::KS; ++r) {
+      __syncthreads();
+      if (slice == r) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            double2* q = &red[(ty * 4 + i) * TBN + tx * 4 + j];
+            *q = r == 0 ? acc[i][j] : cadd(*q, acc[i][j]);
+          }
+      }
+    }
+    __syncthreads();
+    if (slice != 0) return;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = red[(ty * 4 + i) * TBN + tx * 4 + j];
   }
 
   if (p.ksplit == 1) {
@@ -230,11 +273,11 @@ __global__ __launch_bounds__(NT) void gett_kernel(const __grid_constant__ GettPa
     double2* __restrict__ P = p.partial + ((int64_t)ks * p.n_out + out) * p.M * p.N;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      int64_t m = tm * BM + ty * 4 + i;
+      int64_t m = tm * TBM + ty * 4 + i;
       if (m >= p.M) continue;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        int64_t n = tn * BN + tx * 4 + j;
+        int64_t n = tn * TBN + tx * 4 + j;
         if (n >= p.N) continue;
         P[m * p.N + n] = acc[i][j];
       }
@@ -267,8 +310,32 @@ static int64_t prod_ext(int n, const int64_t* e) {
   return r;
 }
 
+// Output tile shapes of the GETT kernel; the launcher takes the one that pads
+// the output least (larger tiles on ties: more reuse per loaded element).
+struct TileShape {
+  int bm, bn, kstep;
+};
+constexpr TileShape kTiles[] = {
+    {64, 64, GettCfg<64, 64>::KSTEP}, {64, 32, GettCfg<64, 32>::KSTEP}, {32, 64, GettCfg<32, 64>::KSTEP},
+    {32, 32, GettCfg<32, 32>::KSTEP}, {32, 16, GettCfg<32, 16>::KSTEP}, {16, 32, GettCfg<16, 32>::KSTEP},
+    {16, 16, GettCfg<16, 16>::KSTEP}};
+
+static int choose_tile(int64_t M, int64_t N) {
+  int best = 0;
+  int64_t best_area = -1;
+  for (int i = 0; i < (int)(sizeof(kTiles) / sizeof(kTiles[0])); ++i) {
+    const int64_t area = ceil_div(M, kTiles[i].bm) * kTiles[i].bm * ceil_div(N, kTiles[i].bn) * kTiles[i].bn;
+    if (best_area < 0 || area < best_area) {
+      best = i;
+      best_area = area;
+    }
+  }
+  return best;
+}
+
 static int choose_ksplit(int64_t M, int64_t N, int64_t K, int n_out, int64_t* kchunk) {
-  int64_t tiles = ceil_div(M, BM) * ceil_div(N, BN) * (int64_t)n_out;
+  const TileShape& t = kTiles[choose_tile(M, N)];
+  int64_t tiles = ceil_div(M, t.bm) * ceil_div(N, t.bn) * (int64_t)n_out;
   int ks = 1;
   const int64_t target = 2 * 152;
   if (tiles < target && K >= 256) {
@@ -277,7 +344,7 @@ static int choose_ksplit(int64_t M, int64_t N, int64_t K, int n_out, int64_t* kc
     ks = (int)std::max<int64_t>(1, std::min<int64_t>({want, maxk, (int64_t)64}));
   }
   int64_t chunk = ceil_div(K, ks);
-  chunk = ceil_div(chunk, BK) * BK;
+  chunk = ceil_div(chunk, t.kstep) * t.kstep;
   ks = (int)ceil_div(K, chunk);
   if (ks < 1) ks = 1;
   *kchunk = chunk;
@@ -373,11 +440,20 @@ int gett_launch(const carc_contract_desc& d, const void* const* a_ptrs, int n_a,
                   (long long)workspace_bytes);
     p.partial = static_cast<double2*>(workspace);
   }
-  int64_t tiles = ceil_div(p.M, BM) * ceil_div(p.N, BN);
+  const int tile = choose_tile(p.M, p.N);
+  int64_t tiles = ceil_div(p.M, kTiles[tile].bm) * ceil_div(p.N, kTiles[tile].bn);
   if (tiles > 0x7fffffff || n_c > 65535 || p.ksplit > 65535)
     return fail(CARC_TOO_LARGE, "grouped contraction: grid too large");
   dim3 grid((unsigned)tiles, (unsigned)p.ksplit, (unsigned)n_c);
-  gett_kernel<<<grid, NT, 0, stream>>>(p);
+  switch (tile) {
+    case 0: gett_kernel<64, 64><<<grid, NT, 0, stream>>>(p); break;
+    case 1: gett_kernel<64, 32><<<grid, NT, 0, stream>>>(p); break;
+    case 2: gett_kernel<32, 64><<<grid, NT, 0, stream>>>(p); break;
+    case 3: gett_kernel<32, 32><<<grid, NT, 0, stream>>>(p); break;
+    case 4: gett_kernel<32, 16><<<grid, NT, 0, stream>>>(p); break;
+    case 5: gett_kernel<16, 32><<<grid, NT, 0, stream>>>(p); break;
+    default: gett_kernel<16, 16><<<grid, NT, 0, stream>>>(p); break;
+  }
   CARC_CHECK_LAUNCH();
   if (p.ksplit > 1) {
     int64_t total = (int64_t)n_c * p.M * p.N;

@@ -48,13 +48,33 @@ __global__ void proj_kernel(int n, int rows, const double2* __restrict__ Q, cons
   }
 }
 
-// w[i] += sign * sum_r h[r] Q[r][i]
-__global__ void combine_kernel(int n, int rows, const double2* __restrict__ Q, const double2* __restrict__ h,
-                               double sign, double2* __restrict__ w, int overwrite) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double2 s = make_double2(0.0, 0.0);
-    for (int r = 0; r < rows; ++r) cfma(s, h[r], Q[(int64_t)r * n + i]);
-    w[i] = overwrite ? cscale(s, sign) : cadd(w[i], cscale(s, sign));
+// w[i] += sign * sum_r h[r] Q[r][i]: a block covers 32 consecutive i with its
+// 8 warps splitting r, the 8 partial sums added in a fixed order
+constexpr int COMB_I = 32, COMB_R = 8;
+__global__ __launch_bounds__(COMB_I * COMB_R) void combine_kernel(int n, int rows, const double2* __restrict__ Q,
+                                                                  const double2* __restrict__ h, double sign,
+                                                                  double2* __restrict__ w, int overwrite) {
+  __shared__ double2 part[COMB_R][COMB_I];
+  const int li = threadIdx.x % COMB_I, lr = threadIdx.x / COMB_I;
+  for (int i0 = blockIdx.x * COMB_I; i0 < n; i0 += gridDim.x * COMB_I) {
+    const int i = i0 + li;
+    double2 s0 = make_double2(0.0, 0.0), s1 = make_double2(0.0, 0.0);
+    if (i < n) {
+      int r = lr;
+      for (; r + COMB_R < rows; r += 2 * COMB_R) {
+        cfma(s0, h[r], Q[(int64_t)r * n + i]);
+        cfma(s1, h[r + COMB_R], Q[(int64_t)(r + COMB_R) * n + i]);
+      }
+      if (r < rows) cfma(s0, h[r], Q[(int64_t)r * n + i]);
+    }
+    part[lr][li] = cadd(s0, s1);
+    __syncthreads();
+    if (lr == 0 && i < n) {
+      double2 t = part[0][li];
+      for (int q = 1; q < COMB_R; ++q) t = cadd(t, part[q][li]);
+      w[i] = overwrite ? cscale(t, sign) : cadd(w[i], cscale(t, sign));
+    }
+    __syncthreads();
   }
 }
 
@@ -91,63 +111,122 @@ __global__ void scale_by_norm_kernel(int n, const double2* __restrict__ nrm2, do
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = cscale(v[i], inv);
 }
 
-// Sturm count of eigenvalues of the tridiagonal (alpha, beta) below x
-__device__ int sturm_count(int m, const double* alpha, const double* beta, double x) {
+// Number of eigenvalues of the symmetric tridiagonal T = (alpha, beta) below
+// x: sign changes of the characteristic-polynomial sequence
+//   p_0 = 1, p_1 = alpha_0 - x, p_i = (alpha_{i-1} - x) p_{i-1} - beta_{i-2}^2 p_{i-2},
+// rescaled as it grows (multiplications and additions only: no division in
+// the recurrence).  A zero p_i takes the sign opposite to p_{i-1}.
+template <typename T>
+__device__ int sturm_count(int m, const double* alpha, const double* beta2, T x) {
   int c = 0;
-  double d = 1.0;
-  for (int i = 0; i < m; ++i) {
-    double b2 = i > 0 ? beta[i - 1] * beta[i - 1] : 0.0;
-    d = alpha[i] - x - (i > 0 ? b2 / d : 0.0);
-    if (d == 0.0) d = -1e-300;
-    if (d < 0) ++c;
+  T p0 = 1, p1 = (T)alpha[0] - x;
+  int s_prev = 1;
+  int s1 = p1 > 0 ? 1 : (p1 < 0 ? -1 : -s_prev);
+  if (s1 != s_prev) ++c;
+  s_prev = s1;
+  for (int i = 1; i < m; ++i) {
+    T p2 = ((T)alpha[i] - x) * p1 - (T)beta2[i - 1] * p0;
+    const int s2 = p2 > 0 ? 1 : (p2 < 0 ? -1 : -s_prev);
+    if (s2 != s_prev) ++c;
+    s_prev = s2;
+    p0 = p1;
+    p1 = p2;
+    const T mag = fabs(p1) + fabs(p0);
+    if (mag > (T)1e16 || (mag < (T)1e-16 && mag > 0)) {
+      const T inv = (T)1 / mag;
+      p0 *= inv;
+      p1 *= inv;
+    }
   }
   return c;
 }
 
 // Lowest eigenpair of the m x m tridiagonal matrix; out = (lambda, residual
-// estimate |beta_m s_m|), s = eigenvector (m).  Single thread; m <= MAXM.
+// estimate |beta_{m-1} s_{m-1}|), s = unit eigenvector (m).  One block of
+// TRI_THREADS threads: parallel multisection of the Gershgorin interval
+// (TRI_THREADS Sturm counts per round, first in FP32 to about 1e-6 of the
+// interval, then in FP64 to machine precision), then inverse iteration by one
+// thread on shared-memory copies.  m <= MAXM.
 constexpr int MAXM = 512;
+constexpr int TRI_THREADS = 256;
 
-__global__ void tridiag_lowest_kernel(int m, const double* __restrict__ alpha, const double* __restrict__ beta,
-                                      double* __restrict__ out, double* __restrict__ s, double* __restrict__ scratch) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double lo = 1e300, hi = -1e300;
-  for (int i = 0; i < m; ++i) {
-    double r = (i > 0 ? fabs(beta[i - 1]) : 0.0) + (i + 1 < m ? fabs(beta[i]) : 0.0);
-    lo = fmin(lo, alpha[i] - r);
-    hi = fmax(hi, alpha[i] + r);
+template <typename T>
+__device__ void multisect(int m, const double* a, const double* b2, double& lo, double& hi, double rel_stop,
+                          int rounds, int* s_first) {
+  for (int r = 0; r < rounds; ++r) {
+    const double w = hi - lo;
+    if (!(w > rel_stop * fmax(fabs(lo), fabs(hi))) || w <= 0.0) break;
+    if (threadIdx.x == 0) *s_first = TRI_THREADS;
+    __syncthreads();
+    const double xt = lo + w * (double)(threadIdx.x + 1) / (double)(TRI_THREADS + 1);
+    if (sturm_count<T>(m, a, b2, (T)xt) >= 1) atomicMin(s_first, (int)threadIdx.x);
+    __syncthreads();
+    const int f = *s_first;
+    const double nlo = f == 0 ? lo : lo + w * (double)f / (double)(TRI_THREADS + 1);
+    const double nhi = f == TRI_THREADS ? hi : lo + w * (double)(f + 1) / (double)(TRI_THREADS + 1);
+    __syncthreads();
+    lo = nlo;
+    hi = nhi;
   }
-  double span = fmax(hi - lo, 1e-300);
-  for (int it = 0; it < 200; ++it) {
-    double mid = 0.5 * (lo + hi);
-    if (sturm_count(m, alpha, beta, mid) >= 1) hi = mid; else lo = mid;
-    if (hi - lo <= 1e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300 * span) break;
+}
+
+__global__ __launch_bounds__(TRI_THREADS) void tridiag_lowest_kernel(int m, const double* __restrict__ alpha,
+                                                                      const double* __restrict__ beta,
+                                                                      double* __restrict__ out, double* __restrict__ s) {
+  __shared__ double sa[MAXM], sb[MAXM], sb2[MAXM];
+  __shared__ double dl[MAXM], dd[MAXM], du[MAXM], du2[MAXM], x[MAXM];
+  __shared__ int piv[MAXM];
+  __shared__ int s_first;
+  __shared__ double s_lo, s_hi;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    sa[i] = alpha[i];
+    sb[i] = i + 1 < m ? beta[i] : 0.0;
+    sb2[i] = sb[i] * sb[i];
   }
-  const double lam = 0.5 * (lo + hi);
+  __syncthreads();
   if (m == 1) {
-    s[0] = 1.0;
-    out[0] = alpha[0];
-    out[1] = fabs(beta[0]);
+    if (threadIdx.x == 0) {
+      s[0] = 1.0;
+      out[0] = sa[0];
+      out[1] = fabs(beta[0]);
+    }
     return;
   }
-  const double scale = fmax(fmax(fabs(lo), fabs(hi)), span);
+  if (threadIdx.x == 0) {
+    double lo = 1e300, hi = -1e300;
+    for (int i = 0; i < m; ++i) {
+      const double r = (i > 0 ? fabs(sb[i - 1]) : 0.0) + (i + 1 < m ? fabs(sb[i]) : 0.0);
+      lo = fmin(lo, sa[i] - r);
+      hi = fmax(hi, sa[i] + r);
+    }
+    s_lo = lo;
+    s_hi = hi;
+  }
+  __syncthreads();
+  double lo = s_lo, hi = s_hi;
+  const double span = fmax(hi - lo, 1e-300);
+  multisect<float>(m, sa, sb2, lo, hi, 1e-5, 2, &s_first);
+  // FP32 counts may be off by one near the eigenvalue: widen before the FP64 rounds
+  {
+    const double w = fmax(hi - lo, 1e-7 * fmax(fabs(lo), fabs(hi)));
+    lo = fmax(s_lo, lo - 4 * w);
+    hi = fmin(s_hi, hi + 4 * w);
+  }
+  multisect<double>(m, sa, sb2, lo, hi, 1e-16, 12, &s_first);
+  const double lam = 0.5 * (lo + hi);
+  if (threadIdx.x != 0) return;
+  const double scale = fmax(fmax(fabs(s_lo), fabs(s_hi)), span);
   // inverse iteration with partial pivoting on T - (lam - delta) I
-  double* dl = scratch;          // sub
-  double* dd = scratch + MAXM;   // diag
-  double* du = scratch + 2 * MAXM;  // super
-  double* du2 = scratch + 3 * MAXM;  // second super (fill-in)
-  double* x = s;
   const double shift = lam - 1e-10 * scale;
   for (int i = 0; i < m; ++i) x[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (i % 7));
-  int piv[MAXM];
   for (int iter = 0; iter < 3; ++iter) {
     for (int i = 0; i < m; ++i) {
-      dd[i] = alpha[i] - shift;
-      dl[i] = i + 1 < m ? beta[i] : 0.0;
-      du[i] = i + 1 < m ? beta[i] : 0.0;
+      dd[i] = sa[i] - shift;
+      dl[i] = sb[i];
+      du[i] = sb[i];
       du2[i] = 0.0;
     }
-    // LU with partial pivoting (LAPACK gttrf pattern)
+    // LU with partial pivoting (the gttrf pattern)
     for (int i = 0; i + 1 < m; ++i) {
       if (fabs(dd[i]) >= fabs(dl[i])) {
         piv[i] = 0;
@@ -168,7 +247,6 @@ __global__ void tridiag_lowest_kernel(int m, const double* __restrict__ alpha, c
         }
       }
     }
-    // solve L U y = x
     for (int i = 0; i + 1 < m; ++i) {
       if (piv[i] == 0) {
         x[i + 1] -= dl[i] * x[i];
@@ -199,6 +277,7 @@ __global__ void tridiag_lowest_kernel(int m, const double* __restrict__ alpha, c
     nrm = sqrt(nrm);
     for (int i = 0; i < m; ++i) x[i] /= nrm;
   }
+  for (int i = 0; i < m; ++i) s[i] = x[i];
   out[0] = lam;
   out[1] = fabs(beta[m - 1] * x[m - 1]);
 }
@@ -232,6 +311,8 @@ __global__ void perturb_start_kernel(int n, double2* __restrict__ u, double eps)
   }
 }
 
+inline int comb_blocks(int n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, COMB_I), 4 * 152)); }
+
 inline int blocks_for(int64_t n, int threads = 256) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, threads), 4 * 152));
 }
@@ -246,7 +327,6 @@ struct LanczosWs {
   double* beta;
   double* tri_out;
   double* s;
-  double* scratch;
   int* breakdown;
   void* dot_ws;
   int64_t dot_ws_bytes;
@@ -270,7 +350,6 @@ int64_t lanczos_ws_layout(int n, int mk, LanczosWs* L, void* base) {
   t.beta = (double*)take((int64_t)(mk + 1) * 8);
   t.tri_out = (double*)take(4 * 8);
   t.s = (double*)take((int64_t)MAXM * 8);
-  t.scratch = (double*)take((int64_t)4 * MAXM * 8);
   t.breakdown = (int*)take(16);
   t.dot_ws_bytes = dot_workspace_size(n);
   t.dot_ws = take(t.dot_ws_bytes);
@@ -330,7 +409,7 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
       for (int pass = 0; pass < 2; ++pass) {
         proj_kernel<<<blocks_for((int64_t)(j + 1) * 32), 256, 0, stream>>>(n, j + 1, W.Q, W.w, W.h);
         CARC_CHECK_LAUNCH();
-        combine_kernel<<<eb, 256, 0, stream>>>(n, j + 1, W.Q, W.h, -1.0, W.w, 0);
+        combine_kernel<<<comb_blocks(n), COMB_I * COMB_R, 0, stream>>>(n, j + 1, W.Q, W.h, -1.0, W.w, 0);
         CARC_CHECK_LAUNCH();
       }
       CARC_RETURN_IF(dot_launch(n, W.w, W.w, 1, W.nrm, W.dot_ws, W.dot_ws_bytes, stream));
@@ -340,7 +419,7 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
       ++total;
       const bool last = (j + 1 == mk);
       if ((m % 8) == 0 || last || m == n) {
-        tridiag_lowest_kernel<<<1, 32, 0, stream>>>(m, W.alpha, W.beta, W.tri_out, W.s, W.scratch);
+        tridiag_lowest_kernel<<<1, TRI_THREADS, 0, stream>>>(m, W.alpha, W.beta, W.tri_out, W.s);
         CARC_CHECK_LAUNCH();
         double hv[2];
         int bd = 0;
@@ -358,7 +437,7 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
     // Ritz vector u = Q^T s (becomes the restart vector)
     real_to_complex_kernel<<<1, 256, 0, stream>>>(m, W.s, W.h);
     CARC_CHECK_LAUNCH();
-    combine_kernel<<<eb, 256, 0, stream>>>(n, m, W.Q, W.h, 1.0, W.w, 1);
+    combine_kernel<<<comb_blocks(n), COMB_I * COMB_R, 0, stream>>>(n, m, W.Q, W.h, 1.0, W.w, 1);
     CARC_CHECK_LAUNCH();
     CARC_RETURN_IF(dot_launch(n, W.w, W.w, 1, W.nrm, W.dot_ws, W.dot_ws_bytes, stream));
     scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.nrm, W.w);
@@ -501,7 +580,8 @@ __global__ void small_eig_min_real_kernel(int k, const double2* __restrict__ A0,
     // deflation test on the last row
     double off = 0.0;
     for (int j = 0; j < m - 1; ++j) off = fmax(off, sqrt(cabs2(A[m - 1][j])));
-    if (off <= 1e-15 * scale) {
+    const double local = sqrt(cabs2(A[m - 1][m - 1])) + sqrt(cabs2(A[m - 2][m - 2]));
+    if (off <= 1e-15 * scale || off <= 2e-15 * local) {
       ev[m - 1] = A[m - 1][m - 1];
       --m;
       continue;
@@ -543,7 +623,12 @@ __global__ void small_eig_min_real_kernel(int k, const double2* __restrict__ A0,
       for (int j = 0; j < m; ++j) A[i][j] = i == j ? cadd(RQ[i][j], mu) : RQ[i][j];
   }
   if (m > 0) {
-    *status = CARC_NOT_CONVERGED;
+    // not deflated to rounding level: accept the diagonal when the remaining
+    // coupling is small (the Ritz values are then accurate to it), else fail
+    double off = 0.0;
+    for (int i = 1; i < m; ++i)
+      for (int j = 0; j < i; ++j) off = fmax(off, sqrt(cabs2(A[i][j])));
+    if (off > 1e-10 * scale) *status = CARC_NOT_CONVERGED;
     for (int i = 0; i < m; ++i) ev[i] = A[i][i];
   }
   int best = 0;
@@ -722,14 +807,29 @@ int relax_over(int n, const void* Hv, const void* Nv, const void* x0, void* x_ou
         CARC_CHECK_LAUNCH();
         CARC_CHECK_CUDA(cudaMemcpyAsync(W.K + (int64_t)(i + 1) * n, W.MK + (int64_t)i * n, (int64_t)n * 16,
                                         cudaMemcpyDeviceToDevice, stream));
-        combine_kernel<<<eb, 256, 0, stream>>>(n, i + 1, W.K, W.h, -1.0, W.K + (int64_t)(i + 1) * n, 0);
+        combine_kernel<<<comb_blocks(n), COMB_I * COMB_R, 0, stream>>>(n, i + 1, W.K, W.h, -1.0, W.K + (int64_t)(i + 1) * n, 0);
         CARC_CHECK_LAUNCH();
-        CARC_RETURN_IF(dot_launch(n, W.K + (int64_t)(i + 1) * n, W.K + (int64_t)(i + 1) * n, 1, W.scal + 2,
-                                  W.dot_ws, W.dot_ws_bytes, stream));
-        double2 nr2;
-        CARC_CHECK_CUDA(cudaMemcpyAsync(&nr2, W.scal + 2, 16, cudaMemcpyDeviceToHost, stream));
+        double2* kn = W.K + (int64_t)(i + 1) * n;
+        CARC_RETURN_IF(dot_launch(n, kn, kn, 1, W.scal + 2, W.dot_ws, W.dot_ws_bytes, stream));
+        CARC_RETURN_IF(dot_launch(n, W.MK + (int64_t)i * n, W.MK + (int64_t)i * n, 1, W.scal + 3, W.dot_ws,
+                                  W.dot_ws_bytes, stream));
+        double2 nr2[2];
+        CARC_CHECK_CUDA(cudaMemcpyAsync(nr2, W.scal + 2, 32, cudaMemcpyDeviceToHost, stream));
         CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
-        if (sqrt(std::max(nr2.x, 0.0)) <= 1e-14) {
+        if (nr2[0].x < 0.5 * nr2[1].x) {
+          // The subtraction cancelled more than half of M K[i] (the reference's own
+          // comment at utils.py:847-850 names the instability near an
+          // eigenvector): a second Gram-Schmidt pass restores orthogonality, so
+          // the projected matrix stays a Rayleigh-Ritz matrix.
+          proj_kernel<<<blocks_for((int64_t)(i + 1) * 32), 256, 0, stream>>>(n, i + 1, W.K, kn, W.h);
+          CARC_CHECK_LAUNCH();
+          combine_kernel<<<comb_blocks(n), COMB_I * COMB_R, 0, stream>>>(n, i + 1, W.K, W.h, -1.0, kn, 0);
+          CARC_CHECK_LAUNCH();
+          CARC_RETURN_IF(dot_launch(n, kn, kn, 1, W.scal + 2, W.dot_ws, W.dot_ws_bytes, stream));
+          CARC_CHECK_CUDA(cudaMemcpyAsync(nr2, W.scal + 2, 16, cudaMemcpyDeviceToHost, stream));
+          CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+        }
+        if (sqrt(std::max(nr2[0].x, 0.0)) <= 1e-14) {
           complete = true;
           kk = i + 1;
           break;
@@ -755,7 +855,7 @@ int relax_over(int n, const void* Hv, const void* Nv, const void* x0, void* x_ou
     CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
     if (sst != 0) return fail(CARC_NOT_CONVERGED, "relaxOver: projected eigenproblem did not converge");
     // x = vec . K, normalized
-    combine_kernel<<<eb, 256, 0, stream>>>(n, kk, W.K, W.vec, 1.0, W.x, 1);
+    combine_kernel<<<comb_blocks(n), COMB_I * COMB_R, 0, stream>>>(n, kk, W.K, W.vec, 1.0, W.x, 1);
     CARC_CHECK_LAUNCH();
     CARC_RETURN_IF(dot_launch(n, W.x, W.x, 1, W.scal, W.dot_ws, W.dot_ws_bytes, stream));
     scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.scal, W.x);

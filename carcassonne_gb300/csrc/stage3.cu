@@ -208,30 +208,25 @@ int stage3_matvec(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, c
                                op_entries.data(), (int)op_c.size(), make_double2(1, 0), 0, nullptr, 0, stream));
   }
 
-  // step A: W = S2_0 . Vin over (k0,k1), one W per distinct (i0, Vin) pair
+  // step A: W_g = sum_{t : i1_t = g} S2_0[i0_t] . Vin_t over (k0,k1), one W per S2_1 tag g (the
+  // grouped launch accumulates all entries of one output slot), so that step B runs once per tag
   std::vector<const void*> vin;  // slot 0 = x, then the op results
   vin.push_back(x);
   for (void* p : op_c) vin.push_back(p);
-  std::map<std::pair<int, int>, int> w_of;
+  std::vector<int> group_of_i1(n1, -1), group_i1;
   std::vector<void*> w_c;
   std::vector<int32_t> a_entries, b_entries;
-  std::vector<int> term_w(n_terms);
   for (int t = 0; t < n_terms; ++t) {
-    int i0 = terms[3 * t], io = terms[3 * t + 2];
-    int vs = io < 0 ? 0 : 1 + op_slot_of[io];
-    auto key = std::make_pair(i0, vs);
-    auto it = w_of.find(key);
-    if (it == w_of.end()) {
-      int wi = (int)w_c.size();
-      w_of[key] = wi;
-      w_c.push_back(w_base + (int64_t)wi * wl.size * 16);
-      a_entries.push_back(i0);
-      a_entries.push_back(vs);
-      a_entries.push_back(wi);
-      term_w[t] = wi;
-    } else {
-      term_w[t] = it->second;
+    const int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
+    const int vs = io < 0 ? 0 : 1 + op_slot_of[io];
+    if (group_of_i1[i1] < 0) {
+      group_of_i1[i1] = (int)w_c.size();
+      group_i1.push_back(i1);
+      w_c.push_back(w_base + (int64_t)w_c.size() * wl.size * 16);
     }
+    a_entries.push_back(i0);
+    a_entries.push_back(vs);
+    a_entries.push_back(group_of_i1[i1]);
   }
   const int64_t vk0 = s.k1 * s.k2 * s.k3 * s.d, vk1 = s.k2 * s.k3 * s.d, vk2 = s.k3 * s.d, vk3 = s.d;
   const int64_t vvec = s.nk4 * s.d;
@@ -248,12 +243,12 @@ int stage3_matvec(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, c
                               .k(s.k1, s.s0[3], vk1)
                               .d;
   CARC_RETURN_IF(gett_launch(da, s0_ptrs, n0, vin.data(), (int)vin.size(), w_c.data(), (int)w_c.size(),
-                             a_entries.data(), (int)w_c.size(), make_double2(1, 0), 0, ws_a, parts[2], stream));
+                             a_entries.data(), n_terms, make_double2(1, 0), 0, ws_a, parts[2], stream));
 
-  // step B: y += sum_t W_t . S2_1[i1_t] over (x0,x1,k2,k3)
-  for (int t = 0; t < n_terms; ++t) {
-    b_entries.push_back(term_w[t]);
-    b_entries.push_back(terms[3 * t + 1]);
+  // step B: y += sum_g W_g . S2_1[g] over (x0,x1,k2,k3)
+  for (size_t g = 0; g < w_c.size(); ++g) {
+    b_entries.push_back((int32_t)g);
+    b_entries.push_back(group_i1[g]);
     b_entries.push_back(0);
   }
   const int64_t yl3 = s.d, yl2 = s.l3 * s.d, yl1 = s.l2 * yl2, yl0 = s.l1 * yl1, yvec = s.l0 * yl0;
@@ -271,7 +266,8 @@ int stage3_matvec(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, c
                               .d;
   void* yc[1] = {y};
   CARC_RETURN_IF(gett_launch(db, (const void* const*)w_c.data(), (int)w_c.size(), s1_ptrs, n1, yc, 1,
-                             b_entries.data(), n_terms, make_double2(1, 0), accumulate, ws_b, parts[3], stream));
+                             b_entries.data(), (int)w_c.size(), make_double2(1, 0), accumulate, ws_b, parts[3],
+                             stream));
   return CARC_OK;
 }
 
