@@ -118,6 +118,7 @@ def solve_section():
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
         res[prec] = dict(seconds=statistics.median(times), energy=out["energy"], lanczos_iterations=out["iterations"],
+                         rayleigh_before_correction=out["rayleigh_before_correction"],
                          breakdown_ms={k: round(v, 3) for k, v in out["timing_ms"].items()})
     e0 = res["plain"]["energy"]
     return dict(config=dict(SOLVE, n=int(np.prod(H.operator.in_shape)), terms=len(H.operator.terms)),

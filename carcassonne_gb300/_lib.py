@@ -12,6 +12,7 @@ import threading
 
 from . import build as _build
 
+CARC_HEGV_TENSOR_CORE = 1
 CARC_OK = 0
 CARC_BAD_SHAPE = 1
 CARC_BAD_ARG = 2
@@ -77,12 +78,15 @@ SIGNATURES = {
     "carc_zpotrf_workspace_size": (_i64, [_i32]),
     "carc_ztrtri_lower": (ctypes.c_int, [_i32, _vp, _vp, _vp, _i64, _vp]),
     "carc_ztrtri_lower_workspace_size": (_i64, [_i32]),
-    "carc_zhegv_lowest": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, ctypes.POINTER(_dbl), _i32, _i32, _dbl,
-                                         ctypes.POINTER(_i32), _vp, _i64, _vp]),
-    "carc_zhegv_lowest_workspace_size": (_i64, [_i32, _i32]),
+    "carc_zhegv_lowest": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, ctypes.POINTER(_dbl), _i32, _i32, _dbl, _i32,
+                                         ctypes.POINTER(_i32), _vp, _vp, _i64, _vp]),
+    "carc_zhegv_lowest_workspace_size": (_i64, [_i32, _i32, _i32]),
     "carc_zheev_lowest_lanczos": (ctypes.c_int, [_i32, _vp, _vp, _vp, ctypes.POINTER(_dbl), _i32, _i32, _dbl,
                                                  ctypes.POINTER(_i32), _vp, _i64, _vp]),
     "carc_zheev_lowest_lanczos_workspace_size": (_i64, [_i32, _i32]),
+    "carc_zminres_projected": (ctypes.c_int, [_i32, _vp, _vp, _dbl, _vp, _vp, _i32, _dbl, ctypes.POINTER(_i32), _vp,
+                                              _i64, _vp]),
+    "carc_zminres_projected_workspace_size": (_i64, [_i32]),
     "carc_relax_over": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _i32, _i32, _dbl, ctypes.POINTER(_dbl),
                                        ctypes.POINTER(_i32), ctypes.POINTER(_dbl), _vp, _i64, _vp]),
     "carc_relax_over_workspace_size": (_i64, [_i32, _i32]),

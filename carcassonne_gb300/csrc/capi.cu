@@ -148,29 +148,44 @@ int carc_ztrtri_lower(int32_t n, const void* L, void* X, void* workspace, int64_
 
 int64_t carc_ztrtri_lower_workspace_size(int32_t n) { return trtri_workspace_size(n); }
 
-int carc_zhegv_lowest(int32_t n, const void* H, const void* N, const void* x0, void* x, double* eigenvalue,
-                      int32_t max_krylov, int32_t max_restarts, double tol, int32_t* iterations, void* workspace,
-                      int64_t workspace_bytes, void* stream) {
+int carc_zhegv_lowest(int32_t n, const void* H, const void* N, const void* x0, void* x, double* eigenvalues,
+                      int32_t max_krylov, int32_t max_restarts, double tol, int32_t flags, int32_t* iterations,
+                      void* factors, void* workspace, int64_t workspace_bytes, void* stream) {
   if (!H || !N || !x) return fail(CARC_BAD_ARG, "carc_zhegv_lowest: NULL argument");
+  if (flags & ~CARC_HEGV_TENSOR_CORE) return fail(CARC_BAD_ARG, "carc_zhegv_lowest: unknown flags 0x%x", flags);
   int it = 0;
-  int st = hegv_lowest(n, H, N, x0, x, eigenvalue, max_krylov, max_restarts, tol, &it, workspace, workspace_bytes,
-                       as_stream(stream));
+  int st = hegv_lowest(n, H, N, x0, x, eigenvalues, max_krylov, max_restarts, tol, flags, &it, factors, workspace,
+                       workspace_bytes, as_stream(stream));
   if (iterations) *iterations = it;
   return st;
 }
 
-int64_t carc_zhegv_lowest_workspace_size(int32_t n, int32_t max_krylov) { return hegv_workspace_size(n, max_krylov); }
+int64_t carc_zhegv_lowest_workspace_size(int32_t n, int32_t max_krylov, int32_t flags) {
+  return hegv_workspace_size(n, max_krylov, flags);
+}
 
-int carc_zheev_lowest_lanczos(int32_t n, const void* C, const void* u0, void* u, double* eigenvalue,
+int carc_zheev_lowest_lanczos(int32_t n, const void* C, const void* u0, void* u, double* eigenvalues,
                               int32_t max_krylov, int32_t max_restarts, double tol, int32_t* iterations,
                               void* workspace, int64_t workspace_bytes, void* stream) {
   if (!C || !u0 || !u) return fail(CARC_BAD_ARG, "carc_zheev_lowest_lanczos: NULL argument");
   int it = 0;
-  int st = lanczos_lowest(n, C, u0, u, eigenvalue, max_krylov, max_restarts, tol, &it, workspace, workspace_bytes,
+  int st = lanczos_lowest(n, C, u0, u, eigenvalues, max_krylov, max_restarts, tol, &it, workspace, workspace_bytes,
                           as_stream(stream));
   if (iterations) *iterations = it;
   return st;
 }
+
+int carc_zminres_projected(int32_t n, const void* C, const void* u, double shift, const void* b, void* z,
+                           int32_t maxit, double rtol, int32_t* iterations, void* workspace, int64_t workspace_bytes,
+                           void* stream) {
+  if (!C || !u || !b || !z) return fail(CARC_BAD_ARG, "carc_zminres_projected: NULL argument");
+  int it = 0;
+  int st = minres_projected(n, C, u, shift, b, z, maxit, rtol, &it, workspace, workspace_bytes, as_stream(stream));
+  if (iterations) *iterations = it;
+  return st;
+}
+
+int64_t carc_zminres_projected_workspace_size(int32_t n) { return minres_workspace_size(n); }
 
 int64_t carc_zheev_lowest_lanczos_workspace_size(int32_t n, int32_t max_krylov) {
   return lanczos_workspace_size(n, max_krylov);

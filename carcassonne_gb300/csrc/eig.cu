@@ -10,9 +10,11 @@
 #include "common.cuh"
 #include "contract.cuh"
 #include "linalg.cuh"
+#include "umma_gemm.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 namespace carc {
@@ -27,8 +29,16 @@ __global__ void gemv_kernel(int n, const double2* __restrict__ A, const double2*
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += warps) {
     const double2* a = A + (int64_t)row * n;
-    double2 s = make_double2(0.0, 0.0);
-    for (int j = lane; j < n; j += 32) cfma(s, a[j], x[j]);
+    double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+    int j = lane;
+    for (; j + 96 < n; j += 128) {  // four independent chains keep four loads in flight
+      cfma(s0, a[j], x[j]);
+      cfma(s1, a[j + 32], x[j + 32]);
+      cfma(s2, a[j + 64], x[j + 64]);
+      cfma(s3, a[j + 96], x[j + 96]);
+    }
+    for (; j < n; j += 32) cfma(s0, a[j], x[j]);
+    double2 s = cadd(cadd(s0, s1), cadd(s2, s3));
     s = warp_sum2(s);
     if (lane == 0) y[row] = s;
   }
@@ -41,8 +51,16 @@ __global__ void proj_kernel(int n, int rows, const double2* __restrict__ Q, cons
   const int warps = (gridDim.x * blockDim.x) >> 5;
   for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += warps) {
     const double2* q = Q + (int64_t)r * n;
-    double2 s = make_double2(0.0, 0.0);
-    for (int j = lane; j < n; j += 32) s = cadd(s, cmulc(q[j], w[j]));
+    double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+    int j = lane;
+    for (; j + 96 < n; j += 128) {
+      s0 = cadd(s0, cmulc(q[j], w[j]));
+      s1 = cadd(s1, cmulc(q[j + 32], w[j + 32]));
+      s2 = cadd(s2, cmulc(q[j + 64], w[j + 64]));
+      s3 = cadd(s3, cmulc(q[j + 96], w[j + 96]));
+    }
+    for (; j < n; j += 32) s0 = cadd(s0, cmulc(q[j], w[j]));
+    double2 s = cadd(cadd(s0, s1), cadd(s2, s3));
     s = warp_sum2(s);
     if (lane == 0) h[r] = s;
   }
@@ -143,23 +161,27 @@ __device__ int sturm_count(int m, const double* alpha, const double* beta2, T x)
 
 // Lowest eigenpair of the m x m tridiagonal matrix; out = (lambda, residual
 // estimate |beta_{m-1} s_{m-1}|), s = unit eigenvector (m).  One block of
-// TRI_THREADS threads: parallel multisection of the Gershgorin interval
-// (TRI_THREADS Sturm counts per round, first in FP32 to about 1e-6 of the
-// interval, then in FP64 to machine precision), then inverse iteration by one
-// thread on shared-memory copies.  m <= MAXM.
+// TRI_THREADS threads: parallel multisection of the Gershgorin interval in
+// FP32 (TRI_THREADS Sturm counts per round; GB300's FP64 rate makes FP64
+// counts the expensive part), then, by one thread on shared-memory copies,
+// inverse iteration in FP64 from the bracket's lower end (below the lowest
+// eigenvalue, so the iteration converges to it) and the FP64 Rayleigh
+// quotient of the iterate as the eigenvalue (quadratically accurate).
+// m <= MAXM.
 constexpr int MAXM = 512;
 constexpr int TRI_THREADS = 256;
 
+// Narrows [lo, hi] around the k-th lowest eigenvalue (k = 1, 2, ...).
 template <typename T>
 __device__ void multisect(int m, const double* a, const double* b2, double& lo, double& hi, double rel_stop,
-                          int rounds, int* s_first) {
+                          int rounds, int* s_first, int k) {
   for (int r = 0; r < rounds; ++r) {
     const double w = hi - lo;
     if (!(w > rel_stop * fmax(fabs(lo), fabs(hi))) || w <= 0.0) break;
     if (threadIdx.x == 0) *s_first = TRI_THREADS;
     __syncthreads();
     const double xt = lo + w * (double)(threadIdx.x + 1) / (double)(TRI_THREADS + 1);
-    if (sturm_count<T>(m, a, b2, (T)xt) >= 1) atomicMin(s_first, (int)threadIdx.x);
+    if (sturm_count<T>(m, a, b2, (T)xt) >= k) atomicMin(s_first, (int)threadIdx.x);
     __syncthreads();
     const int f = *s_first;
     const double nlo = f == 0 ? lo : lo + w * (double)f / (double)(TRI_THREADS + 1);
@@ -189,6 +211,7 @@ __global__ __launch_bounds__(TRI_THREADS) void tridiag_lowest_kernel(int m, cons
       s[0] = 1.0;
       out[0] = sa[0];
       out[1] = fabs(beta[0]);
+      out[2] = nan("");
     }
     return;
   }
@@ -205,21 +228,20 @@ __global__ __launch_bounds__(TRI_THREADS) void tridiag_lowest_kernel(int m, cons
   __syncthreads();
   double lo = s_lo, hi = s_hi;
   const double span = fmax(hi - lo, 1e-300);
-  multisect<float>(m, sa, sb2, lo, hi, 1e-5, 2, &s_first);
-  // FP32 counts may be off by one near the eigenvalue: widen before the FP64 rounds
-  {
-    const double w = fmax(hi - lo, 1e-7 * fmax(fabs(lo), fabs(hi)));
-    lo = fmax(s_lo, lo - 4 * w);
-    hi = fmin(s_hi, hi + 4 * w);
-  }
-  multisect<double>(m, sa, sb2, lo, hi, 1e-16, 12, &s_first);
-  const double lam = 0.5 * (lo + hi);
+  multisect<float>(m, sa, sb2, lo, hi, 1e-6, 3, &s_first, 1);
+  // the second-lowest eigenvalue to FP32 accuracy (a gap estimate for the caller)
+  double lo2 = lo, hi2 = s_hi;
+  multisect<float>(m, sa, sb2, lo2, hi2, 1e-6, 3, &s_first, 2);
   if (threadIdx.x != 0) return;
+  out[2] = 0.5 * (lo2 + hi2);
   const double scale = fmax(fmax(fabs(s_lo), fabs(s_hi)), span);
-  // inverse iteration with partial pivoting on T - (lam - delta) I
-  const double shift = lam - 1e-10 * scale;
+  // FP32 counts can be off near the eigenvalue: shift below the bracket by a
+  // margin larger than their error, so that T - shift is positive definite
+  // and the iteration is drawn to the lowest eigenvector
+  const double shift = lo - fmax(4.0 * (hi - lo), 1e-6 * scale);
   for (int i = 0; i < m; ++i) x[i] = 1.0 / sqrt((double)m) * (1.0 + 0.01 * (i % 7));
-  for (int iter = 0; iter < 3; ++iter) {
+  double lam = 0.5 * (lo + hi);
+  for (int iter = 0; iter < 4; ++iter) {
     for (int i = 0; i < m; ++i) {
       dd[i] = sa[i] - shift;
       dl[i] = sb[i];
@@ -263,20 +285,25 @@ __global__ __launch_bounds__(TRI_THREADS) void tridiag_lowest_kernel(int m, cons
       double d = dd[i] != 0.0 ? dd[i] : 1e-300 * scale;
       x[i] = v / d;
     }
-    double mx = 0.0;
-    for (int i = 0; i < m; ++i) mx = fmax(mx, fabs(x[i]));
-    if (!(mx > 0.0) || isinf(mx)) {
-      for (int i = 0; i < m; ++i) x[i] = (i == 0) ? 1.0 : 0.0;
-      mx = 1.0;
-    }
     double nrm = 0.0;
-    for (int i = 0; i < m; ++i) {
-      x[i] /= mx;
-      nrm += x[i] * x[i];
-    }
+    for (int i = 0; i < m; ++i) nrm += x[i] * x[i];
     nrm = sqrt(nrm);
-    for (int i = 0; i < m; ++i) x[i] /= nrm;
+    if (!(nrm > 0.0) || isinf(nrm)) {
+      for (int i = 0; i < m; ++i) x[i] = (i == 0) ? 1.0 : 0.0;
+      nrm = 1.0;
+    }
+    const double inv = 1.0 / nrm;
+    for (int i = 0; i < m; ++i) x[i] *= inv;
   }
+  // Rayleigh quotient x^T T x
+  double rq = 0.0;
+  for (int i = 0; i < m; ++i) {
+    double tx = sa[i] * x[i];
+    if (i > 0) tx += sb[i - 1] * x[i - 1];
+    if (i + 1 < m) tx += sb[i] * x[i + 1];
+    rq += x[i] * tx;
+  }
+  lam = rq;
   for (int i = 0; i < m; ++i) s[i] = x[i];
   out[0] = lam;
   out[1] = fabs(beta[m - 1] * x[m - 1]);
@@ -364,7 +391,7 @@ int64_t lanczos_workspace_size(int n, int max_krylov) {
   return lanczos_ws_layout(n, mk, nullptr, nullptr);
 }
 
-int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigenvalue, int max_krylov,
+int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigenvalues, int max_krylov,
                    int max_restarts, double tol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream) {
   if (n < 1) return fail(CARC_BAD_SHAPE, "lanczos: n = %d", n);
   const int mk = std::max(1, std::min(max_krylov, std::min(n, MAXM)));
@@ -380,7 +407,7 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
   scale_by_norm_kernel<<<eb, 256, 0, stream>>>(n, W.nrm, W.Q);
   CARC_CHECK_LAUNCH();
   // scale reference for the breakdown test: |C|_max row sum estimate via |C q0|
-  double lam = 0.0, res = 0.0;
+  double lam = 0.0, res = 0.0, lam2 = nan("");
   int total = 0;
   bool converged = false;
   for (int restart = 0; restart <= max_restarts && !converged; ++restart) {
@@ -421,13 +448,14 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
       if ((m % 8) == 0 || last || m == n) {
         tridiag_lowest_kernel<<<1, TRI_THREADS, 0, stream>>>(m, W.alpha, W.beta, W.tri_out, W.s);
         CARC_CHECK_LAUNCH();
-        double hv[2];
+        double hv[3];
         int bd = 0;
-        CARC_CHECK_CUDA(cudaMemcpyAsync(hv, W.tri_out, 16, cudaMemcpyDeviceToHost, stream));
+        CARC_CHECK_CUDA(cudaMemcpyAsync(hv, W.tri_out, 24, cudaMemcpyDeviceToHost, stream));
         CARC_CHECK_CUDA(cudaMemcpyAsync(&bd, W.breakdown, sizeof(int), cudaMemcpyDeviceToHost, stream));
         CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
         lam = hv[0];
         res = hv[1];
+        lam2 = hv[2];
         if (bd || res <= tol * std::max(fabs(lam), 1e-300) || m == n) {
           converged = true;
           break;
@@ -445,26 +473,69 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
     CARC_CHECK_CUDA(cudaMemcpyAsync(W.Q, W.w, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
   }
   CARC_CHECK_CUDA(cudaMemcpyAsync(u, W.w, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
-  if (eigenvalue) *eigenvalue = lam;
+  if (eigenvalues) {
+    eigenvalues[0] = lam;
+    eigenvalues[1] = lam2;
+  }
   if (iterations) *iterations = total;
   if (!converged)
     return fail(CARC_NOT_CONVERGED, "lanczos: residual %.3e after %d iterations (tolerance %.1e)", res, total, tol);
   return CARC_OK;
 }
 
-int64_t hegv_workspace_size(int n, int max_krylov) {
+namespace {
+
+// C = Li H Li^H on the tensor cores: views of the two products
+ZView hegv_view(const void* base, int n, int64_t rs, int64_t ks, int conj) {
+  ZView v;
+  memset(&v, 0, sizeof(v));
+  v.base = base;
+  v.nr = 1;
+  v.r_ext[0] = n;
+  v.r_str[0] = rs;
+  v.nk = 1;
+  v.k_ext[0] = n;
+  v.k_str[0] = ks;
+  v.conj = conj;
+  return v;
+}
+
+ZOut hegv_out(void* base, int n) {
+  ZOut o;
+  memset(&o, 0, sizeof(o));
+  o.base = base;
+  o.nm = 1;
+  o.m_ext[0] = n;
+  o.m_str[0] = n;
+  o.nn = 1;
+  o.n_ext[0] = n;
+  o.n_str[0] = 1;
+  return o;
+}
+
+constexpr int HEGV_TC_KSPLIT = 4;
+
+}  // namespace
+
+int64_t hegv_workspace_size(int n, int max_krylov, int flags) {
   int64_t mat = a256((int64_t)n * n * 16);
   carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
   int64_t g = std::max<int64_t>(gett_workspace_size(d, 1), 0);
-  int64_t sub = std::max({potrf_workspace_size(n), trtri_workspace_size(n), a256(g),
+  int64_t tc = 0;
+  if (flags & CARC_HEGV_TENSOR_CORE) {
+    const ZView a = hegv_view(nullptr, n, n, 1, 0), b = hegv_view(nullptr, n, 1, n, 0);
+    tc = zgemm_tc_workspace(a, b, HEGV_TC_KSPLIT);
+  }
+  int64_t sub = std::max({potrf_workspace_size(n), trtri_workspace_size(n), a256(g), a256(tc),
                           lanczos_workspace_size(n, max_krylov)});
   return 4 * mat + 2 * a256((int64_t)n * 16) + a256(64) + sub;
 }
 
-int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, double* eigenvalue, int max_krylov,
-                int max_restarts, double tol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream) {
+int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, double* eigenvalues, int max_krylov,
+                int max_restarts, double tol, int flags, int* iterations, void* factors, void* ws, int64_t ws_bytes,
+                cudaStream_t stream) {
   if (n < 1) return fail(CARC_BAD_SHAPE, "hegv: n = %d", n);
-  if (ws_bytes < hegv_workspace_size(n, max_krylov)) return fail(CARC_BAD_ARG, "hegv: workspace too small");
+  if (ws_bytes < hegv_workspace_size(n, max_krylov, flags)) return fail(CARC_BAD_ARG, "hegv: workspace too small");
   char* p = static_cast<char*>(ws);
   int64_t mat = a256((int64_t)n * n * 16);
   double2* Lm = (double2*)p;
@@ -485,7 +556,13 @@ int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, d
   if (hstat != CARC_OK) return fail(CARC_NOT_POSDEF, "hegv: the normalization matrix is not positive definite");
   CARC_RETURN_IF(trtri_lower(n, Lm, Li, sub, sub_bytes, stream));
   // T1 = Linv H ; C = T1 Linv^H
-  {
+  if (flags & CARC_HEGV_TENSOR_CORE) {
+    // T1[m][n] = sum_k Li[m][k] H[k][n];  C[m][n] = sum_k T1[m][k] conj(Li[n][k])
+    CARC_RETURN_IF(zgemm_tc(hegv_view(Li, n, n, 1, 0), hegv_view(H, n, 1, n, 0), hegv_out(T1, n), make_double2(1, 0),
+                            0, HEGV_TC_KSPLIT, sub, sub_bytes, status, stream));
+    CARC_RETURN_IF(zgemm_tc(hegv_view(T1, n, n, 1, 0), hegv_view(Li, n, n, 1, 1), hegv_out(Cm, n),
+                            make_double2(1, 0), 0, HEGV_TC_KSPLIT, sub, sub_bytes, status, stream));
+  } else {
     carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
     const void* pa[1] = {Li};
     const void* pb[1] = {H};
@@ -516,8 +593,13 @@ int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, d
   // previous center) would otherwise keep Lanczos out of its sector.
   perturb_start_kernel<<<1, 256, 0, stream>>>(n, u0, x0 ? 1e-3 : 1.0);  // one block: reads finish before writes
   CARC_CHECK_LAUNCH();
-  int st = lanczos_lowest(n, Cm, u0, u, eigenvalue, max_krylov, max_restarts, tol, iterations, sub, sub_bytes, stream);
+  int st = lanczos_lowest(n, Cm, u0, u, eigenvalues, max_krylov, max_restarts, tol, iterations, sub, sub_bytes, stream);
   if (st != CARC_OK && st != CARC_NOT_CONVERGED) return st;
+  if (flags & CARC_HEGV_TENSOR_CORE) {
+    CARC_CHECK_CUDA(cudaMemcpyAsync(&hstat, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+    if (hstat != CARC_OK) return fail(CARC_NOT_CONVERGED, "hegv: a tensor-core pipeline wait timed out");
+  }
   // x = Linv^H u : x[j] = sum_i conj(Li[i][j]) u[i]
   {
     carc_contract_desc d = DescBuilder().m(n, 1, 1).k(n, n, 1).d;
@@ -527,6 +609,14 @@ int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, d
     void* pc[1] = {x};
     int32_t e[3] = {0, 0, 0};
     CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+  }
+  if (factors) {
+    // [C = L^-1 H L^-H | L^-1 | u], for corrections against the same reduced pencil
+    double2* f = static_cast<double2*>(factors);
+    const int64_t nn = (int64_t)n * n;
+    CARC_CHECK_CUDA(cudaMemcpyAsync(f, Cm, nn * 16, cudaMemcpyDeviceToDevice, stream));
+    CARC_CHECK_CUDA(cudaMemcpyAsync(f + nn, Li, nn * 16, cudaMemcpyDeviceToDevice, stream));
+    CARC_CHECK_CUDA(cudaMemcpyAsync(f + 2 * nn, u, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
   }
   return st;
 }
@@ -885,6 +975,216 @@ int relax_over(int n, const void* Hv, const void* Nv, const void* x0, void* x_ou
     have_last = true;
   }
   return fail(CARC_NOT_CONVERGED, "relaxOver: restart budget spent");
+}
+
+
+// ---------------------------------------------------------------------------
+// MINRES for the projected shifted system  P (C - shift) P z = P b,
+// P = I - u u^H (u unit), C dense Hermitian n x n: the correction equation of
+// a Newton step on an approximate pencil (mixed-precision center solve).
+// The Paige-Saunders recurrence scalars stay on the device (double-buffered
+// state, recomputed by every thread of the update kernel); the host checks
+// convergence every MINRES_CHECK iterations.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct MinresState {
+  double beta, oldb, dbar, epsln, phibar, cs, sn;
+  double rtol_abs;  // stop when phibar <= rtol_abs
+  int done;
+  int pad;
+};
+
+constexpr int MINRES_CHECK = 8;
+
+__global__ void minres_scale_kernel(int n, const MinresState* __restrict__ st, const double2* __restrict__ y,
+                                    double2* __restrict__ v) {
+  if (st->done) return;
+  const double inv = 1.0 / st->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v[i] = cscale(y[i], inv);
+}
+
+// y = t - shift v - (u^H t) u - [itn > 0] (beta / oldb) r1
+__global__ void minres_combo1_kernel(int n, int itn, const MinresState* __restrict__ st, double shift,
+                                     const double2* __restrict__ t, const double2* __restrict__ v,
+                                     const double2* __restrict__ u, const double2* __restrict__ ut,
+                                     const double2* __restrict__ r1, double2* __restrict__ y) {
+  if (st->done) return;
+  const double2 c = *ut;
+  const double f = itn > 0 ? st->beta / st->oldb : 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double2 a = csub(csub(t[i], cscale(v[i], shift)), cmul(c, u[i]));
+    if (itn > 0) a = csub(a, cscale(r1[i], f));
+    y[i] = a;
+  }
+}
+
+// out = y - (alfa / beta) r2
+__global__ void minres_combo2_kernel(int n, const MinresState* __restrict__ st, const double2* __restrict__ alfa,
+                                     const double2* __restrict__ y, const double2* __restrict__ r2,
+                                     double2* __restrict__ out) {
+  if (st->done) return;
+  const double f = alfa->x / st->beta;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) out[i] = csub(y[i], cscale(r2[i], f));
+}
+
+// recurrence step; w_new = (v - oldeps wa - delta wb) / gamma written over wa
+// (wa: direction of two iterations ago, wb: of the last one); x += phi w_new
+__global__ void minres_update_kernel(int n, const MinresState* __restrict__ sin, MinresState* __restrict__ sout,
+                                     const double2* __restrict__ alfa_c, const double2* __restrict__ beta2_c,
+                                     const double2* __restrict__ v, double2* __restrict__ wa,
+                                     const double2* __restrict__ wb, double2* __restrict__ x) {
+  MinresState s = *sin;
+  if (s.done) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *sout = s;
+    return;
+  }
+  const double alfa = alfa_c->x;
+  const double beta = sqrt(fmax(beta2_c->x, 0.0));
+  const double oldeps = s.epsln;
+  const double delta = s.cs * s.dbar + s.sn * alfa;
+  const double gbar = s.sn * s.dbar - s.cs * alfa;
+  const double epsln = s.sn * beta;
+  const double dbar = -s.cs * beta;
+  const double gamma = fmax(hypot(gbar, beta), 1e-300);
+  const double cs = gbar / gamma, sn = beta / gamma;
+  const double phi = cs * s.phibar;
+  const double phibar = sn * s.phibar;
+  const double ig = 1.0 / gamma;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double2 wn = cscale(csub(csub(v[i], cscale(wa[i], oldeps)), cscale(wb[i], delta)), ig);
+    wa[i] = wn;
+    x[i] = cadd(x[i], cscale(wn, phi));
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    MinresState o = s;
+    o.oldb = s.beta;
+    o.beta = beta;
+    o.epsln = epsln;
+    o.dbar = dbar;
+    o.cs = cs;
+    o.sn = sn;
+    o.phibar = phibar;
+    o.done = (beta == 0.0 || phibar <= s.rtol_abs) ? 1 : 0;
+    *sout = o;
+  }
+}
+
+__global__ void minres_init_kernel(MinresState* st, const double2* __restrict__ b2, double rtol) {
+  const double beta1 = sqrt(fmax(b2->x, 0.0));
+  MinresState s;
+  s.beta = beta1;
+  s.oldb = 0.0;
+  s.dbar = 0.0;
+  s.epsln = 0.0;
+  s.phibar = beta1;
+  s.cs = -1.0;
+  s.sn = 0.0;
+  s.rtol_abs = rtol * beta1;
+  s.done = beta1 == 0.0 ? 1 : 0;
+  s.pad = 0;
+  st[0] = s;
+  st[1] = s;
+}
+
+// b -= (u^H b) u
+__global__ void project_out_kernel(int n, const double2* __restrict__ u, const double2* __restrict__ ub,
+                                   double2* __restrict__ b) {
+  const double2 c = *ub;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) b[i] = csub(b[i], cmul(c, u[i]));
+}
+
+int64_t minres_ws_layout(int n, double2** vecs, MinresState** st, double2** scal, void** dot_ws, int64_t* dot_bytes,
+                         void* base) {
+  char* p = static_cast<char*>(base);
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) {
+    void* r = p ? p + off : nullptr;
+    off += a256(bytes);
+    return r;
+  };
+  for (int i = 0; i < 8; ++i) {
+    void* q = take((int64_t)n * 16);
+    if (vecs) vecs[i] = static_cast<double2*>(q);
+  }
+  void* s = take(2 * sizeof(MinresState));
+  void* c = take(4 * 16);
+  const int64_t db = dot_workspace_size(n);
+  void* d = take(db);
+  if (st) *st = static_cast<MinresState*>(s);
+  if (scal) *scal = static_cast<double2*>(c);
+  if (dot_ws) *dot_ws = d;
+  if (dot_bytes) *dot_bytes = db;
+  return off;
+}
+
+}  // namespace
+
+int64_t minres_workspace_size(int n) { return minres_ws_layout(n, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr); }
+
+int minres_projected(int n, const void* Cv, const void* uv, double shift, const void* bv, void* zv, int maxit,
+                     double rtol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream) {
+  if (n < 1) return fail(CARC_BAD_SHAPE, "minres: n = %d", n);
+  if (ws_bytes < minres_workspace_size(n)) return fail(CARC_BAD_ARG, "minres: workspace too small");
+  double2* V[8];
+  MinresState* st;
+  double2* scal;
+  void* dws;
+  int64_t dbytes;
+  minres_ws_layout(n, V, &st, &scal, &dws, &dbytes, ws);
+  const double2* C = static_cast<const double2*>(Cv);
+  const double2* u = static_cast<const double2*>(uv);
+  double2* z = static_cast<double2*>(zv);
+  // y: scratch; r1, r2: the two latest Lanczos residuals; wa, wb: the
+  // search directions of two iterations ago and of the last one
+  double2 *y = V[0], *r1 = V[1], *r2 = V[2], *v = V[3], *t = V[4], *wa = V[5], *wb = V[6];
+  const int eb = blocks_for(n);
+  const int gb = blocks_for((int64_t)n * 32);
+  // r1 = r2 = P b; z = wa = wb = 0
+  CARC_CHECK_CUDA(cudaMemcpyAsync(r2, bv, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+  CARC_RETURN_IF(dot_launch(n, u, r2, 1, scal, dws, dbytes, stream));
+  project_out_kernel<<<eb, 256, 0, stream>>>(n, u, scal, r2);
+  CARC_CHECK_LAUNCH();
+  CARC_CHECK_CUDA(cudaMemcpyAsync(r1, r2, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+  CARC_RETURN_IF(fill_launch(n, make_double2(0, 0), z, stream));
+  CARC_RETURN_IF(fill_launch(n, make_double2(0, 0), wa, stream));
+  CARC_RETURN_IF(fill_launch(n, make_double2(0, 0), wb, stream));
+  CARC_RETURN_IF(dot_launch(n, r2, r2, 1, scal + 1, dws, dbytes, stream));
+  minres_init_kernel<<<1, 1, 0, stream>>>(st, scal + 1, rtol);
+  CARC_CHECK_LAUNCH();
+  int itn = 0;
+  for (; itn < maxit; ++itn) {
+    MinresState* sin = st + (itn & 1);
+    MinresState* sout = st + ((itn + 1) & 1);
+    minres_scale_kernel<<<eb, 256, 0, stream>>>(n, sin, r2, v);
+    CARC_CHECK_LAUNCH();
+    gemv_kernel<<<gb, 256, 0, stream>>>(n, C, v, t);
+    CARC_CHECK_LAUNCH();
+    CARC_RETURN_IF(dot_launch(n, u, t, 1, scal + 2, dws, dbytes, stream));
+    minres_combo1_kernel<<<eb, 256, 0, stream>>>(n, itn, sin, shift, t, v, u, scal + 2, r1, y);
+    CARC_CHECK_LAUNCH();
+    CARC_RETURN_IF(dot_launch(n, v, y, 1, scal + 3, dws, dbytes, stream));
+    // new residual y - (alfa/beta) r2 into r1's buffer, then r1 <- r2, r2 <- new
+    minres_combo2_kernel<<<eb, 256, 0, stream>>>(n, sin, scal + 3, y, r2, r1);
+    CARC_CHECK_LAUNCH();
+    std::swap(r1, r2);
+    CARC_RETURN_IF(dot_launch(n, r2, r2, 1, scal + 1, dws, dbytes, stream));
+    // new direction (v - oldeps wa - delta wb) / gamma into wa's buffer, then swap
+    minres_update_kernel<<<eb, 256, 0, stream>>>(n, sin, sout, scal + 3, scal + 1, v, wa, wb, z);
+    CARC_CHECK_LAUNCH();
+    std::swap(wa, wb);
+    if ((itn + 1) % MINRES_CHECK == 0 || itn + 1 == maxit) {
+      MinresState h;
+      CARC_CHECK_CUDA(cudaMemcpyAsync(&h, sout, sizeof(h), cudaMemcpyDeviceToHost, stream));
+      CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+      if (h.done) {
+        ++itn;
+        break;
+      }
+    }
+  }
+  if (iterations) *iterations = itn;
+  return CARC_OK;
 }
 
 }  // namespace carc

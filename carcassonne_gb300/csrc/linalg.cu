@@ -509,25 +509,55 @@ int potrf(int n, void* Av, void* status, void* ws, int64_t ws_bytes, cudaStream_
 // ---------------------------------------------------------------------------
 namespace {
 
-// X[k0:k0+nb, :] = L_kk^{-1} B[k0:k0+nb, :] for columns col < k0+nb (X is lower), in place in X.
-__global__ void trsm_diag_kernel(int n, const double2* __restrict__ Lm, double2* __restrict__ X, int k0, int nb) {
+// X[k0:k0+nb, :] = L_kk^{-1} X[k0:k0+nb, :] for columns col < k0+nb (X is
+// lower), in place.  Each block inverts the nb x nb diagonal block in shared
+// memory (one thread per column of the inverse, forward substitution with the
+// diagonal's reciprocals) and applies it to its 16 columns of X, 16 row groups
+// of threads sharing the work: the columns are independent, so the whole
+// update is parallel over (row, column).
+constexpr int TRSM_COLS = 16, TRSM_ROWG = 16;
+__global__ __launch_bounds__(TRSM_COLS * TRSM_ROWG) void trsm_diag_kernel(int n, const double2* __restrict__ Lm,
+                                                                          double2* __restrict__ X, int k0, int nb) {
   __shared__ double2 Lk[NB][NB + 1];
+  __shared__ double2 Li[NB][NB + 1];
+  __shared__ double2 dinv[NB];
+  __shared__ double2 Xs[NB][TRSM_COLS + 1];
   for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) {
     int i = idx / nb, j = idx % nb;
     Lk[i][j] = Lm[(int64_t)(k0 + i) * n + k0 + j];
   }
   __syncthreads();
-  for (int col = blockIdx.x * blockDim.x + threadIdx.x; col < k0 + nb; col += gridDim.x * blockDim.x) {
-    double2 x[NB];
-    for (int i = 0; i < nb; ++i) x[i] = X[(int64_t)(k0 + i) * n + col];
-    for (int i = 0; i < nb; ++i) {
-      double2 s = x[i];
-      for (int j = 0; j < i; ++j) s = csub(s, cmul(Lk[i][j], x[j]));
-      double2 d = Lk[i][i];
-      double den = cabs2(d);
-      x[i] = make_double2((s.x * d.x + s.y * d.y) / den, (s.y * d.x - s.x * d.y) / den);
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    const double2 d = Lk[i][i];
+    const double den = cabs2(d);
+    dinv[i] = make_double2(d.x / den, -d.y / den);
+  }
+  __syncthreads();
+  // column c of L_kk^{-1}: solve L y = e_c (rows < c are zero)
+  for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+    for (int i = 0; i < c; ++i) Li[i][c] = make_double2(0.0, 0.0);
+    Li[c][c] = dinv[c];
+    for (int i = c + 1; i < nb; ++i) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int j = c; j < i; ++j) acc = cadd(acc, cmul(Lk[i][j], Li[j][c]));
+      Li[i][c] = cmul(dinv[i], make_double2(-acc.x, -acc.y));
     }
-    for (int i = 0; i < nb; ++i) X[(int64_t)(k0 + i) * n + col] = x[i];
+  }
+  const int tc = threadIdx.x % TRSM_COLS, tr = threadIdx.x / TRSM_COLS;
+  const int cols = k0 + nb;
+  for (int c0 = blockIdx.x * TRSM_COLS; c0 < cols; c0 += gridDim.x * TRSM_COLS) {
+    const int col = c0 + tc;
+    __syncthreads();
+    for (int i = tr; i < nb; i += TRSM_ROWG)
+      Xs[i][tc] = col < cols ? X[(int64_t)(k0 + i) * n + col] : make_double2(0.0, 0.0);
+    __syncthreads();
+    if (col < cols) {
+      for (int i = tr; i < nb; i += TRSM_ROWG) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int j = 0; j <= i; ++j) cfma(acc, Li[i][j], Xs[j][tc]);
+        X[(int64_t)(k0 + i) * n + col] = acc;
+      }
+    }
   }
 }
 
@@ -561,7 +591,8 @@ int trtri_lower(int n, const void* Lv, void* Xv, void* ws, int64_t ws_bytes, cud
       CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(-1.0, 0.0), 1, ws, ws_bytes, stream));
     }
     int cols = k0 + nb;
-    trsm_diag_kernel<<<(int)std::max<int64_t>(1, ceil_div(cols, 128)), 128, 0, stream>>>(n, Lm, X, k0, nb);
+    trsm_diag_kernel<<<(int)std::max<int64_t>(1, ceil_div(cols, TRSM_COLS)), TRSM_COLS * TRSM_ROWG, 0, stream>>>(
+        n, Lm, X, k0, nb);
     CARC_CHECK_LAUNCH();
   }
   return CARC_OK;

@@ -13,10 +13,14 @@ int64_t potrf_workspace_size(int n);
 int potrf(int n, void* A, void* status, void* ws, int64_t ws_bytes, cudaStream_t stream);
 int64_t trtri_workspace_size(int n);
 int trtri_lower(int n, const void* L, void* X, void* ws, int64_t ws_bytes, cudaStream_t stream);
-int64_t hegv_workspace_size(int n, int max_krylov);
-int hegv_lowest(int n, const void* H, const void* N, const void* x0, void* x, double* eigenvalue, int max_krylov,
-                int max_restarts, double tol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream);
-int lanczos_lowest(int n, const void* C, const void* u0, void* u, double* eigenvalue, int max_krylov,
+int64_t hegv_workspace_size(int n, int max_krylov, int flags);
+int hegv_lowest(int n, const void* H, const void* N, const void* x0, void* x, double* eigenvalues, int max_krylov,
+                int max_restarts, double tol, int flags, int* iterations, void* factors, void* ws, int64_t ws_bytes,
+                cudaStream_t stream);
+int64_t minres_workspace_size(int n);
+int minres_projected(int n, const void* C, const void* u, double shift, const void* b, void* z, int maxit,
+                     double rtol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream);
+int lanczos_lowest(int n, const void* C, const void* u0, void* u, double* eigenvalues, int max_krylov,
                    int max_restarts, double tol, int* iterations, void* ws, int64_t ws_bytes, cudaStream_t stream);
 int64_t lanczos_workspace_size(int n, int max_krylov);
 int64_t relax_workspace_size(int n, int k);

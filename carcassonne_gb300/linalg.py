@@ -152,8 +152,14 @@ def tri_inverse_lower(L):
     return TorchData(X)
 
 
-def hegv_lowest(H, N, x0=None, tol=1e-13, max_krylov=256, max_restarts=8):
-    """Lowest eigenpair of H x = l N x; returns (l, x, iterations), x N-normalized."""
+def hegv_lowest(H, N, x0=None, tol=1e-13, max_krylov=256, max_restarts=8, tensor_core=False, with_second=False,
+                factors=None):
+    """Lowest eigenpair of H x = l N x; returns (l, x, iterations), x N-normalized
+    (with_second: (l, x, iterations, l2), l2 the second-lowest Ritz value, a
+    gap estimate to about 1e-6).  factors: a complex128 device tensor of
+    2 n^2 + n elements that receives [C = L^-1 H L^-H | L^-1 | u].
+    tensor_core: reduce the pencil with the split-BF16 tensor-core GEMM
+    (~1e-5 relative; for pencils that are tensor-core approximations)."""
     Ht = (H._t if isinstance(H, TorchData) else TorchData(H)._t).contiguous()
     Nt = (N._t if isinstance(N, TorchData) else TorchData(N)._t).contiguous()
     n = Ht.shape[0]
@@ -162,17 +168,39 @@ def hegv_lowest(H, N, x0=None, tol=1e-13, max_krylov=256, max_restarts=8):
     x0t = None
     if x0 is not None:
         x0t = (x0._t if isinstance(x0, TorchData) else TorchData(x0)._t).reshape(-1).contiguous()
-    ws_bytes = lib.carc_zhegv_lowest_workspace_size(n, max_krylov)
+    flags = _lib.CARC_HEGV_TENSOR_CORE if tensor_core else 0
+    ws_bytes = lib.carc_zhegv_lowest_workspace_size(n, max_krylov, flags)
     ws = engine.Workspace.get(ws_bytes, Ht.device)
-    lam = ctypes.c_double(0.0)
+    lam = (ctypes.c_double * 2)(0.0, 0.0)
     iters = ctypes.c_int32(0)
-    st = lib.carc_zhegv_lowest(n, _vp(Ht), _vp(Nt), _vp(x0t) if x0t is not None else None, _vp(x), ctypes.byref(lam),
-                               max_krylov, max_restarts, float(tol), ctypes.byref(iters), _vp(ws), ws_bytes,
+    st = lib.carc_zhegv_lowest(n, _vp(Ht), _vp(Nt), _vp(x0t) if x0t is not None else None, _vp(x), lam,
+                               max_krylov, max_restarts, float(tol), flags, ctypes.byref(iters),
+                               _vp(factors) if factors is not None else None, _vp(ws), ws_bytes,
                                current_stream_handle())
     if st == _lib.CARC_NOT_POSDEF:
         raise np.linalg.LinAlgError(lib.carc_last_error_string().decode())
     _lib.check(st)
-    return lam.value, TorchData(x), iters.value
+    if with_second:
+        return lam[0], TorchData(x), iters.value, lam[1]
+    return lam[0], TorchData(x), iters.value
 
 
-__all__ = ["svd", "unitize", "normalize_axis", "qr", "qr_economic", "eigh_small", "cholesky", "tri_inverse_lower", "hegv_lowest"]
+def minres_projected(C, u, shift, b, maxit=60, rtol=1e-3):
+    """z solving P (C - shift) P z = P b, P = I - u u^H (u unit), C dense
+    Hermitian: MINRES on the device.  Returns (z, iterations)."""
+    Ct = (C._t if isinstance(C, TorchData) else C).contiguous()
+    ut = (u._t if isinstance(u, TorchData) else u).reshape(-1).contiguous()
+    bt = (b._t if isinstance(b, TorchData) else b).reshape(-1).contiguous()
+    n = Ct.shape[0]
+    lib = _lib.load()
+    z = torch.empty((n,), dtype=CDT, device=Ct.device)
+    ws_bytes = lib.carc_zminres_projected_workspace_size(n)
+    ws = engine.Workspace.get(ws_bytes, Ct.device)
+    iters = ctypes.c_int32(0)
+    _lib.check(lib.carc_zminres_projected(n, _vp(Ct), _vp(ut), float(shift), _vp(bt), _vp(z), int(maxit), float(rtol),
+                                          ctypes.byref(iters), _vp(ws), ws_bytes, current_stream_handle()))
+    return z, iters.value
+
+
+__all__ = ["svd", "unitize", "normalize_axis", "qr", "qr_economic", "eigh_small", "cholesky", "tri_inverse_lower",
+           "hegv_lowest", "minres_projected"]

@@ -3,11 +3,12 @@
 plain  : H_eff and N_eff formed in FP64 on the CUDA cores, lowest generalized
          eigenpair by the Cholesky-reduced restarted Lanczos (linalg.hegv_lowest).
 mixed  : H_eff and N_eff formed on the tensor cores from split-BF16 operands
-         (~1e-5 relative), the same eigensolver on them; the energy is the FP64
-         Rayleigh quotient of that eigenvector with the exact operators (one
-         FP64 application of each), whose error is quadratic in the
-         eigenvector's; optional Rayleigh-Ritz steps on span{x, t}, t the FP64
-         residual H x - E N x, also refine the vector.
+         (~1e-5 relative), the pencil reduced with tensor-core GEMMs and the
+         same Lanczos on it (to 1e-7); then one FP64 application of H and N
+         gives the exact residual of that eigenvector, one Newton step against
+         the tensor-core pencil (MINRES on its reduced form) corrects the
+         vector, and the energy is the Rayleigh quotient of the corrected
+         vector (exact first-order terms, tensor-core second-order terms).
 
 Both return the energy, the N-normalized center and a breakdown of where the
 time went (CUDA events on the current stream).
@@ -49,58 +50,67 @@ def _lin(a, x, b, y):
     return TorchData(x)._axpby(a, TorchData(x), b, TorchData(y))._t
 
 
-def _refine(Hop, Nop, x):
-    """One Rayleigh-Ritz step with the FP64 operators on span{x, r},
-    r = H x - E N x the FP64 residual; the 2x2 pencil is solved by the GPU
-    generalized eigensolver."""
-    shp = Hop.in_shape
-    xx = x.reshape(-1)
-    Hx = Hop.apply(x.reshape(shp)).reshape(-1)
-    Nx = Nop.apply(x.reshape(shp)).reshape(-1)
-    e = (_dot(xx, Hx) / _dot(xx, Nx)).real
-    r = _lin(1.0, Hx, -e, Nx)
-    rn = abs(_dot(r, r)) ** 0.5
-    if rn == 0.0:
-        return e, x
-    tt = _lin(1.0 / rn, r, 0.0, r)
-    Ht = Hop.apply(tt.reshape(shp)).reshape(-1)
-    Nt = Nop.apply(tt.reshape(shp)).reshape(-1)
-    hxt, nxt = _dot(xx, Ht), _dot(xx, Nt)
-    Hs = np.array([[_dot(xx, Hx).real, hxt], [np.conj(hxt), _dot(tt, Ht).real]], np.complex128)
-    Ns = np.array([[_dot(xx, Nx).real, nxt], [np.conj(nxt), _dot(tt, Nt).real]], np.complex128)
-    try:
-        lam2, c, _ = linalg.hegv_lowest(TorchData(Hs), TorchData(Ns), max_krylov=2)
-    except (np.linalg.LinAlgError, RuntimeError):
-        return e, x
-    cc = c.toArray()
-    y = _lin(complex(cc[0]), xx, complex(cc[1]), tt)
-    Ny = _lin(complex(cc[0]), Nx, complex(cc[1]), Nt)
-    Hy = _lin(complex(cc[0]), Hx, complex(cc[1]), Ht)
-    e2 = (_dot(y, Hy) / _dot(y, Ny)).real
-    if not (e2 <= e):
-        return e, x
-    nrm = abs(_dot(y, Ny)) ** 0.5
-    return e2, _lin(1.0 / nrm, y, 0.0, y)
+def _apply(op, x):
+    return op.apply(x.reshape(op.in_shape)).reshape(-1)
 
 
-def _rayleigh(Hop, Nop, x):
-    """FP64 Rayleigh quotient of x and x N-normalized with the FP64 operators."""
-    shp = Hop.in_shape
+def _mv(A, v):
+    """A v for a dense (n, n) device matrix (one strided contraction launch)."""
+    return TorchData(A).contractWith(TorchData(v), (1,), (0,))._t
+
+
+def _mhv(A, v):
+    """A^H v."""
+    return TorchData(A).conj().contractWith(TorchData(v), (0,), (0,))._t
+
+
+def _norm(v):
+    return abs(_dot(v, v)) ** 0.5
+
+
+def _correct(Hop, Nop, x, Ht, Nt, factors):
+    """Energy and vector from the tensor-core eigenvector x, recovered to FP64
+    accuracy with one FP64 application of H and N.
+
+    r = H x - E N x is the exact residual.  One Newton step against the
+    tensor-core pencil (H~ - E N~) delta = -r, taken in the reduced
+    coordinates (C~ - E) z = -L^-1 r with z orthogonal to u (the Lanczos
+    eigenvector of C~, which x maps to) and solved by MINRES on the device
+    (linalg.minres_projected), moves the
+    eigenvector error from eps/gap to (eps/gap)^2, eps ~ 1e-5 the pencil's
+    error.  The new Rayleigh quotient uses the exact H x, N x and the
+    tensor-core matrices only for the second-order terms delta^H H~ delta,
+    delta^H N~ delta (error eps |delta|^2): no second FP64 application."""
+    n = Ht.shape[0]
+    C = factors[: n * n].reshape(n, n)
+    Li = factors[n * n: 2 * n * n].reshape(n, n)
+    u = factors[2 * n * n:]
     xf = x.reshape(-1)
-    hx = Hop.apply(x.reshape(shp)).reshape(-1)
-    nx = Nop.apply(x.reshape(shp)).reshape(-1)
+    hx, nx = _apply(Hop, xf), _apply(Nop, xf)
     nn = _dot(xf, nx).real
-    e = _dot(xf, hx).real / nn
-    return e, _lin(1.0 / abs(nn) ** 0.5, xf, 0.0, xf)
+    xhx = _dot(xf, hx).real
+    e = xhx / nn
+    r = _lin(1.0, hx, -e, nx)
+    uu = _lin(1.0 / _norm(u), u, 0.0, u)
+    b = _lin(-1.0, _mv(Li, r), 0.0, r)
+    z, _ = linalg.minres_projected(C, uu, e, b, maxit=60, rtol=1e-3)
+    d = _mhv(Li, z)
+    hd, nd = _mv(Ht, d), _mv(Nt, d)
+    num = xhx + 2.0 * _dot(d, hx).real + _dot(d, hd).real
+    den = nn + 2.0 * _dot(d, nx).real + _dot(d, nd).real
+    x2 = _lin(1.0, xf, 1.0, d)
+    return num / den, _lin(1.0 / abs(den) ** 0.5, x2, 0.0, x2), e
 
 
-def solve_center(H, N, x0=None, precision="plain", refine_steps=0, tol=1e-13):
+def solve_center(H, N, x0=None, precision="plain", tol=None):
     """Lowest eigenpair of (H_eff, N_eff) given the two stage-3 Multipliers.
 
     mixed: the eigenvector of the tensor-core pencil is accurate to about the
-    operands' 1e-5, so the FP64 Rayleigh quotient of it is accurate to about
-    1e-10 (quadratic); ``refine_steps`` > 0 adds Rayleigh-Ritz steps with the
-    FP64 residual that also improve the vector."""
+    operands' 1e-5 over the gap; one Newton correction against the same
+    pencil with the exact FP64 residual (``_correct``) recovers FP64-level
+    energies.  ``tol`` is the Lanczos residual tolerance (default 1e-13
+    plain; 1e-7 mixed: the tensor-core pencil's own error, which the Newton
+    correction removes, dominates the eigenvector's below that)."""
     Hop, Nop = getattr(H, "operator", None), N.operator
     timer = _Timer()
     timer.mark("start")
@@ -111,7 +121,7 @@ def solve_center(H, N, x0=None, precision="plain", refine_steps=0, tol=1e-13):
         nrm = abs(_dot(xt.reshape(-1), Nop.apply(xt).reshape(-1))) ** 0.5
         timer.mark("eigensolve")
         return dict(energy=0.0, center=TorchData(_lin(1.0 / nrm, xt, 0.0, xt)), iterations=0,
-                    timing_ms=timer.breakdown(), lanczos_eigenvalue=0.0)
+                    timing_ms=timer.breakdown(), lanczos_eigenvalue=0.0, rayleigh_before_correction=None)
     if precision == "plain":
         Hm = Hop.form_matrix()
         Nm = Nop.form_matrix()
@@ -121,22 +131,27 @@ def solve_center(H, N, x0=None, precision="plain", refine_steps=0, tol=1e-13):
     else:
         raise ValueError("precision must be 'plain' or 'mixed'")
     timer.mark("form")
-    lam, x, iters = linalg.hegv_lowest(TorchData(Hm), TorchData(Nm), x0=x0, tol=tol)
+    if tol is None:
+        tol = 1e-7 if precision == "mixed" else 1e-13
+    factors = None
+    if precision == "mixed":
+        n = Hm.shape[0]
+        factors = torch.empty(2 * n * n + n, dtype=CDT, device=Hm.device)
+    lam, x, iters = linalg.hegv_lowest(TorchData(Hm), TorchData(Nm), x0=x0, tol=tol,
+                                       tensor_core=(precision == "mixed"), factors=factors)
     timer.mark("eigensolve")
     xt = x._t
     energy = lam
+    rq0 = None
     if precision == "mixed":
         Hop.check_status()
         Nop.check_status()
-        for _ in range(refine_steps):
-            e, xt = _refine(Hop, Nop, xt)
-        # FP64 Rayleigh quotient and N-normalization with the exact operators
-        energy, xt = _rayleigh(Hop, Nop, xt)
+        energy, xt, rq0 = _correct(Hop, Nop, xt, Hm, Nm, factors)
         energy = float(energy)
         timer.mark("refine")
     out = TorchData(xt.reshape(Hop.in_shape))
     return dict(energy=float(energy), center=out, iterations=iters, timing_ms=timer.breakdown(),
-                lanczos_eigenvalue=float(lam))
+                lanczos_eigenvalue=float(lam), rayleigh_before_correction=rq0 if precision == "mixed" else None)
 
 
 __all__ = ["solve_center"]

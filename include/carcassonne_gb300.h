@@ -284,20 +284,39 @@ int64_t carc_ztrtri_lower_workspace_size(int32_t n);
  * definite, both n x n): Cholesky of N, C = L^-1 H L^-H, restarted Lanczos
  * with full reorthogonalisation from u0 = L^H x0 (x0 may be NULL), stopping
  * when |beta_m s_m| <= tol |l|; x is N-normalized (x^H N x = 1).
- * *eigenvalue and *iterations are HOST pointers.  The call synchronizes the
+ * eigenvalues (HOST, 2 doubles, may be NULL): [0] the lowest eigenvalue,
+ * [1] the second-lowest Ritz value of the last Lanczos tridiagonal to about
+ * 1e-6 relative (an estimate of the spectral gap; NaN after one step).
+ * *iterations is a HOST pointer.  factors (device, may be NULL; 2 n^2 + n
+ * complex128) receives [C | L^-1 | u], u the unit Lanczos eigenvector of C
+ * (x = L^-H u / |..|): what a caller needs to solve correction equations
+ * against the same reduced pencil.  The call synchronizes the
  * stream at its convergence checkpoints.  Replaces
  * minimizeExpectationUsingFullEigensolver (system/_2d.py:498-502) and the
  * solve of minimizeExpectation (:489-497).
+ * flags: CARC_HEGV_TENSOR_CORE forms C = L^-1 H L^-H with the split-BF16
+ * tensor-core GEMM (about 1e-5 relative) instead of FP64 -- for pencils that
+ * are themselves tensor-core approximations (the mixed-precision solve).
  */
-int carc_zhegv_lowest(int32_t n, const void* H, const void* N, const void* x0, void* x, double* eigenvalue,
-                      int32_t max_krylov, int32_t max_restarts, double tol, int32_t* iterations,
-                      void* workspace, int64_t workspace_bytes, void* stream);
-int64_t carc_zhegv_lowest_workspace_size(int32_t n, int32_t max_krylov);
-/* The Lanczos part alone, for a dense Hermitian C. */
-int carc_zheev_lowest_lanczos(int32_t n, const void* C, const void* u0, void* u, double* eigenvalue,
+#define CARC_HEGV_TENSOR_CORE 1
+int carc_zhegv_lowest(int32_t n, const void* H, const void* N, const void* x0, void* x, double* eigenvalues,
+                      int32_t max_krylov, int32_t max_restarts, double tol, int32_t flags, int32_t* iterations,
+                      void* factors, void* workspace, int64_t workspace_bytes, void* stream);
+int64_t carc_zhegv_lowest_workspace_size(int32_t n, int32_t max_krylov, int32_t flags);
+/* The Lanczos part alone, for a dense Hermitian C (eigenvalues as above). */
+int carc_zheev_lowest_lanczos(int32_t n, const void* C, const void* u0, void* u, double* eigenvalues,
                               int32_t max_krylov, int32_t max_restarts, double tol, int32_t* iterations,
                               void* workspace, int64_t workspace_bytes, void* stream);
 int64_t carc_zheev_lowest_lanczos_workspace_size(int32_t n, int32_t max_krylov);
+/* MINRES for P (C - shift) P z = P b with P = I - u u^H (u unit, C dense
+ * Hermitian n x n): the correction equation of a Newton step against the
+ * reduced tensor-core pencil in the mixed-precision center solve (no
+ * counterpart in the reference, whose solves are FP64 throughout).  Stops at
+ * |residual| <= rtol |P b| or after maxit iterations; *iterations (HOST). */
+int carc_zminres_projected(int32_t n, const void* C, const void* u, double shift, const void* b, void* z,
+                           int32_t maxit, double rtol, int32_t* iterations, void* workspace, int64_t workspace_bytes,
+                           void* stream);
+int64_t carc_zminres_projected_workspace_size(int32_t n);
 
 /*
  * relaxOver (utils.py:805-878): restarted Krylov / Rayleigh-Ritz on

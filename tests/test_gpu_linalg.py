@@ -156,3 +156,25 @@ def test_product_compressor_exact_recovery(env):
         # same seed, same starting compressor as the reference: the projector agrees too
         Pr = g[f"pc_{case}_P"]
         assert rel(P.conj().T @ P, Pr.conj().T @ Pr) < 1e-6
+
+
+@pytest.mark.parametrize("n,shift", [(40, 0.3), (130, -1.7)])
+def test_minres_projected(n, shift):
+    """MINRES on P (C - shift) P z = P b (P = I - u u^H) against numpy: the
+    residual of the projected system and z's orthogonality to u."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from carcassonne_gb300 import linalg
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    C = (a + a.conj().T) / 2
+    u = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    u /= np.linalg.norm(u)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    z, its = linalg.minres_projected(torch.as_tensor(C).cuda(), torch.as_tensor(u).cuda(), shift,
+                                     torch.as_tensor(b).cuda(), maxit=4 * n, rtol=1e-10)
+    z = z.cpu().numpy()
+    P = np.eye(n) - np.outer(u, u.conj())
+    res = P @ (C - shift * np.eye(n)) @ P @ z - P @ b
+    assert np.linalg.norm(res) <= 1e-8 * np.linalg.norm(P @ b), (np.linalg.norm(res), its)
+    assert abs(np.vdot(u, z)) <= 1e-10 * np.linalg.norm(z)
