@@ -87,6 +87,13 @@ SIGNATURES = {
     "carc_zminres_projected": (ctypes.c_int, [_i32, _vp, _vp, _dbl, _vp, _vp, _i32, _dbl, ctypes.POINTER(_i32), _vp,
                                               _i64, _vp]),
     "carc_zminres_projected_workspace_size": (_i64, [_i32]),
+    "carc_mlp_linear_forward": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _i32, _vp, _vp]),
+    "carc_mlp_linear_backward": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "carc_mlp_mse": (ctypes.c_int, [_i64, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "carc_mlp_adam": (ctypes.c_int, [_i64, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_float, _i32, _vp]),
+    "carc_mlp_to_bf16": (ctypes.c_int, [_i64, _vp, _vp, _vp]),
+    "carc_mlp_linear_bf16": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _i32, _vp, _vp, _vp]),
     "carc_relax_over": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _i32, _i32, _dbl, ctypes.POINTER(_dbl),
                                        ctypes.POINTER(_i32), ctypes.POINTER(_dbl), _vp, _i64, _vp]),
     "carc_relax_over_workspace_size": (_i64, [_i32, _i32]),

@@ -8,6 +8,20 @@
 
 using namespace carc;
 
+namespace carc {
+// ---- learned start vector: MLP kernels (csrc/mlp.cu) ------------------------
+int mlp_linear_forward(int B, int K, int N, const float* X, const float* W, const float* b, int relu, float* Y,
+                       cudaStream_t stream);
+int mlp_linear_backward(int B, int K, int N, const float* X, const float* W, const float* Y, const float* dY,
+                        int relu, float* dZ, float* dX, float* dW, float* db, cudaStream_t stream);
+int mlp_mse(int64_t n, int B, const float* Y, const float* T, float* dY, float* loss, cudaStream_t stream);
+int mlp_adam(int64_t n, float* p, const float* g, float* m, float* v, float lr, float b1, float b2, float eps, int step,
+             cudaStream_t stream);
+int mlp_to_bf16(int64_t n, const float* x, void* y, cudaStream_t stream);
+int mlp_linear_bf16(int B, int K, int N, const void* X, const void* W, const float* b, int relu, void* Yb, float* Yf,
+                    cudaStream_t stream);
+}  // namespace carc
+
 extern "C" {
 
 const char* carc_last_error_string(void) { return last_error(); }
@@ -285,6 +299,42 @@ int64_t carc_stage3_form_matrix_tc_workspace_size(const int64_t* s0_shape, const
                                                   int32_t n_terms) {
   if (!s0_shape || !s1_shape) return -1;
   return stage3_form_matrix_tc_ws(s0_shape, s1_shape, d, n_terms);
+}
+
+
+int carc_mlp_linear_forward(int32_t B, int32_t K, int32_t N, const float* X, const float* W, const float* b,
+                            int32_t relu, float* Y, void* stream) {
+  if (!X || !W || !Y) return fail(CARC_BAD_ARG, "carc_mlp_linear_forward: NULL argument");
+  return mlp_linear_forward(B, K, N, X, W, b, relu, Y, as_stream(stream));
+}
+
+int carc_mlp_linear_backward(int32_t B, int32_t K, int32_t N, const float* X, const float* W, const float* Y,
+                             const float* dY, int32_t relu, float* dZ, float* dX, float* dW, float* db, void* stream) {
+  if (!X || !W || !Y || !dY || !dW || !db || (relu && !dZ))
+    return fail(CARC_BAD_ARG, "carc_mlp_linear_backward: NULL argument");
+  return mlp_linear_backward(B, K, N, X, W, Y, dY, relu, dZ, dX, dW, db, as_stream(stream));
+}
+
+int carc_mlp_mse(int64_t n, int32_t B, const float* Y, const float* T, float* dY, float* loss, void* stream) {
+  if (!Y || !T || !dY || !loss || B < 1) return fail(CARC_BAD_ARG, "carc_mlp_mse: bad argument");
+  return mlp_mse(n, B, Y, T, dY, loss, as_stream(stream));
+}
+
+int carc_mlp_adam(int64_t n, float* p, const float* g, float* m, float* v, float lr, float beta1, float beta2,
+                  float eps, int32_t step, void* stream) {
+  if (!p || !g || !m || !v) return fail(CARC_BAD_ARG, "carc_mlp_adam: NULL argument");
+  return mlp_adam(n, p, g, m, v, lr, beta1, beta2, eps, step, as_stream(stream));
+}
+
+int carc_mlp_to_bf16(int64_t n, const float* x, void* y, void* stream) {
+  if (!x || !y) return fail(CARC_BAD_ARG, "carc_mlp_to_bf16: NULL argument");
+  return mlp_to_bf16(n, x, y, as_stream(stream));
+}
+
+int carc_mlp_linear_bf16(int32_t B, int32_t K, int32_t N, const void* X, const void* W, const float* b, int32_t relu,
+                         void* Yb, float* Yf, void* stream) {
+  if (!X || !W || (!Yb && !Yf)) return fail(CARC_BAD_ARG, "carc_mlp_linear_bf16: bad argument");
+  return mlp_linear_bf16(B, K, N, X, W, b, relu, Yb, Yf, as_stream(stream));
 }
 
 }  // extern "C"

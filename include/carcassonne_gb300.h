@@ -332,6 +332,30 @@ int carc_relax_over(int32_t n, const void* H, const void* N, const void* x0, voi
                     void* workspace, int64_t workspace_bytes, void* stream);
 int64_t carc_relax_over_workspace_size(int32_t n, int32_t k);
 
+/*
+ * Learned start vector (no counterpart in the reference, whose start is the
+ * previous center, system/_2d.py:435-439 and :491-492): a fully connected
+ * network from boundary features to the center, trained and run by these
+ * kernels.  FP32 training, BF16 inference with FP32 accumulation.  Layouts:
+ * activations row-major (batch, features); weights (out, in) row-major; a
+ * layer computes Y = X W^T + b (ReLU when relu != 0).  All pointers device.
+ */
+int carc_mlp_linear_forward(int32_t B, int32_t K, int32_t N, const float* X, const float* W, const float* b,
+                            int32_t relu, float* Y, void* stream);
+/* dY (B, N): gradient w.r.t. the layer output Y; dZ (B, N) scratch when relu;
+ * outputs dX (B, K, may be NULL), dW (N, K), db (N). */
+int carc_mlp_linear_backward(int32_t B, int32_t K, int32_t N, const float* X, const float* W, const float* Y,
+                             const float* dY, int32_t relu, float* dZ, float* dX, float* dW, float* db, void* stream);
+/* loss (one float) = sum (Y - T)^2 / (2 B) over n = B * features; dY = (Y - T) / B */
+int carc_mlp_mse(int64_t n, int32_t B, const float* Y, const float* T, float* dY, float* loss, void* stream);
+/* Adam step (bias-corrected, step >= 1) on n parameters */
+int carc_mlp_adam(int64_t n, float* p, const float* g, float* m, float* v, float lr, float beta1, float beta2,
+                  float eps, int32_t step, void* stream);
+int carc_mlp_to_bf16(int64_t n, const float* x, void* y, void* stream);
+/* Y = X W^T + b with BF16 X, W; output BF16 (Yb) and/or FP32 (Yf) */
+int carc_mlp_linear_bf16(int32_t B, int32_t K, int32_t N, const void* X, const void* W, const float* b, int32_t relu,
+                         void* Yb, float* Yf, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
