@@ -149,7 +149,7 @@ def boundary_features(corners, sides, h, k=16):
         c0, c1 = a.shape[0], a.shape[1]
         m = a.reshape(c0 * c1, -1)
         _, S, _ = linalg.svd(TorchData(m))
-        s = S._t.float()
+        s = (S._t.real if S._t.is_complex() else S._t).float()
         v = torch.zeros(k, dtype=torch.float32, device=a.device)
         v[: min(k, s.numel())] = s[:k]
         feats.append(v)
