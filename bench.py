@@ -41,6 +41,10 @@ L2_FLUSH_BYTES = 512 << 20
 # D=4, chi=64 = 8x8, Hermitian-definite synthetic boundaries, seed 2)
 SOLVE = dict(workload="center-site solve, Heisenberg XXX d=2, D=4, chi=64 (8x8)", D=4, c=8, seed=2, reps=3)
 
+# batched uneven problems: transverse Ising, h ~ U[2,4], D ~ U{2..6},
+# chi ~ U{16,24,..,96}, a block of 8 vectors each, seed 3
+BATCHED = dict(workload="batched center-site matvecs, TI, D in 2..6, chi in 16..96, block 8", nvec=8, seed=3)
+
 # phases of the tensor-core operator, as numbered by carc_phase_timing_read
 PHASE_NAMES = ("pack", "step_a", "step_b", "reduce")
 KERNEL_OF_PHASE = dict(pack="pack_vin_kernel", step_a="gemm_bf16_tn_kernel<256,1> (folding epilogue)",
@@ -139,6 +143,9 @@ def parse_args():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-solve", dest="solve", action="store_false",
                    help="skip the mixed-vs-plain center-site solve comparison")
+    p.add_argument("--no-batched", dest="batched", action="store_false",
+                   help="skip the batched uneven-problems comparison (graph replay vs launch loop)")
+    p.add_argument("--batched-count", type=int, default=32)
     return p.parse_args()
 
 
@@ -438,6 +445,11 @@ def main():
                         whole_operator_frac_of_bf16=achieved_tflops / peaks["bf16_tflops"])
     cpu = cpu_reference(args, args.cpu_seconds) if world == 1 else None
     solve = solve_section() if args.solve else None
+    batched = None
+    if args.batched and world == 1:
+        from carcassonne_gb300 import batched as batched_mod
+        batched = dict(BATCHED, count=args.batched_count,
+                       **batched_mod.run(count=args.batched_count, nvec=BATCHED["nvec"], seed=BATCHED["seed"]))
     line = dict(
         metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
         ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None,
@@ -452,7 +464,7 @@ def main():
         e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=int(xh.numel() * 16),
                  d2h_bytes_per_step=int(yh.numel() * 16)),
         gpu_launches=int(launches_in_steps),
-        roofline=roofline, phases=phases, solve=solve,
+        roofline=roofline, phases=phases, solve=solve, batched=batched,
         cpu_baseline=None if cpu is None else dict(value=cpu["value"], unit=UNIT, cores=cpu["cores"],
                                                    kind=cpu["kind"], sample=cpu["sample"]),
         clocks=clocks, step_ms=dict(min=min(times), max=max(times)),

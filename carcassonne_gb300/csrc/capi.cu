@@ -278,6 +278,14 @@ int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int6
                           workspace, workspace_bytes, static_cast<int*>(status), as_stream(stream));
 }
 
+int carc_tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int32_t nvec, int32_t groups,
+                         int32_t ksplit) {
+  if (!s0_shape || !s1_shape) return fail(CARC_BAD_ARG, "carc_tc_autotune_set: NULL shape");
+  return tc_autotune_set(s0_shape, s1_shape, d, nvec, groups, ksplit);
+}
+
+int carc_tc_autotune_clear(void) { return tc_autotune_clear(); }
+
 int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
                                              const int32_t* terms, int32_t n_terms, int32_t nvec) {
   if (!s0_shape || !s1_shape || (n_terms > 0 && !terms)) return -1;

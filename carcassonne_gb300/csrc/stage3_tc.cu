@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 
 namespace carc {
@@ -167,6 +168,35 @@ __global__ void clear_w_padding_kernel(__nv_bfloat16* __restrict__ W, int64_t ro
 
 inline int grid_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * 152)); }
 
+// Autotune cache: the step-B split-K count per problem shape, written by the
+// host-side autotuner (carc_tc_autotune_set) after timing candidates; shapes
+// without an entry use the one-wave heuristic below.  The only mutable global
+// of the library, guarded by a mutex.
+struct TuneKey {
+  int64_t v[15];
+  bool operator<(const TuneKey& o) const { return std::lexicographical_compare(v, v + 15, o.v, o.v + 15); }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+
+TuneKey tune_key(const int64_t* s0, const int64_t* s1, int64_t d, int nvec, int groups) {
+  TuneKey k;
+  for (int i = 0; i < 6; ++i) {
+    k.v[i] = s0[i];
+    k.v[6 + i] = s1[i];
+  }
+  k.v[12] = d;
+  k.v[13] = nvec;
+  k.v[14] = groups;
+  return k;
+}
+
+int tuned_ksplit(const int64_t* s0, const int64_t* s1, int64_t d, int nvec, int groups) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(tune_key(s0, s1, d, nvec, groups));
+  return it == g_tune.end() ? 0 : it->second;
+}
+
 // split-K count that fills the 152 SMs (one CTA each) in a single wave
 int choose_ksplit(int64_t tiles, int64_t kp) {
   const int64_t kb = kp / 64;
@@ -186,6 +216,23 @@ int64_t plan_bytes_for(const Geo& g1, const TermGroups& tg) {
 }
 
 }  // namespace
+
+int tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int nvec, int groups, int ksplit) {
+  if (ksplit < 0 || nvec < 1 || groups < 1) return fail(CARC_BAD_ARG, "tc autotune: bad entry");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  const TuneKey k = tune_key(s0_shape, s1_shape, d, nvec, groups);
+  if (ksplit == 0)
+    g_tune.erase(k);
+  else
+    g_tune[k] = ksplit;
+  return CARC_OK;
+}
+
+int tc_autotune_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
+  return CARC_OK;
+}
 
 int64_t stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, const int32_t* terms, int n_terms) {
   S3 s;
@@ -232,11 +279,13 @@ struct MvWs {
   std::vector<int64_t> vin_off;  // byte offset of each group's Vin operand
 };
 
-int64_t mv_layout(const S3& s, int nvec, const TermGroups& tg, MvWs* w, void* base) {
+int64_t mv_layout(const S3& s, const int64_t* s0_shape, const int64_t* s1_shape, int nvec, const TermGroups& tg,
+                  MvWs* w, void* base) {
   const Geo g = geometry(s, nvec);
   const int64_t kpB = g.regB * (int64_t)tg.i1.size();
   const int64_t tilesB = (g.rowsB_a / 128) * (g.rowsB_b / bn_for(g.rowsB_b));
-  const int ksB = gemm_effective_ksplit((int)kpB, choose_ksplit(tilesB, kpB));
+  const int tuned = tuned_ksplit(s0_shape, s1_shape, s.d, nvec, (int)tg.i1.size());
+  const int ksB = gemm_effective_ksplit((int)kpB, tuned > 0 ? tuned : choose_ksplit(tilesB, kpB));
   std::vector<int64_t> vin_off;
   int64_t vin_bytes = 0;
   for (auto& v : tg.terms) {
@@ -325,7 +374,7 @@ int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, in
   S3 s;
   if (s3_shapes(s0_shape, s1_shape, d, &s) != CARC_OK) return -1;
   if (n_terms < 1 || nvec < 1) return 0;
-  return mv_layout(s, nvec, group_terms(terms, n_terms), nullptr, nullptr);
+  return mv_layout(s, s0_shape, s1_shape, nvec, group_terms(terms, n_terms), nullptr, nullptr);
 }
 
 int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int n0, int n1,
@@ -344,12 +393,12 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
       return fail(CARC_BAD_ARG, "stage3 tc matvec: term %d out of range", t);
   }
   const TermGroups tg = group_terms(terms, n_terms);
-  if (ws_bytes < mv_layout(s, nvec, tg, nullptr, nullptr))
+  if (ws_bytes < mv_layout(s, s0_shape, s1_shape, nvec, tg, nullptr, nullptr))
     return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
   const Geo g1 = geometry(s, 1);
   const Geo g = geometry(s, nvec);
   MvWs w;
-  mv_layout(s, nvec, tg, &w, ws);
+  mv_layout(s, s0_shape, s1_shape, nvec, tg, &w, ws);
   const int G = (int)tg.i1.size();
   const int64_t kpB = g.regB * G;
   // Vin of every term, operator applied and packed, in launches of up to 64 terms

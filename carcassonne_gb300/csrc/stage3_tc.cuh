@@ -7,6 +7,8 @@ int64_t stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, co
 int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const void* const* s0_ptrs, int n0,
                       const void* const* s1_ptrs, int n1, const int32_t* terms, int n_terms, void* plan,
                       int64_t plan_bytes, cudaStream_t stream);
+int tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int nvec, int groups, int ksplit);
+int tc_autotune_clear();
 int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const int32_t* terms,
                             int n_terms, int nvec);
 int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int n0, int n1,

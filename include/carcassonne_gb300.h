@@ -186,6 +186,13 @@ int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int6
                           int32_t n0, int32_t n1, const void* const* op_ptrs, int32_t nop,
                           const int32_t* terms, int32_t n_terms, const void* x, void* y, int32_t nvec,
                           int32_t accumulate, void* workspace, int64_t workspace_bytes, void* status, void* stream);
+/* Autotune cache of the tensor-core matvec (no counterpart in the reference):
+ * the step-B split-K count for one problem shape (S2 shapes, d, block size,
+ * number of S2_1 tags carrying terms); 0 removes the entry (the one-wave
+ * heuristic applies).  Query workspace sizes after setting an entry. */
+int carc_tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int32_t nvec, int32_t groups,
+                         int32_t ksplit);
+int carc_tc_autotune_clear(void);
 int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
                                              const int32_t* terms, int32_t n_terms, int32_t nvec);
 int carc_stage3_form_matrix_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
