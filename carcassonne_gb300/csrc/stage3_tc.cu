@@ -20,6 +20,7 @@
 #include "contract.cuh"
 #include "stage3.cuh"
 #include "stage3_tc.cuh"
+#include "umma.cuh"
 #include "umma_gemm.cuh"
 
 #include <cuda_bf16.h>
@@ -272,28 +273,37 @@ namespace {
 
 struct MvWs {
   char* vin;     // packed Vin operands of all groups (step-A B operands)
-  char* w_pk;    // packed W of all groups (step-B operand)
+  char* w_pk;    // packed W of all groups (step-B operand); unused when fused
   float* pB;     // step-B split planes
   char* red;     // reduction partial sums
   int ksB;
+  bool fused;    // step A and step B in one kernel, W on chip
   std::vector<int64_t> vin_off;  // byte offset of each group's Vin operand
 };
+
+bool fused_eligible(const S3& s, int nvec, const TermGroups& tg);
+int fused_grid(const S3& s, const TermGroups& tg);
 
 int64_t mv_layout(const S3& s, const int64_t* s0_shape, const int64_t* s1_shape, int nvec, const TermGroups& tg,
                   MvWs* w, void* base) {
   const Geo g = geometry(s, nvec);
   const int64_t kpB = g.regB * (int64_t)tg.i1.size();
   const int64_t tilesB = (g.rowsB_a / 128) * (g.rowsB_b / bn_for(g.rowsB_b));
+  // autotune entry: > 0 the unfused path with that step-B split, -1 (or none) the fused kernel where eligible
   const int tuned = tuned_ksplit(s0_shape, s1_shape, s.d, nvec, (int)tg.i1.size());
-  const int ksB = gemm_effective_ksplit((int)kpB, tuned > 0 ? tuned : choose_ksplit(tilesB, kpB));
+  const bool fused = tuned <= 0 && fused_eligible(s, nvec, tg);
+  const int ksB = fused ? fused_grid(s, tg)
+                        : gemm_effective_ksplit((int)kpB, tuned > 0 ? tuned : choose_ksplit(tilesB, kpB));
   std::vector<int64_t> vin_off;
   int64_t vin_bytes = 0;
   for (auto& v : tg.terms) {
     vin_off.push_back(vin_bytes);
     vin_bytes += a256(g.rowsA_b * g.regA * (int64_t)v.size() * 2);
   }
-  const int64_t sizes[4] = {vin_bytes, g.rowsB_b * kpB * 2, (int64_t)ksB * g.rowsB_a * g.rowsB_b * 4,
-                            reduce_partials2_workspace(s.l2 * s.l3, (int64_t)nvec * s.l0 * s.l1 * s.d, ksB)};
+  const int64_t nb = (int64_t)nvec * s.l0 * s.l1 * s.d;
+  const int64_t sizes[4] = {vin_bytes, fused ? 0 : g.rowsB_b * kpB * 2,
+                            fused ? (int64_t)ksB * 128 * nb * 4 : (int64_t)ksB * g.rowsB_a * g.rowsB_b * 4,
+                            reduce_partials2_workspace(s.l2 * s.l3, nb, ksB)};
   char* p = static_cast<char*>(base);
   int64_t off = 0;
   char* ptrs[4];
@@ -307,6 +317,7 @@ int64_t mv_layout(const S3& s, const int64_t* s0_shape, const int64_t* s1_shape,
     w->pB = reinterpret_cast<float*>(ptrs[2]);
     w->red = ptrs[3];
     w->ksB = ksB;
+    w->fused = fused;
     w->vin_off = vin_off;
   }
   return off;
@@ -369,6 +380,309 @@ __global__ void pack_vin_kernel(const double2* __restrict__ x, uint32_t* __restr
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Fused matvec: step A and step B in one persistent kernel, W kept on chip.
+//
+// A unit of work is (x-tile t, S2_1 tag g): 32 complex rows of step A (XP
+// x-pairs x all L = l0 l1 rows) against the group's Vin.  Per unit:
+//   MMA-A   TMEM_A[128 x NA] = packed S2_0 tile . Vin_g      (TMA-fed, 2 stages)
+//   fold    epilogue warps read TMEM_A, fold (hi+lo, re/im) and write the
+//           unit's W slice straight into shared memory as step B's K-major
+//           128B-swizzled operand B_B (rows (vec,l0,l1,p), 32 complex k)
+//   MMA-B   TMEM_B[128 x NB] += S2_1[g] K-slice (TMA) . B_B
+// TMEM_B accumulates over all units of the CTA and becomes one split-K plane;
+// the planes are summed by the FP64 two-level reduction.  Warp 0 issues the
+// step-A TMA loads, warp 10 the step-B slice loads, warp 1 the MMAs (one
+// thread each); warps 2..17 run the fold, four per TMEM lane quadrant.  Every wait is bounded; on expiry the CTA aborts, lets its
+// copies land, frees TMEM and flags the caller's status word.
+// Shapes: L divides 32, k2 k3 == l0 l1 (so a unit's K slice is 128 bf16
+// columns: two swizzle atoms), NA = nvec k2 k3 d and NB = nvec l0 l1 d
+// multiples of 16 up to 256, at most 8 S2_1 tags with terms.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int FU_THREADS = 608;  // warps: 0 A loads, 1 MMA, 2..17 fold, 18 B loads
+constexpr int FU_MAXG = 8;
+constexpr int FU_STAGE_A = 128 * 128;        // A tile: 128 rows x 64 bf16
+constexpr int FU_STAGE_V = 256 * 128;        // Vin tile: up to 256 rows x 64 bf16
+constexpr int FU_STAGE = FU_STAGE_A + FU_STAGE_V;
+constexpr int FU_BB_ATOM = 256 * 128;        // B_B atom: up to 256 rows x 128 B
+constexpr int FU_AB_ATOM = 128 * 128;        // A_B atom: 128 rows x 128 B
+constexpr int FU_SMEM = 1024 + 2 * FU_STAGE + 2 * FU_BB_ATOM + 2 * FU_AB_ATOM + 256 * 8 + 32 * 8 + 256;
+
+struct FusedMaps {
+  CUtensorMap a[FU_MAXG];    // packed S2_0 tags of group g: rows (x0,x1,l0,l1, re/im, hi/lo), K (terms, k0 k1)
+  CUtensorMap vin[FU_MAXG];  // packed Vin of group g: rows (vec,k2,k3,p)
+  CUtensorMap b;             // packed S2_1 tags: rows (l2,l3, re/im, hi/lo), K regions per group
+};
+
+struct FusedParams {
+  int n_units, x_tiles, G;
+  int nkb[FU_MAXG];
+  int NA, NB, a_rows;
+  int L, K23, d, XP;
+  int64_t regB, kcB;
+  float* planes;  // [grid][128][NB]
+  int* err;
+};
+
+__global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __grid_constant__ FusedMaps maps,
+                                                                     const __grid_constant__ FusedParams p) {
+  using namespace umma;
+  extern __shared__ uint8_t fsm_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fsm_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* stage = sm;                                   // 2 x (A tile, Vin tile)
+  uint8_t* bB = sm + 2 * FU_STAGE;                       // 2 atoms (hi, lo)
+  uint8_t* aB = bB + 2 * FU_BB_ATOM;                     // 2 atoms (hi, lo)
+  int2* tabN = reinterpret_cast<int2*>(aB + 2 * FU_AB_ATOM);
+  int2* tabM = tabN + 256;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tabM + 32);
+  uint64_t* full = bars;         // [2]
+  uint64_t* empty = bars + 2;    // [2]
+  uint64_t* accA_full = bars + 4;
+  uint64_t* bB_ready = bars + 5;
+  uint64_t* aB_full = bars + 6;
+  uint64_t* aB_empty = bars + 7;
+  uint64_t* doneB = bars + 8;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accA_full, 1);
+    mbar_init(bB_ready, 16);
+    mbar_init(aB_full, 1);
+    mbar_init(aB_empty, 1);
+    mbar_init(doneB, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (p.a_rows < 128) {
+    // rows [a_rows, 128) of both A_B atoms stay zero (the operand's padding rows)
+    for (int h = 0; h < 2; ++h) {
+      uint4* z = reinterpret_cast<uint4*>(aB + h * FU_AB_ATOM + p.a_rows * 128);
+      for (int i = threadIdx.x; i < (128 - p.a_rows) * 128 / 16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    fence_proxy_async();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tA = tmem, tB = tmem + 256;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- TMA producer
+      for (int g = 0; g < p.G; ++g) {
+        prefetch_tensormap(&maps.a[g]);
+        prefetch_tensormap(&maps.vin[g]);
+      }
+      prefetch_tensormap(&maps.b);
+      const uint32_t stage_bytes = (uint32_t)(FU_STAGE_A + p.NA * 128);
+      int kbg = 0, issued = 0;
+      bool ok = true;
+      for (int u = blockIdx.x; ok && u < p.n_units; u += gridDim.x) {
+        const int t = u / p.G, g = u % p.G;
+        for (int kb = 0; kb < p.nkb[g]; ++kb, ++kbg) {
+          const int s = kbg & 1;
+          const uint32_t ph = (uint32_t)((kbg >> 1) & 1);
+          if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
+          mbar_arrive_expect_tx(&full[s], stage_bytes);
+          tma_load_2d(stage + s * FU_STAGE, &maps.a[g], kb * 64, t * 128, &full[s]);
+          tma_load_2d(stage + s * FU_STAGE + FU_STAGE_A, &maps.vin[g], kb * 64, 0, &full[s]);
+          ++issued;
+        }
+      }
+      if (*abort_flag) {
+        // let copies already in flight land before the CTA exits (bounded)
+        for (int i = max(0, issued - 2); i < issued; ++i)
+          for (uint32_t q = 0; q < (1u << 20); ++q)
+            if (mbar_try_wait(&full[i & 1], (uint32_t)((i >> 1) & 1))) break;
+      }
+    }
+  } else if (warp == 18) {
+    if (lane == 0) {
+      // ---- TMA producer of step B's S2_1 slices (its own thread, so that the
+      // step-A loads run ahead independently of step B's progress)
+      int uc = 0, issued = 0;
+      for (int u = blockIdx.x; u < p.n_units; u += gridDim.x, ++uc) {
+        const int t = u / p.G, g = u % p.G;
+        if (!mbar_wait_sleep(aB_empty, (uint32_t)((uc & 1) ^ 1), abort_flag)) break;
+        mbar_arrive_expect_tx(aB_full, (uint32_t)(2 * p.a_rows * 128));
+        const int64_t kk0 = (int64_t)t * p.XP * p.K23;
+        tma_load_2d(aB, &maps.b, (int)(g * p.regB + 2 * kk0), 0, aB_full);
+        tma_load_2d(aB + FU_AB_ATOM, &maps.b, (int)(g * p.regB + 2 * p.kcB + 2 * kk0), 0, aB_full);
+        ++issued;
+      }
+      if (*abort_flag && issued > 0)
+        for (uint32_t q = 0; q < (1u << 20); ++q)
+          if (mbar_try_wait(aB_full, (uint32_t)((issued - 1) & 1))) break;
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // ---- MMA issuer
+      const uint32_t idA = idesc_bf16_f32(128, p.NA), idB = idesc_bf16_f32(128, p.NB);
+      int kbg = 0, uc = 0;
+      bool ok = true;
+      auto step_b = [&](int unit_count) -> bool {
+        // step B of unit (unit_count - 1): its B_B is written, its A_B slice loaded
+        const uint32_t ph = (uint32_t)((unit_count - 1) & 1);
+        if (!mbar_wait_sleep(bB_ready, ph, abort_flag)) return false;
+        if (!mbar_wait_sleep(aB_full, ph, abort_flag)) return false;
+        tc_fence_after();
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t a0 = smem_u32(aB + h * FU_AB_ATOM), b0 = smem_u32(bB + h * FU_BB_ATOM);
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+            mma_bf16(tB, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idB,
+                     (unit_count > 1 || h > 0 || kk > 0) ? 1u : 0u);
+        }
+        mma_commit(aB_empty);
+        return true;
+      };
+      for (int u = blockIdx.x; ok && u < p.n_units; u += gridDim.x, ++uc) {
+        const int g = u % p.G;
+        if (uc > 0 && !(ok = step_b(uc))) break;
+        for (int kb = 0; kb < p.nkb[g]; ++kb, ++kbg) {
+          const int s = kbg & 1;
+          const uint32_t ph = (uint32_t)((kbg >> 1) & 1);
+          if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(stage + s * FU_STAGE), b0 = smem_u32(stage + s * FU_STAGE + FU_STAGE_A);
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+            mma_bf16(tA, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idA,
+                     (kb > 0 || kk > 0) ? 1u : 0u);
+          mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(accA_full);
+      }
+      if (ok && uc > 0) ok = step_b(uc);
+      mma_commit(doneB);
+    }
+  } else if (warp >= 2 && warp <= 17) {
+    // ---- fold epilogue: warps 2..17; quadrant = warp % 4, column quarter = (warp - 2) / 4
+    const int quad = warp & 3, quarter = (warp - 2) >> 2;
+    const int et = threadIdx.x - 64;  // 0..511
+    // tables: per step-A column n = (vec, k23, p): {B_B row part, k part}; per tile row m = (xp, l)
+    for (int n = et; n < p.NA; n += 512) {
+      const int pp = n % p.d, q = n / p.d;
+      const int k23 = q % p.K23, vec = q / p.K23;
+      tabN[n] = make_int2(vec * p.L * p.d + pp, k23);
+    }
+    if (et < 32) tabM[et] = make_int2((et % p.L) * p.d, (et / p.L) * p.K23);
+    asm volatile("bar.sync 1, 512;" ::: "memory");
+    const int m = quad * 8 + (lane >> 2);  // complex row of this lane's quad within the tile
+    const int2 tm = tabM[m];
+    uint8_t* atom_hi = bB;
+    uint8_t* atom_lo = bB + FU_BB_ATOM;
+    // The B_B byte offsets this lane stores to are the same in every unit:
+    // compute them once (no shared-memory loads between the fold's stores).
+    const int qsel = lane & 3;
+    uint32_t offs[16];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int gi = 0; gi < 8; ++gi) {
+        const int col = quarter * 32 + 128 * i + 4 * gi + qsel;
+        uint32_t off = 0xffffffffu;
+        if (col < p.NA) {
+          const int2 tn = tabN[col];
+          const int row = tn.x + tm.x, kk = tn.y + tm.y;
+          off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + (((kk >> 2) ^ (row & 7)) << 4) + ((kk & 3) << 2));
+        }
+        offs[i * 8 + gi] = off;
+      }
+    int uc = 0;
+    bool ok = true;
+    for (int u = blockIdx.x; u < p.n_units; u += gridDim.x, ++uc) {
+      if (!(ok = mbar_wait_sleep(accA_full, (uint32_t)(uc & 1), abort_flag))) break;
+      tc_fence_after();
+      // this warp's 32-column chunks (columns 128 apart: the four quarters
+      // interleave), one TMEM load each; per group of 4 columns the quad sums
+      // its hi/lo rows (lane ^ 1), exchanges re/im (lane ^ 2), and each of its
+      // 4 lanes splits and stores one column at a precomputed offset
+      const uint32_t lanes = (uint32_t)(quad * 32) << 16;
+      const int nch = (p.NA - quarter * 32 + 127) / 128;
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        if (i >= nch) break;
+        uint32_t r[32];
+        tmem_ld_32x32b_x32(tA + lanes + (uint32_t)(quarter * 32 + 128 * i), r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j0 = 0; j0 < 32; j0 += 4) {
+          float v[4], o[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            v[q] = __uint_as_float(r[j0 + q]) + __shfl_xor_sync(0xffffffffu, __uint_as_float(r[j0 + q]), 1);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) o[q] = __shfl_xor_sync(0xffffffffu, v[q], 2);
+          const float vq = qsel == 0 ? v[0] : qsel == 1 ? v[1] : qsel == 2 ? v[2] : v[3];
+          const float oq = qsel == 0 ? o[0] : qsel == 1 ? o[1] : qsel == 2 ? o[2] : o[3];
+          const float re = (lane & 2) ? oq : vq, im = (lane & 2) ? vq : oq;
+          const __nv_bfloat162 h2 = __floats2bfloat162_rn(re, im);
+          const float2 hf = __bfloat1622float2(h2);
+          const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+          const uint32_t off = offs[i * 8 + j0 / 4];
+          if (off != 0xffffffffu) {
+            *reinterpret_cast<__nv_bfloat162*>(atom_hi + off) = h2;
+            *reinterpret_cast<__nv_bfloat162*>(atom_lo + off) = l2;
+          }
+        }
+      }
+      fence_proxy_async();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(bB_ready);
+    }
+    // ---- TMEM_B -> this CTA's split-K plane (zeros when the CTA had no unit)
+    const bool done = ok && mbar_wait_sleep(doneB, 0, abort_flag);
+    tc_fence_after();
+    if (done) {
+      float* plane = p.planes + (int64_t)blockIdx.x * 128 * p.NB;
+      const int row = quad * 32 + lane;
+      for (int c0 = quarter * 32; c0 < p.NB; c0 += 128) {
+        uint32_t r[32];
+        tmem_ld_32x32b_x32(tB + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (c0 + j < p.NB) plane[(int64_t)row * p.NB + c0 + j] = uc > 0 ? __uint_as_float(r[j]) : 0.f;
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(p.err, CARC_NOT_CONVERGED);
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+}
+
+int fused_grid(const S3& s, const TermGroups& tg) {
+  const int64_t units = (s.x0 * s.x1 * s.l0 * s.l1 / 32) * (int64_t)tg.i1.size();
+  return (int)std::max<int64_t>(1, std::min<int64_t>(152, units));
+}
+
+bool fused_eligible(const S3& s, int nvec, const TermGroups& tg) {
+  const int64_t L = s.l0 * s.l1, K23 = s.k2 * s.k3;
+  const int64_t NA = (int64_t)nvec * K23 * s.d, NB = (int64_t)nvec * L * s.d;
+  return L <= 32 && 32 % L == 0 && K23 == L && NA % 16 == 0 && NA <= 256 && NB % 16 == 0 && NB <= 256 &&
+         (int)tg.i1.size() <= FU_MAXG && 4 * s.l2 * s.l3 <= 128 && (s.x0 * s.x1 * L) % 32 == 0;
+}
+
+}  // namespace
+
 int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const int32_t* terms,
                             int n_terms, int nvec) {
   S3 s;
@@ -377,61 +691,13 @@ int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, in
   return mv_layout(s, s0_shape, s1_shape, nvec, group_terms(terms, n_terms), nullptr, nullptr);
 }
 
-int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int n0, int n1,
-                     const void* const* op_ptrs, int nop, const int32_t* terms, int n_terms, const void* x, void* y,
-                     int nvec, int accumulate, void* ws, int64_t ws_bytes, int* status, cudaStream_t stream) {
-  S3 s;
-  CARC_RETURN_IF(s3_shapes(s0_shape, s1_shape, d, &s));
-  const int64_t nl4 = s.l0 * s.l1 * s.l2 * s.l3, nk4 = s.k0 * s.k1 * s.k2 * s.k3;
-  if (n_terms == 0) {
-    if (!accumulate) return fill_launch((int64_t)nvec * nl4 * d, make_double2(0, 0), y, stream);
-    return CARC_OK;
-  }
-  for (int t = 0; t < n_terms; ++t) {
-    int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
-    if (i0 < 0 || i0 >= n0 || i1 < 0 || i1 >= n1 || io >= nop)
-      return fail(CARC_BAD_ARG, "stage3 tc matvec: term %d out of range", t);
-  }
-  const TermGroups tg = group_terms(terms, n_terms);
-  if (ws_bytes < mv_layout(s, s0_shape, s1_shape, nvec, tg, nullptr, nullptr))
-    return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
-  const Geo g1 = geometry(s, 1);
-  const Geo g = geometry(s, nvec);
-  MvWs w;
-  mv_layout(s, s0_shape, s1_shape, nvec, tg, &w, ws);
+namespace {
+
+// step A (one folding GEMM per S2_1 tag, W to HBM) and step B (one split-K GEMM)
+int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, const Geo& g, const void* plan,
+                  const MvWs& w, int* status, cudaStream_t stream) {
   const int G = (int)tg.i1.size();
   const int64_t kpB = g.regB * G;
-  // Vin of every term, operator applied and packed, in launches of up to 64 terms
-  {
-    PhaseScope ph(PH_TC_PACK, stream);
-    VinTerms vt;
-    memset(&vt, 0, sizeof(vt));
-    vt.rows_out = g.rowsA_b;
-    vt.rows_valid = g.NA;
-    vt.kc = s.k0 * s.k1;
-    vt.reg4 = g.regA / 4;
-    vt.k23 = s.k2 * s.k3;
-    vt.d = s.d;
-    auto flush = [&]() -> int {
-      if (vt.n == 0) return CARC_OK;
-      pack_vin_kernel<<<grid_of((int64_t)vt.n * vt.rows_out * vt.reg4), 256, 0, stream>>>(
-          static_cast<const double2*>(x), reinterpret_cast<uint32_t*>(w.vin), vt);
-      CARC_CHECK_LAUNCH();
-      vt.n = 0;
-      return CARC_OK;
-    };
-    for (int q = 0; q < G; ++q) {
-      const int nt = (int)tg.terms[q].size();
-      for (int j = 0; j < nt; ++j) {
-        const int io = terms[3 * tg.terms[q][j] + 2];
-        vt.op[vt.n] = io < 0 ? nullptr : static_cast<const double2*>(op_ptrs[io]);
-        vt.dst[vt.n] = w.vin_off[q] / 4 + (int64_t)j * g.regA / 2;
-        vt.pitch[vt.n] = g.regA * nt / 2;
-        if (++vt.n == kVinTermsPerLaunch) CARC_RETURN_IF(flush());
-      }
-    }
-    CARC_RETURN_IF(flush());
-  }
   const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
   const int64_t pad_w = rows_valid_w * G * (g.regB - 4 * g.kcB) + (g.rowsB_b - rows_valid_w) * kpB;
   if (pad_w > 0) {
@@ -467,11 +733,124 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   }
   // step B: y^T[(l2,l3),(vec,l0,l1,p)] = sum_g S2_1[i1_g] . W_g in one split-K GEMM
   const char* planB = planA;
-  const int64_t planeB = g.rowsB_a * g.rowsB_b;
   {
     PhaseScope ph(PH_TC_STEP_B, stream);
     CARC_RETURN_IF(gemm_bf16_tn(planB, (int)g1.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)kpB, w.pB, g.rowsB_b, w.ksB,
                                 status, stream, (int)(4 * s.l2 * s.l3)));
+  }
+  return CARC_OK;
+}
+
+int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, const Geo& g, const void* plan,
+                 const MvWs& w, int* status, cudaStream_t stream) {
+  const int G = (int)tg.i1.size();
+  FusedMaps maps;
+  memset(&maps, 0, sizeof(maps));
+  FusedParams fp;
+  memset(&fp, 0, sizeof(fp));
+  const char* planA = static_cast<const char*>(plan);
+  for (int q = 0; q < G; ++q) {
+    const int64_t kpA = g.regA * (int64_t)tg.terms[q].size();
+    CARC_RETURN_IF(tma_map_bf16(&maps.a[q], planA, (uint64_t)kpA, (uint64_t)g1.rowsA_a, 128));
+    CARC_RETURN_IF(tma_map_bf16(&maps.vin[q], w.vin + w.vin_off[q], (uint64_t)kpA, (uint64_t)g.rowsA_b,
+                                (uint32_t)g.NA));
+    fp.nkb[q] = (int)(kpA / 64);
+    planA += a256(g1.rowsA_a * kpA * 2);
+  }
+  const int live_b = (int)(4 * s.l2 * s.l3);
+  fp.a_rows = live_b <= 64 ? 64 : 128;
+  CARC_RETURN_IF(tma_map_bf16(&maps.b, planA, (uint64_t)(g.regB * G), (uint64_t)g1.rowsB_a, (uint32_t)fp.a_rows));
+  fp.L = (int)(s.l0 * s.l1);
+  fp.K23 = (int)(s.k2 * s.k3);
+  fp.d = (int)s.d;
+  fp.XP = 32 / fp.L;
+  fp.x_tiles = (int)(s.x0 * s.x1 * s.l0 * s.l1 / 32);
+  fp.G = G;
+  fp.n_units = fp.x_tiles * G;
+  fp.NA = (int)g.NA;
+  fp.NB = (int)(nvec * s.l0 * s.l1 * s.d);
+  fp.regB = g.regB;
+  fp.kcB = g.kcB;
+  fp.planes = w.pB;
+  fp.err = status;
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    attr = cudaFuncSetAttribute(stage3_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
+  });
+  if (attr != cudaSuccess) return fail(CARC_CUDA_ERROR, "fused matvec: %s", cudaGetErrorString(attr));
+  PhaseScope ph(PH_TC_STEP_A, stream);
+  stage3_fused_kernel<<<w.ksB, FU_THREADS, FU_SMEM, stream>>>(maps, fp);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+}  // namespace
+
+int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const void* plan, int n0, int n1,
+                     const void* const* op_ptrs, int nop, const int32_t* terms, int n_terms, const void* x, void* y,
+                     int nvec, int accumulate, void* ws, int64_t ws_bytes, int* status, cudaStream_t stream) {
+  S3 s;
+  CARC_RETURN_IF(s3_shapes(s0_shape, s1_shape, d, &s));
+  const int64_t nl4 = s.l0 * s.l1 * s.l2 * s.l3;
+  if (n_terms == 0) {
+    if (!accumulate) return fill_launch((int64_t)nvec * nl4 * d, make_double2(0, 0), y, stream);
+    return CARC_OK;
+  }
+  for (int t = 0; t < n_terms; ++t) {
+    int i0 = terms[3 * t], i1 = terms[3 * t + 1], io = terms[3 * t + 2];
+    if (i0 < 0 || i0 >= n0 || i1 < 0 || i1 >= n1 || io >= nop)
+      return fail(CARC_BAD_ARG, "stage3 tc matvec: term %d out of range", t);
+  }
+  const TermGroups tg = group_terms(terms, n_terms);
+  if (ws_bytes < mv_layout(s, s0_shape, s1_shape, nvec, tg, nullptr, nullptr))
+    return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
+  const Geo g1 = geometry(s, 1);
+  const Geo g = geometry(s, nvec);
+  MvWs w;
+  mv_layout(s, s0_shape, s1_shape, nvec, tg, &w, ws);
+  const int G = (int)tg.i1.size();
+  // Vin of every term, operator applied and packed, in launches of up to 64 terms
+  {
+    PhaseScope ph(PH_TC_PACK, stream);
+    VinTerms vt;
+    memset(&vt, 0, sizeof(vt));
+    vt.rows_out = g.rowsA_b;
+    vt.rows_valid = g.NA;
+    vt.kc = s.k0 * s.k1;
+    vt.reg4 = g.regA / 4;
+    vt.k23 = s.k2 * s.k3;
+    vt.d = s.d;
+    auto flush = [&]() -> int {
+      if (vt.n == 0) return CARC_OK;
+      pack_vin_kernel<<<grid_of((int64_t)vt.n * vt.rows_out * vt.reg4), 256, 0, stream>>>(
+          static_cast<const double2*>(x), reinterpret_cast<uint32_t*>(w.vin), vt);
+      CARC_CHECK_LAUNCH();
+      vt.n = 0;
+      return CARC_OK;
+    };
+    for (int q = 0; q < G; ++q) {
+      const int nt = (int)tg.terms[q].size();
+      for (int j = 0; j < nt; ++j) {
+        const int io = terms[3 * tg.terms[q][j] + 2];
+        vt.op[vt.n] = io < 0 ? nullptr : static_cast<const double2*>(op_ptrs[io]);
+        vt.dst[vt.n] = w.vin_off[q] / 4 + (int64_t)j * g.regA / 2;
+        vt.pitch[vt.n] = g.regA * nt / 2;
+        if (++vt.n == kVinTermsPerLaunch) CARC_RETURN_IF(flush());
+      }
+    }
+    CARC_RETURN_IF(flush());
+  }
+  const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
+  int64_t plane_ld, plane_stride;
+  if (w.fused) {
+    CARC_RETURN_IF(launch_fused(s, nvec, tg, g1, g, plan, w, status, stream));
+    plane_ld = rows_valid_w;
+    plane_stride = 128 * rows_valid_w;
+  } else {
+    CARC_RETURN_IF(unfused_steps(s, nvec, tg, g1, g, plan, w, status, stream));
+    plane_ld = g.rowsB_b;
+    plane_stride = g.rowsB_a * g.rowsB_b;
   }
   ZOut o;
   memset(&o, 0, sizeof(o));
@@ -486,7 +865,7 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   o.n_ext[2] = s.l1; o.n_str[2] = yl1;
   o.n_ext[3] = s.d; o.n_str[3] = 1;
   PhaseScope ph(PH_TC_REDUCE, stream);
-  return reduce_partials2(w.pB, g.rowsB_b, planeB, w.ksB, o, make_double2(1, 0), accumulate, w.red,
+  return reduce_partials2(w.pB, plane_ld, plane_stride, w.ksB, o, make_double2(1, 0), accumulate, w.red,
                           reduce_partials2_workspace(s.l2 * s.l3, rows_valid_w, w.ksB), stream);
 }
 

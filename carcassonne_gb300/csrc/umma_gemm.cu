@@ -395,6 +395,10 @@ int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const F
   return launch_any<1>(bn, ma, mb, M, N, BM, nullptr, N, 0, 1, kb_total, kb_total, err, fe, stream);
 }
 
+int tma_map_bf16(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_rows) {
+  return make_map(map, base, inner, rows, box_rows);
+}
+
 int gemm_effective_ksplit(int K, int ksplit) {
   const int kb_total = K / BK;
   ksplit = std::max(1, std::min(ksplit, kb_total));

@@ -1,6 +1,7 @@
 // Host-side interface of the split-BF16 tensor-core complex GEMM (umma_gemm.cu).
 #pragma once
 #include "common.cuh"
+#include <cuda.h>
 
 namespace carc {
 
@@ -45,6 +46,9 @@ int64_t round_up(int64_t a, int64_t b);
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
                  cudaStream_t stream, int m_live = 0);
 int gemm_effective_ksplit(int K, int ksplit);
+// 2D tensor map of a BF16 K-major matrix (inner = K columns, rows), box of
+// 64 columns x box_rows rows, 128-byte swizzle (the GEMM operand layout).
+int tma_map_bf16(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_rows);
 // The same GEMM (no K split) with the folding epilogue instead of FP32 planes.
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
                       cudaStream_t stream);

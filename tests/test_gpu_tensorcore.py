@@ -111,3 +111,32 @@ def test_stage3_tensorcore_matches_fp64(lib, D, c_ket, c_bra, nvec):
             opr.check_status()
             err = np.abs(Htc - H64).max() / np.abs(H64).max()
             assert err < 5e-5, err
+
+
+@pytest.mark.parametrize("D,c_ket,c_bra,nvec", [(2, 2, 2, 8), (4, 4, 4, 2), (4, 8, 4, 8)])
+def test_fused_matvec_matches_unfused_and_fp64(lib, D, c_ket, c_bra, nvec):
+    """The fused step-A/step-B kernel (W kept on chip) against the two-kernel
+    path (forced through the autotune cache) and the FP64 path."""
+    from carcassonne_gb300 import workloads
+    from carcassonne_gb300.tensors._2d import sparse as tsp
+    L = lib.load()
+    corners_a, sides_a, op_a = workloads.matvec_problem_arrays(D=D, c_ket=c_ket, c_bra=c_bra, seed=7)
+    corners, sides, op = workloads.to_device(corners_a, sides_a, op_a)
+    H, _ = tsp.formExpectationAndNormalizationMultipliers(corners, sides, op)
+    opr = H.operator
+    rng = np.random.default_rng(3)
+    shape = (nvec,) + opr.in_shape
+    x = torch.as_tensor(rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).cuda()
+    y64 = opr.apply(x, nvec=nvec).cpu().numpy()
+    y_fused = opr.apply_tc(x, nvec=nvec).cpu().numpy()
+    opr.check_status()
+    for g in opr._groups:  # force the two-kernel path for this shape
+        groups = len({t[1] for t in g["terms"]})
+        lib.check(L.carc_tc_autotune_set(g["s0"], g["s1"], opr.d, nvec, groups, 152))
+    y_two = opr.apply_tc(x, nvec=nvec).cpu().numpy()
+    opr.check_status()
+    lib.check(L.carc_tc_autotune_clear())
+    scale = np.abs(y64).max()
+    assert np.abs(y_fused - y64).max() / scale < 5e-5
+    assert np.abs(y_two - y64).max() / scale < 5e-5
+    assert np.abs(y_fused - y_two).max() / scale < 2e-5
