@@ -48,10 +48,15 @@ BATCHED = dict(workload="batched center-site matvecs, TI, D in 2..6, chi in 16..
 # phases of the tensor-core operator, as numbered by carc_phase_timing_read
 PHASE_NAMES = ("pack", "step_a", "step_b", "reduce")
 KERNEL_OF_PHASE = dict(pack="pack_vin_kernel", step_a="gemm_bf16_tn_kernel<256,1> (folding epilogue)",
-                       step_b="gemm_bf16_tn_kernel<256,0> (split-K)", reduce="reduce_slices/finish_kernel")
+                       step_b="gemm_bf16_tn_kernel<256,0> (split-K)", reduce="reduce_planes_kernel",
+                       fused="stage3_fused_kernel (step A + fold + step B, W on chip)")
 # DRAM bytes (read + write) per launch from one ncu capture of this workload
 # (profiles/ holds the summary and the command that produced it)
 NCU_TRAFFIC = {
+    ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "fused"): dict(
+        bytes_per_launch=131.5e6,
+        source="profiles/stage3_fused_matvec_D4_chi32_nvec8.md: one fused launch, dram read 126.5 MB + write "
+               "5.0 MB"),
     ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "step_a"): dict(
         bytes_per_launch=8.97e6,
         source="profiles/stage3_tc_matvec_D4_chi32_nvec8.md: one step-A launch (1-term group, 41.9 MB "
@@ -96,6 +101,13 @@ def tc_bytes_per_step(opr, nvec):
         live_rows = live_b if rows_sb == 128 and live_b <= 64 else rows_sb
         out["step_b"] += 2 * (live_rows * kp_b + rows_w * kp_b) + 4 * ks_b * rows_sb * rows_w
         out["launches"]["step_b"] += 1
+        # the fused kernel (W on chip): packed S2_0 and Vin of every term, the
+        # live rows of the packed S2_1 tags, one FP32 plane per CTA
+        units = (x0 * x1 * l0 * l1 // 32) * len(groups)
+        grid = max(1, min(152, units))
+        out["fused"] = out.get("fused", 0) + 2 * (rows_a * reg_a * nt + rows_vin * reg_a * nt + live_rows * kp_b) \
+            + 4 * grid * 128 * rows_w
+        out["launches"]["fused"] = out["launches"].get("fused", 0) + 1
     return out
 
 
@@ -425,6 +437,11 @@ def main():
                     note="whole operator: algorithmic (CostTracker) flops per step / step time")
     if phases:
         geo = tc_bytes_per_step(opr, nvec)
+        fused = phases["step_b"]["intervals_per_step"] == 0
+        if fused:
+            # the step-A interval brackets the fused kernel, which does both steps
+            phases["fused"] = phases.pop("step_a")
+            phases.pop("step_b")
         for pname, ph in phases.items():
             ph["share"] = ph["ms_per_step"] / ms
             if pname in geo:
@@ -434,15 +451,23 @@ def main():
         ph = phases[top]
         launches = geo["launches"][top]
         traffic = NCU_TRAFFIC.get((WORKLOAD["workload"], top))
-        roofline = dict(bound="hbm", kernel=KERNEL_OF_PHASE[top], achieved=ph["achieved_gbs"],
-                        peak=peaks["hbm_gbs"], unit="GB/s", frac=ph["achieved_gbs"] / peaks["hbm_gbs"],
-                        traffic=None if traffic is None else traffic["bytes_per_launch"],
-                        algorithmic_bytes_per_launch=geo[top] / launches,
-                        launch_ms=ph["ms_per_step"] / launches, launches_per_step=launches,
-                        peak_source=peaks["source"] + " HBM copy",
-                        traffic_source=None if traffic is None else traffic["source"],
-                        whole_operator_tflops=achieved_tflops,
-                        whole_operator_frac_of_bf16=achieved_tflops / peaks["bf16_tflops"])
+        common = dict(kernel=KERNEL_OF_PHASE[top], traffic=None if traffic is None else traffic["bytes_per_launch"],
+                      algorithmic_bytes_per_launch=geo[top] / launches, launch_ms=ph["ms_per_step"] / launches,
+                      launches_per_step=launches, traffic_source=None if traffic is None else traffic["source"],
+                      whole_operator_tflops=achieved_tflops,
+                      whole_operator_frac_of_bf16=achieved_tflops / peaks["bf16_tflops"])
+        if top == "fused":
+            # algorithmic flops per launch (CostTracker, the whole operator) over the kernel's time;
+            # the split-BF16 tensor work is 4x that, reported beside it
+            kt = flops_per_step / (ph["ms_per_step"] * 1e-3) / 1e12
+            roofline = dict(bound="tensor", achieved=kt, peak=peaks["bf16_tflops"], unit="TFLOP/s",
+                            frac=kt / peaks["bf16_tflops"], tensor_executed_tflops=4 * kt,
+                            hbm_achieved_gbs=ph["achieved_gbs"], hbm_frac=ph["achieved_gbs"] / peaks["hbm_gbs"],
+                            peak_source=peaks["source"] + " bf16 dense", **common)
+        else:
+            roofline = dict(bound="hbm", achieved=ph["achieved_gbs"], peak=peaks["hbm_gbs"], unit="GB/s",
+                            frac=ph["achieved_gbs"] / peaks["hbm_gbs"], peak_source=peaks["source"] + " HBM copy",
+                            **common)
     cpu = cpu_reference(args, args.cpu_seconds) if world == 1 else None
     solve = solve_section() if args.solve else None
     batched = None

@@ -582,8 +582,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     asm volatile("bar.sync 1, 512;" ::: "memory");
     const int m = quad * 8 + (lane >> 2);  // complex row of this lane's quad within the tile
     const int2 tm = tabM[m];
-    uint8_t* atom_hi = bB;
-    uint8_t* atom_lo = bB + FU_BB_ATOM;
+    const uint32_t sh_hi = smem_u32(bB), sh_lo = smem_u32(bB + FU_BB_ATOM);
     // The B_B byte offsets this lane stores to are the same in every unit:
     // compute them once (no shared-memory loads between the fold's stores).
     const int qsel = lane & 3;
@@ -634,8 +633,11 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
           const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
           const uint32_t off = offs[i * 8 + j0 / 4];
           if (off != 0xffffffffu) {
-            *reinterpret_cast<__nv_bfloat162*>(atom_hi + off) = h2;
-            *reinterpret_cast<__nv_bfloat162*>(atom_lo + off) = l2;
+            // explicit shared-space stores (the aligned base pointer is generic)
+            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_hi + off), "r"(*reinterpret_cast<const uint32_t*>(&h2))
+                         : "memory");
+            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_lo + off), "r"(*reinterpret_cast<const uint32_t*>(&l2))
+                         : "memory");
           }
         }
       }

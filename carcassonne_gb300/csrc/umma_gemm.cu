@@ -527,33 +527,32 @@ __global__ void reduce_kernel(const float* __restrict__ P, double2* __restrict__
   }
 }
 
-// partial[s][m][n] = sum over planes z = s, s+S, ... of the folded complex value
-__global__ void reduce_slices_kernel(const float* __restrict__ P, double2* __restrict__ part,
-                                     const __grid_constant__ ReduceParams p, int S) {
-  const int64_t total = (int64_t)S * p.Mc * p.Nc;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t n = t % p.Nc;
-    const int64_t rest = t / p.Nc;
-    const int64_t m = rest % p.Mc;
-    const int s = (int)(rest / p.Mc);
-    double re = 0.0, im = 0.0;
-    for (int z = s; z < p.ksplit; z += S) {
+// C[m,n] (+)= alpha * sum_z (P[z][4m..4m+1][n] + i P[z][4m+2..4m+3][n]), in
+// FP64 and in a fixed order: a block covers one complex row m and 32
+// consecutive n (lanes: coalesced 128-byte rows), its 8 warps take the planes
+// z = w, w+8, ... and the 8 partial sums are added in warp order.
+constexpr int RP_WARPS = 8;
+__global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const float* __restrict__ P,
+                                                                       double2* __restrict__ C,
+                                                                       const __grid_constant__ ReduceParams p) {
+  __shared__ double2 part[RP_WARPS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t m = blockIdx.y;
+  const int64_t n = (int64_t)blockIdx.x * 32 + lane;
+  double re = 0.0, im = 0.0;
+  if (n < p.Nc) {
+    for (int z = w; z < p.ksplit; z += RP_WARPS) {
       const float* b = P + z * p.split_stride + (4 * m) * p.ld + n;
       re += (double)b[0] + (double)b[p.ld];
       im += (double)b[2 * p.ld] + (double)b[3 * p.ld];
     }
-    part[t] = make_double2(re, im);
   }
-}
-
-__global__ void reduce_finish_kernel(const double2* __restrict__ part, double2* __restrict__ C,
-                                     const __grid_constant__ ReduceParams p, int S) {
-  const int64_t total = p.Mc * p.Nc;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    double2 v = make_double2(0.0, 0.0);
-    for (int s = 0; s < S; ++s) v = cadd(v, part[(int64_t)s * total + t]);
+  part[w][lane] = make_double2(re, im);
+  __syncthreads();
+  if (w == 0 && n < p.Nc) {
+    double2 v = part[0][lane];
+    for (int q = 1; q < RP_WARPS; ++q) v = cadd(v, part[q][lane]);
     v = cmul(p.alpha, v);
-    const int64_t m = t / p.Nc, n = t % p.Nc;
     const int64_t off = pdecomp(m, p.nm, p.m_ext, p.m_str) + pdecomp(n, p.nn, p.n_ext, p.n_str);
     if (p.accumulate) v = cadd(v, C[off]);
     C[off] = v;
@@ -658,10 +657,12 @@ int reduce_partials(const float* P, int64_t ld, int64_t split_stride, int ksplit
   return CARC_OK;
 }
 
-static int reduce_slices_for(int ksplit) { return std::max(1, std::min(ksplit, 32)); }
 
 int64_t reduce_partials2_workspace(int64_t Mc, int64_t Nc, int ksplit) {
-  return (int64_t)reduce_slices_for(ksplit) * Mc * Nc * 16 + 256;
+  (void)Mc;
+  (void)Nc;
+  (void)ksplit;
+  return 256;
 }
 
 int reduce_partials2(const float* P, int64_t ld, int64_t split_stride, int ksplit, const ZOut& o, double2 alpha,
@@ -687,12 +688,11 @@ int reduce_partials2(const float* P, int64_t ld, int64_t split_stride, int kspli
   p.ksplit = ksplit;
   p.accumulate = accumulate;
   p.alpha = alpha;
-  const int S = reduce_slices_for(ksplit);
-  if (ws_bytes < reduce_partials2_workspace(p.Mc, p.Nc, ksplit)) return fail(CARC_BAD_ARG, "reduce: workspace too small");
-  double2* part = static_cast<double2*>(ws);
-  reduce_slices_kernel<<<grid_of((int64_t)S * p.Mc * p.Nc), 256, 0, stream>>>(P, part, p, S);
-  CARC_CHECK_LAUNCH();
-  reduce_finish_kernel<<<grid_of(p.Mc * p.Nc), 256, 0, stream>>>(part, static_cast<double2*>(o.base), p, S);
+  (void)ws;
+  (void)ws_bytes;
+  if (p.Mc > 65535) return fail(CARC_TOO_LARGE, "reduce: %lld output rows", (long long)p.Mc);
+  dim3 grid((unsigned)((p.Nc + 31) / 32), (unsigned)p.Mc);
+  reduce_planes_kernel<<<grid, 32 * RP_WARPS, 0, stream>>>(P, static_cast<double2*>(o.base), p);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }

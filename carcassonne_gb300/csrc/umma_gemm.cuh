@@ -52,8 +52,9 @@ int tma_map_bf16(CUtensorMap* map, const void* base, uint64_t inner, uint64_t ro
 // The same GEMM (no K split) with the folding epilogue instead of FP32 planes.
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
                       cudaStream_t stream);
-// Two-level deterministic reduction of split-K planes into a complex output
-// (coalesced over columns; the plane sum is spread over `slices` partial sums).
+// Deterministic FP64 reduction of split-K planes into a complex output in one
+// launch (coalesced over columns, planes spread over 8 warps per block); the
+// workspace arguments are kept for the callers' layouts and need 256 bytes.
 int64_t reduce_partials2_workspace(int64_t Mc, int64_t Nc, int ksplit);
 int reduce_partials2(const float* P, int64_t ld, int64_t split_stride, int ksplit, const ZOut& o, double2 alpha,
                      int accumulate, void* ws, int64_t ws_bytes, cudaStream_t stream);
