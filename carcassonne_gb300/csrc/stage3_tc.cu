@@ -302,7 +302,8 @@ int64_t mv_layout(const S3& s, const int64_t* s0_shape, const int64_t* s1_shape,
   }
   const int64_t nb = (int64_t)nvec * s.l0 * s.l1 * s.d;
   const int64_t sizes[4] = {vin_bytes, fused ? 0 : g.rowsB_b * kpB * 2,
-                            fused ? (int64_t)ksB * 128 * nb * 4 : (int64_t)ksB * g.rowsB_a * g.rowsB_b * 4,
+                            fused ? (int64_t)ksB * round_up(4 * s.l2 * s.l3, 32) * nb * 4
+                                  : (int64_t)ksB * g.rowsB_a * g.rowsB_b * 4,
                             reduce_partials2_workspace(s.l2 * s.l3, nb, ksB)};
   char* p = static_cast<char*>(base);
   int64_t off = 0;
@@ -403,58 +404,74 @@ namespace {
 
 constexpr int FU_THREADS = 608;  // warps: 0 A loads, 1 MMA, 2..17 fold, 18 B loads
 constexpr int FU_MAXG = 8;
+constexpr int FU_STAGES = 3;
 constexpr int FU_STAGE_A = 128 * 128;        // A tile: 128 rows x 64 bf16
 constexpr int FU_STAGE_V = 256 * 128;        // Vin tile: up to 256 rows x 64 bf16
 constexpr int FU_STAGE = FU_STAGE_A + FU_STAGE_V;
 constexpr int FU_BB_ATOM = 256 * 128;        // B_B atom: up to 256 rows x 128 B
 constexpr int FU_AB_ATOM = 128 * 128;        // A_B atom: 128 rows x 128 B
-constexpr int FU_SMEM = 1024 + 2 * FU_STAGE + 2 * FU_BB_ATOM + 2 * FU_AB_ATOM + 256 * 8 + 32 * 8 + 256;
+constexpr int FU_SMEM_BIG = 1024 + 2 * FU_STAGE + 2 * FU_BB_ATOM + 2 * FU_AB_ATOM + 256 * 8 + 32 * 8 + 512;
 
 struct FusedMaps {
   CUtensorMap a[FU_MAXG];    // packed S2_0 tags of group g: rows (x0,x1,l0,l1, re/im, hi/lo), K (terms, k0 k1)
-  CUtensorMap vin[FU_MAXG];  // packed Vin of group g: rows (vec,k2,k3,p)
+  CUtensorMap vin[FU_MAXG];  // packed Vin of group g: rows (vec,k2,k3,p), box NA / VH rows
   CUtensorMap b;             // packed S2_1 tags: rows (l2,l3, re/im, hi/lo), K regions per group
 };
 
 struct FusedParams {
-  int n_units, x_tiles, G;
+  int n_pairs, x_tiles, G;
   int nkb[FU_MAXG];
   int NA, NB, a_rows;
+  int VH;                 // vector parts per (x-tile, tag) pair: units are (pair, part)
+  int NAh, NBh;           // step-A / step-B columns of one part
+  int nbuf;               // TMEM_A buffers (2 when 2 NAh <= 256)
+  int stages;             // step-A pipeline depth
+  int stage_bytes;        // bytes of one stage (A tile + Vin part)
   int L, K23, d, XP;
   int64_t regB, kcB;
-  float* planes;  // [grid][128][NB]
+  int live_rows;  // rows of TMEM_B that carry data (4 l2 l3, rounded to 32)
+  float* planes;  // [grid][NB][live_rows], column-major per CTA
   int* err;
 };
 
+// Unit uc of a CTA (local counter) is part (uc % VH) of its pair (uc / VH);
+// the CTA takes pairs blockIdx.x, blockIdx.x + gridDim.x, ... so that both
+// parts of a pair run back to back (they share the pair's S2_1 slice).
 __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __grid_constant__ FusedMaps maps,
                                                                      const __grid_constant__ FusedParams p) {
   using namespace umma;
   extern __shared__ uint8_t fsm_raw[];
   uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(fsm_raw) + 1023) & ~uintptr_t(1023));
-  uint8_t* stage = sm;                                   // 2 x (A tile, Vin tile)
-  uint8_t* bB = sm + 2 * FU_STAGE;                       // 2 atoms (hi, lo)
+  uint8_t* stage = sm;                                   // stages x (A tile, Vin part)
+  uint8_t* bB = sm + p.stages * p.stage_bytes;           // 2 atoms (hi, lo), rows of part h at h NBh
   uint8_t* aB = bB + 2 * FU_BB_ATOM;                     // 2 atoms (hi, lo)
   int2* tabN = reinterpret_cast<int2*>(aB + 2 * FU_AB_ATOM);
   int2* tabM = tabN + 256;
   uint64_t* bars = reinterpret_cast<uint64_t*>(tabM + 32);
-  uint64_t* full = bars;         // [2]
-  uint64_t* empty = bars + 2;    // [2]
-  uint64_t* accA_full = bars + 4;
-  uint64_t* bB_ready = bars + 5;
-  uint64_t* aB_full = bars + 6;
-  uint64_t* aB_empty = bars + 7;
-  uint64_t* doneB = bars + 8;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 9);
+  uint64_t* full = bars;             // [FU_STAGES]
+  uint64_t* empty = bars + 4;        // [FU_STAGES]
+  uint64_t* accA_full = bars + 8;    // [2] per TMEM_A buffer
+  uint64_t* bB_ready = bars + 10;    // [2] per TMEM_A buffer: fold done (buffer free, B_B part written)
+  uint64_t* bB_free = bars + 12;     // [2] per part: MMA-B of the part done (its B_B rows free)
+  uint64_t* aB_full = bars + 14;
+  uint64_t* aB_empty = bars + 15;
+  uint64_t* doneB = bars + 16;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 17);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int my_pairs = blockIdx.x < p.n_pairs ? (p.n_pairs - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int n_units = my_pairs * p.VH;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < 2; ++s) {
+    for (int s = 0; s < FU_STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(accA_full, 1);
-    mbar_init(bB_ready, 16);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accA_full[b], 1);
+      mbar_init(&bB_ready[b], 16);
+      mbar_init(&bB_free[b], 1);
+    }
     mbar_init(aB_full, 1);
     mbar_init(aB_empty, 1);
     mbar_init(doneB, 1);
@@ -474,46 +491,46 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tA = tmem, tB = tmem + 256;
+  const uint32_t tB = tmem + 256;
 
   if (warp == 0) {
     if (lane == 0) {
-      // ---- TMA producer
+      // ---- TMA producer of step A: the unit's S2_0 tile and its Vin part
       for (int g = 0; g < p.G; ++g) {
         prefetch_tensormap(&maps.a[g]);
         prefetch_tensormap(&maps.vin[g]);
       }
       prefetch_tensormap(&maps.b);
-      const uint32_t stage_bytes = (uint32_t)(FU_STAGE_A + p.NA * 128);
       int kbg = 0, issued = 0;
       bool ok = true;
-      for (int u = blockIdx.x; ok && u < p.n_units; u += gridDim.x) {
-        const int t = u / p.G, g = u % p.G;
+      for (int uc = 0; ok && uc < n_units; ++uc) {
+        const int pr = (int)blockIdx.x + (uc / p.VH) * (int)gridDim.x, part = uc % p.VH;
+        const int t = pr / p.G, g = pr % p.G;
         for (int kb = 0; kb < p.nkb[g]; ++kb, ++kbg) {
-          const int s = kbg & 1;
-          const uint32_t ph = (uint32_t)((kbg >> 1) & 1);
+          const int s = kbg % p.stages;
+          const uint32_t ph = (uint32_t)((kbg / p.stages) & 1);
           if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
-          mbar_arrive_expect_tx(&full[s], stage_bytes);
-          tma_load_2d(stage + s * FU_STAGE, &maps.a[g], kb * 64, t * 128, &full[s]);
-          tma_load_2d(stage + s * FU_STAGE + FU_STAGE_A, &maps.vin[g], kb * 64, 0, &full[s]);
+          mbar_arrive_expect_tx(&full[s], (uint32_t)(FU_STAGE_A + p.NAh * 128));
+          tma_load_2d(stage + s * p.stage_bytes, &maps.a[g], kb * 64, t * 128, &full[s]);
+          tma_load_2d(stage + s * p.stage_bytes + FU_STAGE_A, &maps.vin[g], kb * 64, part * p.NAh, &full[s]);
           ++issued;
         }
       }
       if (*abort_flag) {
         // let copies already in flight land before the CTA exits (bounded)
-        for (int i = max(0, issued - 2); i < issued; ++i)
+        for (int i = max(0, issued - p.stages); i < issued; ++i)
           for (uint32_t q = 0; q < (1u << 20); ++q)
-            if (mbar_try_wait(&full[i & 1], (uint32_t)((i >> 1) & 1))) break;
+            if (mbar_try_wait(&full[i % p.stages], (uint32_t)((i / p.stages) & 1))) break;
       }
     }
   } else if (warp == 18) {
     if (lane == 0) {
-      // ---- TMA producer of step B's S2_1 slices (its own thread, so that the
-      // step-A loads run ahead independently of step B's progress)
-      int uc = 0, issued = 0;
-      for (int u = blockIdx.x; u < p.n_units; u += gridDim.x, ++uc) {
-        const int t = u / p.G, g = u % p.G;
-        if (!mbar_wait_sleep(aB_empty, (uint32_t)((uc & 1) ^ 1), abort_flag)) break;
+      // ---- TMA producer of step B's S2_1 slice, one per pair
+      int issued = 0;
+      for (int pc = 0; pc < my_pairs; ++pc) {
+        const int pr = (int)blockIdx.x + pc * (int)gridDim.x;
+        const int t = pr / p.G, g = pr % p.G;
+        if (!mbar_wait_sleep(aB_empty, (uint32_t)((pc & 1) ^ 1), abort_flag)) break;
         mbar_arrive_expect_tx(aB_full, (uint32_t)(2 * p.a_rows * 128));
         const int64_t kk0 = (int64_t)t * p.XP * p.K23;
         tma_load_2d(aB, &maps.b, (int)(g * p.regB + 2 * kk0), 0, aB_full);
@@ -526,36 +543,45 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      // ---- MMA issuer
-      const uint32_t idA = idesc_bf16_f32(128, p.NA), idB = idesc_bf16_f32(128, p.NB);
-      int kbg = 0, uc = 0;
+      // ---- MMA issuer.  Iteration uc issues MMA-A(uc) into TMEM_A buffer
+      // uc % nbuf, then MMA-B(uc - 1) once its fold is done: the tensor pipe
+      // works on unit uc while the epilogue warps fold unit uc - 1.
+      const uint32_t idA = idesc_bf16_f32(128, p.NAh), idB = idesc_bf16_f32(128, p.NBh);
+      int kbg = 0;
       bool ok = true;
-      auto step_b = [&](int unit_count) -> bool {
-        // step B of unit (unit_count - 1): its B_B is written, its A_B slice loaded
-        const uint32_t ph = (uint32_t)((unit_count - 1) & 1);
-        if (!mbar_wait_sleep(bB_ready, ph, abort_flag)) return false;
-        if (!mbar_wait_sleep(aB_full, ph, abort_flag)) return false;
+      auto step_b = [&](int u) -> bool {
+        // MMA-B of unit u: its fold wrote B_B part (u % VH); the pair's S2_1 slice is loaded
+        const int b = u % p.nbuf, part = u % p.VH, pc = u / p.VH;
+        if (!mbar_wait_sleep(&bB_ready[b], (uint32_t)((u / p.nbuf) & 1), abort_flag)) return false;
+        if (part == 0 && !mbar_wait_sleep(aB_full, (uint32_t)(pc & 1), abort_flag)) return false;
         tc_fence_after();
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const uint32_t a0 = smem_u32(aB + h * FU_AB_ATOM), b0 = smem_u32(bB + h * FU_BB_ATOM);
+          const uint32_t a0 = smem_u32(aB + h * FU_AB_ATOM);
+          const uint32_t b0 = smem_u32(bB + h * FU_BB_ATOM + part * p.NBh * 128);
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(tB, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idB,
-                     (unit_count > 1 || h > 0 || kk > 0) ? 1u : 0u);
+            mma_bf16(tB + (uint32_t)(part * p.NBh), smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idB,
+                     (pc > 0 || h > 0 || kk > 0) ? 1u : 0u);
         }
-        mma_commit(aB_empty);
+        mma_commit(&bB_free[part]);
+        if (part == p.VH - 1) mma_commit(aB_empty);
         return true;
       };
-      for (int u = blockIdx.x; ok && u < p.n_units; u += gridDim.x, ++uc) {
-        const int g = u % p.G;
-        if (uc > 0 && !(ok = step_b(uc))) break;
+      for (int uc = 0; ok && uc < n_units; ++uc) {
+        const int pr = (int)blockIdx.x + (uc / p.VH) * (int)gridDim.x;
+        const int g = pr % p.G, b = uc % p.nbuf;
+        // TMEM_A buffer b was last read by the fold of unit uc - nbuf
+        if (uc >= p.nbuf &&
+            !(ok = mbar_wait_sleep(&bB_ready[b], (uint32_t)(((uc - p.nbuf) / p.nbuf) & 1), abort_flag)))
+          break;
+        const uint32_t tA = tmem + (uint32_t)(b * p.NAh);
         for (int kb = 0; kb < p.nkb[g]; ++kb, ++kbg) {
-          const int s = kbg & 1;
-          const uint32_t ph = (uint32_t)((kbg >> 1) & 1);
+          const int s = kbg % p.stages;
+          const uint32_t ph = (uint32_t)((kbg / p.stages) & 1);
           if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
           tc_fence_after();
-          const uint32_t a0 = smem_u32(stage + s * FU_STAGE), b0 = smem_u32(stage + s * FU_STAGE + FU_STAGE_A);
+          const uint32_t a0 = smem_u32(stage + s * p.stage_bytes), b0 = smem_u32(stage + s * p.stage_bytes + FU_STAGE_A);
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk)
             mma_bf16(tA, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idA,
@@ -563,17 +589,19 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
           mma_commit(&empty[s]);
         }
         if (!ok) break;
-        mma_commit(accA_full);
+        mma_commit(&accA_full[b]);
+        if (uc > 0 && !(ok = step_b(uc - 1))) break;
       }
-      if (ok && uc > 0) ok = step_b(uc);
+      if (ok && n_units > 0) ok = step_b(n_units - 1);
       mma_commit(doneB);
     }
   } else if (warp >= 2 && warp <= 17) {
     // ---- fold epilogue: warps 2..17; quadrant = warp % 4, column quarter = (warp - 2) / 4
     const int quad = warp & 3, quarter = (warp - 2) >> 2;
     const int et = threadIdx.x - 64;  // 0..511
-    // tables: per step-A column n = (vec, k23, p): {B_B row part, k part}; per tile row m = (xp, l)
-    for (int n = et; n < p.NA; n += 512) {
+    // tables over the columns of part 0 (part h shifts the B_B rows by h NBh):
+    // per step-A column n = (vec, k23, p): {B_B row part, k part}; per tile row m = (xp, l)
+    for (int n = et; n < p.NAh; n += 512) {
       const int pp = n % p.d, q = n / p.d;
       const int k23 = q % p.K23, vec = q / p.K23;
       tabN[n] = make_int2(vec * p.L * p.d + pp, k23);
@@ -583,17 +611,18 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     const int m = quad * 8 + (lane >> 2);  // complex row of this lane's quad within the tile
     const int2 tm = tabM[m];
     const uint32_t sh_hi = smem_u32(bB), sh_lo = smem_u32(bB + FU_BB_ATOM);
-    // The B_B byte offsets this lane stores to are the same in every unit:
-    // compute them once (no shared-memory loads between the fold's stores).
+    // This lane's B_B byte offsets are the same in every unit (plus the part's
+    // row shift): computed once, so no shared-memory load sits between stores.
     const int qsel = lane & 3;
+    const int nch = (p.NAh / 32 - quarter + 3) / 4;  // chunks quarter, quarter + 4, ...
     uint32_t offs[16];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
       for (int gi = 0; gi < 8; ++gi) {
-        const int col = quarter * 32 + 128 * i + 4 * gi + qsel;
+        const int col = (quarter + 4 * i) * 32 + 4 * gi + qsel;
         uint32_t off = 0xffffffffu;
-        if (col < p.NA) {
+        if (i < nch && col < p.NAh) {
           const int2 tn = tabN[col];
           const int row = tn.x + tm.x, kk = tn.y + tm.y;
           off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + (((kk >> 2) ^ (row & 7)) << 4) + ((kk & 3) << 2));
@@ -602,21 +631,24 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       }
     int uc = 0;
     bool ok = true;
-    for (int u = blockIdx.x; u < p.n_units; u += gridDim.x, ++uc) {
-      if (!(ok = mbar_wait_sleep(accA_full, (uint32_t)(uc & 1), abort_flag))) break;
+    for (; uc < n_units; ++uc) {
+      const int b = uc % p.nbuf, part = uc % p.VH;
+      if (!(ok = mbar_wait_sleep(&accA_full[b], (uint32_t)((uc / p.nbuf) & 1), abort_flag))) break;
+      // B_B part `part` was last read by the MMA-B of unit uc - VH
+      if (uc >= p.VH && !(ok = mbar_wait_sleep(&bB_free[part], (uint32_t)(((uc - p.VH) / p.VH) & 1), abort_flag)))
+        break;
       tc_fence_after();
-      // this warp's 32-column chunks (columns 128 apart: the four quarters
-      // interleave), one TMEM load each; per group of 4 columns the quad sums
-      // its hi/lo rows (lane ^ 1), exchanges re/im (lane ^ 2), and each of its
-      // 4 lanes splits and stores one column at a precomputed offset
+      const uint32_t tA = tmem + (uint32_t)(b * p.NAh);
       const uint32_t lanes = (uint32_t)(quad * 32) << 16;
-      const int nch = (p.NA - quarter * 32 + 127) / 128;
+      const uint32_t shift = (uint32_t)(part * p.NBh * 128);
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
         if (i >= nch) break;
         uint32_t r[32];
-        tmem_ld_32x32b_x32(tA + lanes + (uint32_t)(quarter * 32 + 128 * i), r);
+        tmem_ld_32x32b_x32(tA + lanes + (uint32_t)((quarter + 4 * i) * 32), r);
         tmem_ld_wait();
+        // groups of 4 columns: the quad sums its hi/lo rows (lane ^ 1) and
+        // exchanges re/im (lane ^ 2); each of its 4 lanes stores one column
 #pragma unroll
         for (int j0 = 0; j0 < 32; j0 += 4) {
           float v[4], o[4];
@@ -634,9 +666,11 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
           const uint32_t off = offs[i * 8 + j0 / 4];
           if (off != 0xffffffffu) {
             // explicit shared-space stores (the aligned base pointer is generic)
-            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_hi + off), "r"(*reinterpret_cast<const uint32_t*>(&h2))
+            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_hi + shift + off),
+                         "r"(*reinterpret_cast<const uint32_t*>(&h2))
                          : "memory");
-            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_lo + off), "r"(*reinterpret_cast<const uint32_t*>(&l2))
+            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_lo + shift + off),
+                         "r"(*reinterpret_cast<const uint32_t*>(&l2))
                          : "memory");
           }
         }
@@ -644,13 +678,15 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       fence_proxy_async();
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(bB_ready);
+      if (lane == 0) mbar_arrive(&bB_ready[b]);
     }
     // ---- TMEM_B -> this CTA's split-K plane (zeros when the CTA had no unit)
     const bool done = ok && mbar_wait_sleep(doneB, 0, abort_flag);
     tc_fence_after();
-    if (done) {
-      float* plane = p.planes + (int64_t)blockIdx.x * 128 * p.NB;
+    if (done && quad * 32 < p.live_rows) {
+      // column-major plane [NB][live_rows]: a warp's 32 lanes (rows) store 128
+      // consecutive bytes per column
+      float* plane = p.planes + (int64_t)blockIdx.x * p.live_rows * p.NB;
       const int row = quad * 32 + lane;
       for (int c0 = quarter * 32; c0 < p.NB; c0 += 128) {
         uint32_t r[32];
@@ -658,7 +694,8 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         tmem_ld_wait();
 #pragma unroll
         for (int j = 0; j < 32; ++j)
-          if (c0 + j < p.NB) plane[(int64_t)row * p.NB + c0 + j] = uc > 0 ? __uint_as_float(r[j]) : 0.f;
+          if (c0 + j < p.NB && row < p.live_rows)
+            plane[(int64_t)(c0 + j) * p.live_rows + row] = n_units > 0 ? __uint_as_float(r[j]) : 0.f;
       }
     }
   }
@@ -672,8 +709,8 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
 }
 
 int fused_grid(const S3& s, const TermGroups& tg) {
-  const int64_t units = (s.x0 * s.x1 * s.l0 * s.l1 / 32) * (int64_t)tg.i1.size();
-  return (int)std::max<int64_t>(1, std::min<int64_t>(152, units));
+  const int64_t pairs = (s.x0 * s.x1 * s.l0 * s.l1 / 32) * (int64_t)tg.i1.size();
+  return (int)std::max<int64_t>(1, std::min<int64_t>(152, pairs));
 }
 
 bool fused_eligible(const S3& s, int nvec, const TermGroups& tg) {
@@ -750,12 +787,19 @@ int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, con
   memset(&maps, 0, sizeof(maps));
   FusedParams fp;
   memset(&fp, 0, sizeof(fp));
+  fp.NA = (int)g.NA;
+  fp.NB = (int)(nvec * s.l0 * s.l1 * s.d);
+  // two vector parts per pair when the halves stay MMA-shaped: TMEM_A is then
+  // double-buffered and one part's fold overlaps the next part's MMAs
+  fp.VH = (nvec % 2 == 0 && (fp.NA / 2) % 16 == 0 && (fp.NB / 2) % 16 == 0) ? 2 : 1;
+  fp.NAh = fp.NA / fp.VH;
+  fp.NBh = fp.NB / fp.VH;
   const char* planA = static_cast<const char*>(plan);
   for (int q = 0; q < G; ++q) {
     const int64_t kpA = g.regA * (int64_t)tg.terms[q].size();
     CARC_RETURN_IF(tma_map_bf16(&maps.a[q], planA, (uint64_t)kpA, (uint64_t)g1.rowsA_a, 128));
     CARC_RETURN_IF(tma_map_bf16(&maps.vin[q], w.vin + w.vin_off[q], (uint64_t)kpA, (uint64_t)g.rowsA_b,
-                                (uint32_t)g.NA));
+                                (uint32_t)fp.NAh));
     fp.nkb[q] = (int)(kpA / 64);
     planA += a256(g1.rowsA_a * kpA * 2);
   }
@@ -768,21 +812,25 @@ int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, con
   fp.XP = 32 / fp.L;
   fp.x_tiles = (int)(s.x0 * s.x1 * s.l0 * s.l1 / 32);
   fp.G = G;
-  fp.n_units = fp.x_tiles * G;
-  fp.NA = (int)g.NA;
-  fp.NB = (int)(nvec * s.l0 * s.l1 * s.d);
+  fp.n_pairs = fp.x_tiles * G;
+  fp.nbuf = 2 * fp.NAh <= 256 ? 2 : 1;
+  fp.stage_bytes = FU_STAGE_A + fp.NAh * 128;
+  const int fixed = 1024 + 2 * FU_BB_ATOM + 2 * FU_AB_ATOM + 256 * 8 + 32 * 8 + 512;
+  fp.stages = fixed + FU_STAGES * fp.stage_bytes <= FU_SMEM_BIG ? FU_STAGES : 2;
+  const int smem = fixed + fp.stages * fp.stage_bytes;
   fp.regB = g.regB;
   fp.kcB = g.kcB;
+  fp.live_rows = (int)round_up(4 * s.l2 * s.l3, 32);
   fp.planes = w.pB;
   fp.err = status;
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(stage3_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM);
+    attr = cudaFuncSetAttribute(stage3_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM_BIG);
   });
   if (attr != cudaSuccess) return fail(CARC_CUDA_ERROR, "fused matvec: %s", cudaGetErrorString(attr));
   PhaseScope ph(PH_TC_STEP_A, stream);
-  stage3_fused_kernel<<<w.ksB, FU_THREADS, FU_SMEM, stream>>>(maps, fp);
+  stage3_fused_kernel<<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }
@@ -848,7 +896,7 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   if (w.fused) {
     CARC_RETURN_IF(launch_fused(s, nvec, tg, g1, g, plan, w, status, stream));
     plane_ld = rows_valid_w;
-    plane_stride = 128 * rows_valid_w;
+    plane_stride = round_up(4 * s.l2 * s.l3, 32) * rows_valid_w;
   } else {
     CARC_RETURN_IF(unfused_steps(s, nvec, tg, g1, g, plan, w, status, stream));
     plane_ld = g.rowsB_b;
@@ -867,6 +915,9 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   o.n_ext[2] = s.l1; o.n_str[2] = yl1;
   o.n_ext[3] = s.d; o.n_str[3] = 1;
   PhaseScope ph(PH_TC_REDUCE, stream);
+  if (w.fused)  // column-major planes [z][n][row]
+    return reduce_planes_colmajor(w.pB, round_up(4 * s.l2 * s.l3, 32), plane_stride, w.ksB, o, make_double2(1, 0),
+                                  accumulate, stream);
   return reduce_partials2(w.pB, plane_ld, plane_stride, w.ksB, o, make_double2(1, 0), accumulate, w.red,
                           reduce_partials2_workspace(s.l2 * s.l3, rows_valid_w, w.ksB), stream);
 }

@@ -559,6 +559,37 @@ __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const floa
   }
 }
 
+// Column-major planes P[z][n][r] (r = 4m + 2c + s over `rows` rows): a block
+// covers one column n and 32 consecutive rows (8 complex m), its 8 warps take
+// planes z = w, w+8, ... (coalesced 128-byte loads), partial sums added in
+// warp order, then each quad of lanes folds its 4 rows into C[m, n].
+__global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_cm_kernel(const float* __restrict__ P,
+                                                                          double2* __restrict__ C, int64_t rows,
+                                                                          const __grid_constant__ ReduceParams p) {
+  __shared__ double part[RP_WARPS][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t n = blockIdx.x;
+  const int64_t r = (int64_t)blockIdx.y * 32 + lane;
+  double acc = 0.0;
+  if (r < rows)
+    for (int z = w; z < p.ksplit; z += RP_WARPS) acc += (double)P[z * p.split_stride + n * rows + r];
+  part[w][lane] = acc;
+  __syncthreads();
+  if (w == 0) {
+    double v = part[0][lane];
+    for (int q = 1; q < RP_WARPS; ++q) v += part[q][lane];
+    v += __shfl_xor_sync(0xffffffffu, v, 1);            // hi + lo
+    const double o = __shfl_xor_sync(0xffffffffu, v, 2);  // the other of re / im
+    const int64_t m = r >> 2;
+    if ((lane & 3) == 0 && m < p.Mc) {
+      double2 val = cmul(p.alpha, make_double2(v, o));
+      const int64_t off = pdecomp(m, p.nm, p.m_ext, p.m_str) + pdecomp(n, p.nn, p.n_ext, p.n_str);
+      if (p.accumulate) val = cadd(val, C[off]);
+      C[off] = val;
+    }
+  }
+}
+
 inline int grid_of(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8 * 152)); }
 
 PackParams pack_params(const ZView& v, int64_t rows_out, int64_t kp_out, int64_t col_off) {
@@ -693,6 +724,36 @@ int reduce_partials2(const float* P, int64_t ld, int64_t split_stride, int kspli
   if (p.Mc > 65535) return fail(CARC_TOO_LARGE, "reduce: %lld output rows", (long long)p.Mc);
   dim3 grid((unsigned)((p.Nc + 31) / 32), (unsigned)p.Mc);
   reduce_planes_kernel<<<grid, 32 * RP_WARPS, 0, stream>>>(P, static_cast<double2*>(o.base), p);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+int reduce_planes_colmajor(const float* P, int64_t rows, int64_t split_stride, int ksplit, const ZOut& o,
+                           double2 alpha, int accumulate, cudaStream_t stream) {
+  ReduceParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.nm = o.nm;
+  p.nn = o.nn;
+  p.Mc = 1;
+  p.Nc = 1;
+  for (int i = 0; i < o.nm; ++i) {
+    p.m_ext[i] = o.m_ext[i];
+    p.m_str[i] = o.m_str[i];
+    p.Mc *= o.m_ext[i];
+  }
+  for (int i = 0; i < o.nn; ++i) {
+    p.n_ext[i] = o.n_ext[i];
+    p.n_str[i] = o.n_str[i];
+    p.Nc *= o.n_ext[i];
+  }
+  p.split_stride = split_stride;
+  p.ksplit = ksplit;
+  p.accumulate = accumulate;
+  p.alpha = alpha;
+  if (4 * p.Mc > rows || rows % 32 != 0) return fail(CARC_BAD_ARG, "reduce: %lld plane rows", (long long)rows);
+  if (p.Nc > 0x7fffffff) return fail(CARC_TOO_LARGE, "reduce: %lld output columns", (long long)p.Nc);
+  dim3 grid((unsigned)p.Nc, (unsigned)(rows / 32));
+  reduce_planes_cm_kernel<<<grid, 32 * RP_WARPS, 0, stream>>>(P, static_cast<double2*>(o.base), rows, p);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }

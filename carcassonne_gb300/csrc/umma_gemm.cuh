@@ -56,6 +56,9 @@ int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const F
 // launch (coalesced over columns, planes spread over 8 warps per block); the
 // workspace arguments are kept for the callers' layouts and need 256 bytes.
 int64_t reduce_partials2_workspace(int64_t Mc, int64_t Nc, int ksplit);
+// The same for column-major planes P[z][n][r] with `rows` rows (a multiple of 32).
+int reduce_planes_colmajor(const float* P, int64_t rows, int64_t split_stride, int ksplit, const ZOut& o,
+                           double2 alpha, int accumulate, cudaStream_t stream);
 int reduce_partials2(const float* P, int64_t ld, int64_t split_stride, int ksplit, const ZOut& o, double2 alpha,
                      int accumulate, void* ws, int64_t ws_bytes, cudaStream_t stream);
 // role 0: A operand (rows (m, re/im, hi/lo)); role 1: B operand (row n, K = [hi | lo]).
