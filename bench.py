@@ -54,9 +54,9 @@ KERNEL_OF_PHASE = dict(pack="pack_vin_kernel", step_a="gemm_bf16_tn_kernel<256,1
 # (profiles/ holds the summary and the command that produced it)
 NCU_TRAFFIC = {
     ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "fused"): dict(
-        bytes_per_launch=131.5e6,
-        source="profiles/stage3_fused_matvec_D4_chi32_nvec8.md: one fused launch, dram read 126.5 MB + write "
-               "5.0 MB"),
+        bytes_per_launch=129.5e6,
+        source="profiles/stage3_fused_matvec_D4_chi32_nvec8.md: one fused launch, dram read 126.2 MB + write "
+               "3.2 MB"),
     ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "step_a"): dict(
         bytes_per_launch=8.97e6,
         source="profiles/stage3_tc_matvec_D4_chi32_nvec8.md: one step-A launch (1-term group, 41.9 MB "
@@ -102,11 +102,12 @@ def tc_bytes_per_step(opr, nvec):
         out["step_b"] += 2 * (live_rows * kp_b + rows_w * kp_b) + 4 * ks_b * rows_sb * rows_w
         out["launches"]["step_b"] += 1
         # the fused kernel (W on chip): packed S2_0 and Vin of every term, the
-        # live rows of the packed S2_1 tags, one FP32 plane per CTA
+        # live rows of the packed S2_1 tags, one FP32 plane of the live rows
+        # (rounded to 32) per CTA
         units = (x0 * x1 * l0 * l1 // 32) * len(groups)
         grid = max(1, min(152, units))
         out["fused"] = out.get("fused", 0) + 2 * (rows_a * reg_a * nt + rows_vin * reg_a * nt + live_rows * kp_b) \
-            + 4 * grid * 128 * rows_w
+            + 4 * grid * _round_up(live_b, 32) * rows_w
         out["launches"]["fused"] = out["launches"].get("fused", 0) + 1
     return out
 
