@@ -493,27 +493,41 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   const uint32_t tmem = *tmem_slot;
   const uint32_t tB = tmem + 256;
 
+  // Per-CTA walk over pairs pr = blockIdx.x + pc * gridDim.x, t = pr / G,
+  // g = pr % G, advanced incrementally (no division in the loops).
+  const int t_step = (int)gridDim.x / p.G, g_step = (int)gridDim.x % p.G;
   if (warp == 0) {
     if (lane == 0) {
       // ---- TMA producer of step A: the unit's S2_0 tile and its Vin part
-      for (int g = 0; g < p.G; ++g) {
-        prefetch_tensormap(&maps.a[g]);
-        prefetch_tensormap(&maps.vin[g]);
+      for (int q = 0; q < p.G; ++q) {
+        prefetch_tensormap(&maps.a[q]);
+        prefetch_tensormap(&maps.vin[q]);
       }
       prefetch_tensormap(&maps.b);
-      int kbg = 0, issued = 0;
+      int issued = 0, s = 0, t = (int)blockIdx.x / p.G, g = (int)blockIdx.x % p.G, part = 0;
+      uint32_t ph = 0;
       bool ok = true;
       for (int uc = 0; ok && uc < n_units; ++uc) {
-        const int pr = (int)blockIdx.x + (uc / p.VH) * (int)gridDim.x, part = uc % p.VH;
-        const int t = pr / p.G, g = pr % p.G;
-        for (int kb = 0; kb < p.nkb[g]; ++kb, ++kbg) {
-          const int s = kbg % p.stages;
-          const uint32_t ph = (uint32_t)((kbg / p.stages) & 1);
+        const int nkb = p.nkb[g];
+        for (int kb = 0; kb < nkb; ++kb) {
           if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
+          uint8_t* st = stage + s * p.stage_bytes;
           mbar_arrive_expect_tx(&full[s], (uint32_t)(FU_STAGE_A + p.NAh * 128));
-          tma_load_2d(stage + s * p.stage_bytes, &maps.a[g], kb * 64, t * 128, &full[s]);
-          tma_load_2d(stage + s * p.stage_bytes + FU_STAGE_A, &maps.vin[g], kb * 64, part * p.NAh, &full[s]);
+          tma_load_2d(st, &maps.a[g], kb * 64, t * 128, &full[s]);
+          tma_load_2d(st + FU_STAGE_A, &maps.vin[g], kb * 64, part * p.NAh, &full[s]);
           ++issued;
+          if (++s == p.stages) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (++part == p.VH) {
+          part = 0;
+          t += t_step;
+          if ((g += g_step) >= p.G) {
+            g -= p.G;
+            ++t;
+          }
         }
       }
       if (*abort_flag) {
@@ -526,16 +540,19 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   } else if (warp == 18) {
     if (lane == 0) {
       // ---- TMA producer of step B's S2_1 slice, one per pair
-      int issued = 0;
+      int issued = 0, t = (int)blockIdx.x / p.G, g = (int)blockIdx.x % p.G;
       for (int pc = 0; pc < my_pairs; ++pc) {
-        const int pr = (int)blockIdx.x + pc * (int)gridDim.x;
-        const int t = pr / p.G, g = pr % p.G;
         if (!mbar_wait_sleep(aB_empty, (uint32_t)((pc & 1) ^ 1), abort_flag)) break;
         mbar_arrive_expect_tx(aB_full, (uint32_t)(2 * p.a_rows * 128));
         const int64_t kk0 = (int64_t)t * p.XP * p.K23;
         tma_load_2d(aB, &maps.b, (int)(g * p.regB + 2 * kk0), 0, aB_full);
         tma_load_2d(aB + FU_AB_ATOM, &maps.b, (int)(g * p.regB + 2 * p.kcB + 2 * kk0), 0, aB_full);
         ++issued;
+        t += t_step;
+        if ((g += g_step) >= p.G) {
+          g -= p.G;
+          ++t;
+        }
       }
       if (*abort_flag && issued > 0)
         for (uint32_t q = 0; q < (1u << 20); ++q)
@@ -545,54 +562,77 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     if (lane == 0) {
       // ---- MMA issuer.  Iteration uc issues MMA-A(uc) into TMEM_A buffer
       // uc % nbuf, then MMA-B(uc - 1) once its fold is done: the tensor pipe
-      // works on unit uc while the epilogue warps fold unit uc - 1.
+      // works on unit uc while the epilogue warps fold unit uc - 1.  The
+      // issuing thread runs a serial chain, so everything per MMA is an add
+      // to precomputed descriptors (start-address field = bytes >> 4).
       const uint32_t idA = idesc_bf16_f32(128, p.NAh), idB = idesc_bf16_f32(128, p.NBh);
-      int kbg = 0;
-      bool ok = true;
-      auto step_b = [&](int u) -> bool {
-        // MMA-B of unit u: its fold wrote B_B part (u % VH); the pair's S2_1 slice is loaded
-        const int b = u % p.nbuf, part = u % p.VH, pc = u / p.VH;
-        if (!mbar_wait_sleep(&bB_ready[b], (uint32_t)((u / p.nbuf) & 1), abort_flag)) return false;
-        if (part == 0 && !mbar_wait_sleep(aB_full, (uint32_t)(pc & 1), abort_flag)) return false;
+      const uint64_t dStage = smem_desc_sw128(smem_u32(stage));
+      const uint64_t dAB = smem_desc_sw128(smem_u32(aB)), dBB = smem_desc_sw128(smem_u32(bB));
+      const uint32_t dStageStep = (uint32_t)p.stage_bytes >> 4, dPartB = (uint32_t)(p.NBh * 128) >> 4;
+      constexpr uint32_t dV = FU_STAGE_A >> 4, dAtomAB = FU_AB_ATOM >> 4, dAtomBB = FU_BB_ATOM >> 4;
+      struct Unit {
+        int b, part, pc;
+        uint32_t bph;  // phase parity of the unit's use of TMEM_A buffer b
+      };
+      auto advance = [&](Unit u) {
+        if (++u.part == p.VH) {
+          u.part = 0;
+          ++u.pc;
+        }
+        if (++u.b == p.nbuf) {
+          u.b = 0;
+          u.bph ^= 1u;
+        }
+        return u;
+      };
+      auto step_b = [&](const Unit& u) -> bool {
+        // MMA-B of unit u: its fold wrote B_B part u.part; the pair's S2_1 slice is loaded
+        if (!mbar_wait_sleep(&bB_ready[u.b], u.bph, abort_flag)) return false;
+        if (u.part == 0 && !mbar_wait_sleep(aB_full, (uint32_t)(u.pc & 1), abort_flag)) return false;
         tc_fence_after();
+        const uint32_t d = tB + (uint32_t)(u.part * p.NBh);
+        const uint64_t bb = dBB + u.part * dPartB;
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const uint32_t a0 = smem_u32(aB + h * FU_AB_ATOM);
-          const uint32_t b0 = smem_u32(bB + h * FU_BB_ATOM + part * p.NBh * 128);
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(tB + (uint32_t)(part * p.NBh), smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idB,
-                     (pc > 0 || h > 0 || kk > 0) ? 1u : 0u);
-        }
-        mma_commit(&bB_free[part]);
-        if (part == p.VH - 1) mma_commit(aB_empty);
+            mma_bf16(d, dAB + (h * dAtomAB + kk * 2), bb + (h * dAtomBB + kk * 2), idB,
+                     (u.pc > 0 || h > 0 || kk > 0) ? 1u : 0u);
+        mma_commit(&bB_free[u.part]);
+        if (u.part == p.VH - 1) mma_commit(aB_empty);
         return true;
       };
+      int s = 0, g = (int)blockIdx.x % p.G;
+      uint32_t ph = 0;
+      bool ok = true;
+      Unit cur{0, 0, 0, 0u}, prev{0, 0, 0, 0u};
       for (int uc = 0; ok && uc < n_units; ++uc) {
-        const int pr = (int)blockIdx.x + (uc / p.VH) * (int)gridDim.x;
-        const int g = pr % p.G, b = uc % p.nbuf;
-        // TMEM_A buffer b was last read by the fold of unit uc - nbuf
-        if (uc >= p.nbuf &&
-            !(ok = mbar_wait_sleep(&bB_ready[b], (uint32_t)(((uc - p.nbuf) / p.nbuf) & 1), abort_flag)))
-          break;
-        const uint32_t tA = tmem + (uint32_t)(b * p.NAh);
-        for (int kb = 0; kb < p.nkb[g]; ++kb, ++kbg) {
-          const int s = kbg % p.stages;
-          const uint32_t ph = (uint32_t)((kbg / p.stages) & 1);
+        // TMEM_A buffer cur.b was last read by the fold of unit uc - nbuf: with
+        // two buffers step_b(uc - 2) of the previous iteration waited for it
+        if (p.nbuf == 1 && uc > 0 && !(ok = mbar_wait_sleep(&bB_ready[0], prev.bph, abort_flag))) break;
+        const uint32_t tA = tmem + (uint32_t)(cur.b * p.NAh);
+        const int nkb = p.nkb[g];
+        for (int kb = 0; kb < nkb; ++kb) {
           if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
           tc_fence_after();
-          const uint32_t a0 = smem_u32(stage + s * p.stage_bytes), b0 = smem_u32(stage + s * p.stage_bytes + FU_STAGE_A);
+          const uint64_t da = dStage + s * dStageStep;
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(tA, smem_desc_sw128(a0 + kk * 32), smem_desc_sw128(b0 + kk * 32), idA,
-                     (kb > 0 || kk > 0) ? 1u : 0u);
+            mma_bf16(tA, da + kk * 2, da + (dV + kk * 2), idA, (kb > 0 || kk > 0) ? 1u : 0u);
           mma_commit(&empty[s]);
+          if (++s == p.stages) {
+            s = 0;
+            ph ^= 1u;
+          }
         }
         if (!ok) break;
-        mma_commit(&accA_full[b]);
-        if (uc > 0 && !(ok = step_b(uc - 1))) break;
+        mma_commit(&accA_full[cur.b]);
+        if (uc > 0 && !(ok = step_b(prev))) break;
+        prev = cur;
+        cur = advance(cur);
+        if (cur.part == 0 && (g += g_step) >= p.G) g -= p.G;
       }
-      if (ok && n_units > 0) ok = step_b(n_units - 1);
+      if (ok && n_units > 0) ok = step_b(prev);
       mma_commit(doneB);
     }
   } else if (warp >= 2 && warp <= 17) {
@@ -629,14 +669,13 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         }
         offs[i * 8 + gi] = off;
       }
-    int uc = 0;
     bool ok = true;
-    for (; uc < n_units; ++uc) {
-      const int b = uc % p.nbuf, part = uc % p.VH;
-      if (!(ok = mbar_wait_sleep(&accA_full[b], (uint32_t)((uc / p.nbuf) & 1), abort_flag))) break;
-      // B_B part `part` was last read by the MMA-B of unit uc - VH
-      if (uc >= p.VH && !(ok = mbar_wait_sleep(&bB_free[part], (uint32_t)(((uc - p.VH) / p.VH) & 1), abort_flag)))
-        break;
+    int b = 0, part = 0, pc = 0;
+    uint32_t bph = 0;
+    for (int uc = 0; uc < n_units; ++uc) {
+      if (!(ok = mbar_wait_sleep(&accA_full[b], bph, abort_flag))) break;
+      // B_B part `part` was last read by the MMA-B of unit uc - VH (pair pc - 1)
+      if (pc > 0 && !(ok = mbar_wait_sleep(&bB_free[part], (uint32_t)((pc & 1) ^ 1), abort_flag))) break;
       tc_fence_after();
       const uint32_t tA = tmem + (uint32_t)(b * p.NAh);
       const uint32_t lanes = (uint32_t)(quad * 32) << 16;
@@ -679,6 +718,14 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&bB_ready[b]);
+      if (++b == p.nbuf) {
+        b = 0;
+        bph ^= 1u;
+      }
+      if (++part == p.VH) {
+        part = 0;
+        ++pc;
+      }
     }
     // ---- TMEM_B -> this CTA's split-K plane (zeros when the CTA had no unit)
     const bool done = ok && mbar_wait_sleep(doneB, 0, abort_flag);

@@ -84,7 +84,24 @@ __device__ __forceinline__ bool mbar_try_wait_suspend(uint64_t* bar, uint32_t pa
   return ok != 0;
 }
 
+// Non-blocking test of a phase: returns at once, so a wait whose phase has
+// already completed costs one shared-memory round trip.
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
 __device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, volatile int* abort) {
+  if (mbar_test(bar, parity)) return true;
   for (uint32_t i = 0; i < kSleepPolls; ++i) {
     if (mbar_try_wait_suspend(bar, parity)) return true;
     if (*abort) return false;
