@@ -559,37 +559,39 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
           if (mbar_try_wait(aB_full, (uint32_t)((issued - 1) & 1))) break;
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      // ---- MMA issuer.  Iteration uc issues MMA-A(uc) into TMEM_A buffer
-      // uc % nbuf, then MMA-B(uc - 1) once its fold is done: the tensor pipe
-      // works on unit uc while the epilogue warps fold unit uc - 1.  The
-      // issuing thread runs a serial chain, so everything per MMA is an add
-      // to precomputed descriptors (start-address field = bytes >> 4).
-      const uint32_t idA = idesc_bf16_f32(128, p.NAh), idB = idesc_bf16_f32(128, p.NBh);
-      const uint64_t dStage = smem_desc_sw128(smem_u32(stage));
-      const uint64_t dAB = smem_desc_sw128(smem_u32(aB)), dBB = smem_desc_sw128(smem_u32(bB));
-      const uint32_t dStageStep = (uint32_t)p.stage_bytes >> 4, dPartB = (uint32_t)(p.NBh * 128) >> 4;
-      constexpr uint32_t dV = FU_STAGE_A >> 4, dAtomAB = FU_AB_ATOM >> 4, dAtomBB = FU_BB_ATOM >> 4;
-      struct Unit {
-        int b, part, pc;
-        uint32_t bph;  // phase parity of the unit's use of TMEM_A buffer b
-      };
-      auto advance = [&](Unit u) {
-        if (++u.part == p.VH) {
-          u.part = 0;
-          ++u.pc;
-        }
-        if (++u.b == p.nbuf) {
-          u.b = 0;
-          u.bph ^= 1u;
-        }
-        return u;
-      };
-      auto step_b = [&](const Unit& u) -> bool {
-        // MMA-B of unit u: its fold wrote B_B part u.part; the pair's S2_1 slice is loaded
-        if (!mbar_wait_sleep(&bB_ready[u.b], u.bph, abort_flag)) return false;
-        if (u.part == 0 && !mbar_wait_sleep(aB_full, (uint32_t)(u.pc & 1), abort_flag)) return false;
-        tc_fence_after();
+    // ---- MMA issuer.  Iteration uc issues MMA-A(uc) into TMEM_A buffer
+    // uc % nbuf, then MMA-B(uc - 1) once its fold is done: the tensor pipe
+    // works on unit uc while the epilogue warps fold unit uc - 1.  The whole
+    // warp runs the loop (its values stay warp-uniform) and one elected lane
+    // issues each MMA and commit; per MMA the descriptors only advance their
+    // start-address field (bytes >> 4).
+    const bool leader = elect_one();
+    const uint32_t idA = idesc_bf16_f32(128, p.NAh), idB = idesc_bf16_f32(128, p.NBh);
+    const uint64_t dStage = smem_desc_sw128(smem_u32(stage));
+    const uint64_t dAB = smem_desc_sw128(smem_u32(aB)), dBB = smem_desc_sw128(smem_u32(bB));
+    const uint32_t dStageStep = (uint32_t)p.stage_bytes >> 4, dPartB = (uint32_t)(p.NBh * 128) >> 4;
+    constexpr uint32_t dV = FU_STAGE_A >> 4, dAtomAB = FU_AB_ATOM >> 4, dAtomBB = FU_BB_ATOM >> 4;
+    struct Unit {
+      int b, part, pc;
+      uint32_t bph;  // phase parity of the unit's use of TMEM_A buffer b
+    };
+    auto advance = [&](Unit u) {
+      if (++u.part == p.VH) {
+        u.part = 0;
+        ++u.pc;
+      }
+      if (++u.b == p.nbuf) {
+        u.b = 0;
+        u.bph ^= 1u;
+      }
+      return u;
+    };
+    auto step_b = [&](const Unit& u) -> bool {
+      // MMA-B of unit u: its fold wrote B_B part u.part; the pair's S2_1 slice is loaded
+      if (!mbar_wait_sleep(&bB_ready[u.b], u.bph, abort_flag)) return false;
+      if (u.part == 0 && !mbar_wait_sleep(aB_full, (uint32_t)(u.pc & 1), abort_flag)) return false;
+      tc_fence_after();
+      if (leader) {
         const uint32_t d = tB + (uint32_t)(u.part * p.NBh);
         const uint64_t bb = dBB + u.part * dPartB;
 #pragma unroll
@@ -600,41 +602,47 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
                      (u.pc > 0 || h > 0 || kk > 0) ? 1u : 0u);
         mma_commit(&bB_free[u.part]);
         if (u.part == p.VH - 1) mma_commit(aB_empty);
-        return true;
-      };
-      int s = 0, g = (int)blockIdx.x % p.G;
-      uint32_t ph = 0;
-      bool ok = true;
-      Unit cur{0, 0, 0, 0u}, prev{0, 0, 0, 0u};
-      for (int uc = 0; ok && uc < n_units; ++uc) {
-        // TMEM_A buffer cur.b was last read by the fold of unit uc - nbuf: with
-        // two buffers step_b(uc - 2) of the previous iteration waited for it
-        if (p.nbuf == 1 && uc > 0 && !(ok = mbar_wait_sleep(&bB_ready[0], prev.bph, abort_flag))) break;
-        const uint32_t tA = tmem + (uint32_t)(cur.b * p.NAh);
-        const int nkb = p.nkb[g];
-        for (int kb = 0; kb < nkb; ++kb) {
-          if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
-          tc_fence_after();
+      }
+      __syncwarp();
+      return true;
+    };
+    int s = 0, g = (int)blockIdx.x % p.G;
+    uint32_t ph = 0;
+    bool ok = true;
+    Unit cur{0, 0, 0, 0u}, prev{0, 0, 0, 0u};
+    for (int uc = 0; ok && uc < n_units; ++uc) {
+      // TMEM_A buffer cur.b was last read by the fold of unit uc - nbuf: with
+      // two buffers step_b(uc - 2) of the previous iteration waited for it
+      if (p.nbuf == 1 && uc > 0 && !(ok = mbar_wait_sleep(&bB_ready[0], prev.bph, abort_flag))) break;
+      const uint32_t tA = tmem + (uint32_t)(cur.b * p.NAh);
+      const int nkb = p.nkb[g];
+      for (int kb = 0; kb < nkb; ++kb) {
+        if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
+        tc_fence_after();
+        if (leader) {
           const uint64_t da = dStage + s * dStageStep;
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk)
             mma_bf16(tA, da + kk * 2, da + (dV + kk * 2), idA, (kb > 0 || kk > 0) ? 1u : 0u);
           mma_commit(&empty[s]);
-          if (++s == p.stages) {
-            s = 0;
-            ph ^= 1u;
-          }
         }
-        if (!ok) break;
-        mma_commit(&accA_full[cur.b]);
-        if (uc > 0 && !(ok = step_b(prev))) break;
-        prev = cur;
-        cur = advance(cur);
-        if (cur.part == 0 && (g += g_step) >= p.G) g -= p.G;
+        __syncwarp();
+        if (++s == p.stages) {
+          s = 0;
+          ph ^= 1u;
+        }
       }
-      if (ok && n_units > 0) ok = step_b(prev);
-      mma_commit(doneB);
+      if (!ok) break;
+      if (leader) mma_commit(&accA_full[cur.b]);
+      __syncwarp();
+      if (uc > 0 && !(ok = step_b(prev))) break;
+      prev = cur;
+      cur = advance(cur);
+      if (cur.part == 0 && (g += g_step) >= p.G) g -= p.G;
     }
+    if (ok && n_units > 0) ok = step_b(prev);
+    if (leader) mma_commit(doneB);
+    __syncwarp();
   } else if (warp >= 2 && warp <= 17) {
     // ---- fold epilogue: warps 2..17; quadrant = warp % 4, column quarter = (warp - 2) / 4
     const int quad = warp & 3, quarter = (warp - 2) >> 2;

@@ -122,6 +122,19 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap* map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
+// One lane of the (converged) warp is elected: true in exactly one lane.
+__device__ __forceinline__ bool elect_one() {
+  uint32_t is_elected = 0;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "elect.sync _|p, 0xffffffff;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(is_elected));
+  return is_elected != 0;
+}
+
 // ---- TMEM -------------------------------------------------------------------
 // Executed by one full warp; the allocated base address is written to *slot.
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
