@@ -437,6 +437,9 @@ struct FusedParams {
 // Unit uc of a CTA (local counter) is part (uc % VH) of its pair (uc / VH);
 // the CTA takes pairs blockIdx.x, blockIdx.x + gridDim.x, ... so that both
 // parts of a pair run back to back (they share the pair's S2_1 slice).
+// DD = d, the physical dimension (1, 2, 4 or 8): a compile-time constant so
+// that the fold's register indexing is static.
+template <int DD>
 __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __grid_constant__ FusedMaps maps,
                                                                      const __grid_constant__ FusedParams p) {
   using namespace umma;
@@ -650,33 +653,43 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     // tables over the columns of part 0 (part h shifts the B_B rows by h NBh):
     // per step-A column n = (vec, k23, p): {B_B row part, k part}; per tile row m = (xp, l)
     for (int n = et; n < p.NAh; n += 512) {
-      const int pp = n % p.d, q = n / p.d;
+      const int pp = n % DD, q = n / DD;
       const int k23 = q % p.K23, vec = q / p.K23;
-      tabN[n] = make_int2(vec * p.L * p.d + pp, k23);
+      tabN[n] = make_int2(vec * p.L * DD + pp, k23);
     }
-    if (et < 32) tabM[et] = make_int2((et % p.L) * p.d, (et / p.L) * p.K23);
+    if (et < 32) tabM[et] = make_int2((et % p.L) * DD, (et / p.L) * p.K23);
     asm volatile("bar.sync 1, 512;" ::: "memory");
     const int m = quad * 8 + (lane >> 2);  // complex row of this lane's quad within the tile
     const int2 tm = tabM[m];
     const uint32_t sh_hi = smem_u32(bB), sh_lo = smem_u32(bB + FU_BB_ATOM);
+    // Ownership after the two exchange stages.  The 32 columns of a chunk form
+    // 8 sets of 4 columns with one (vec, p) and 4 consecutive k23 (column
+    // stride d): the 4 complex values of a set are 16 contiguous bytes of one
+    // B_B row, written with one 16-byte store per half (hi, lo).  Lane
+    // (c, h) = ((lane >> 1) & 1, lane & 1) of a quad ends with sets
+    // 4h + 2c + s2, s2 = 0, 1.  Set S holds chunk columns (S / d) 4d + e d + S % d.
+    const int hsel = lane & 1, csel = (lane >> 1) & 1;
+    const int nchunks = (p.NAh + 31) / 32;
+    const int nch = (nchunks - quarter + 3) / 4;  // chunks quarter, quarter + 4
     // This lane's B_B byte offsets are the same in every unit (plus the part's
     // row shift): computed once, so no shared-memory load sits between stores.
-    const int qsel = lane & 3;
-    const int nch = (p.NAh / 32 - quarter + 3) / 4;  // chunks quarter, quarter + 4, ...
-    uint32_t offs[16];
+    uint32_t offs[4];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
-      for (int gi = 0; gi < 8; ++gi) {
-        const int col = (quarter + 4 * i) * 32 + 4 * gi + qsel;
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int S = 4 * hsel + 2 * csel + s2;
+        const int col = (quarter + 4 * i) * 32 + (S / DD) * 4 * DD + S % DD;
         uint32_t off = 0xffffffffu;
         if (i < nch && col < p.NAh) {
           const int2 tn = tabN[col];
-          const int row = tn.x + tm.x, kk = tn.y + tm.y;
-          off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + (((kk >> 2) ^ (row & 7)) << 4) + ((kk & 3) << 2));
+          const int row = tn.x + tm.x, kk = tn.y + tm.y;  // kk % 4 == 0
+          off = (uint32_t)((row >> 3) * 1024 + (row & 7) * 128 + (((kk >> 2) ^ (row & 7)) << 4));
         }
-        offs[i * 8 + gi] = off;
+        offs[i * 2 + s2] = off;
       }
+    // chunk column of element e of set S: (S / d) 4d + e d + S % d
+    auto setcol = [](int S, int e) { return (S / DD) * 4 * DD + e * DD + S % DD; };
     bool ok = true;
     int b = 0, part = 0, pc = 0;
     uint32_t bph = 0;
@@ -694,30 +707,39 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         uint32_t r[32];
         tmem_ld_32x32b_x32(tA + lanes + (uint32_t)((quarter + 4 * i) * 32), r);
         tmem_ld_wait();
-        // groups of 4 columns: the quad sums its hi/lo rows (lane ^ 1) and
-        // exchanges re/im (lane ^ 2); each of its 4 lanes stores one column
+        // stage 1 (lane ^ 1): sum the hi/lo rows; lane h keeps sets 4h..4h+3
+        float v[16];
 #pragma unroll
-        for (int j0 = 0; j0 < 32; j0 += 4) {
-          float v[4], o[4];
+        for (int k = 0; k < 16; ++k) {
+          const float a = __uint_as_float(r[setcol(k >> 2, k & 3)]);
+          const float z = __uint_as_float(r[setcol(4 + (k >> 2), k & 3)]);
+          const float keep = hsel ? z : a, send = hsel ? a : z;
+          v[k] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+        }
+        // stage 2 (lane ^ 2): exchange re/im; lane c keeps sets 4h + 2c + s2
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            v[q] = __uint_as_float(r[j0 + q]) + __shfl_xor_sync(0xffffffffu, __uint_as_float(r[j0 + q]), 1);
+        for (int s2 = 0; s2 < 2; ++s2) {
+          uint32_t hi[4], lo[4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) o[q] = __shfl_xor_sync(0xffffffffu, v[q], 2);
-          const float vq = qsel == 0 ? v[0] : qsel == 1 ? v[1] : qsel == 2 ? v[2] : v[3];
-          const float oq = qsel == 0 ? o[0] : qsel == 1 ? o[1] : qsel == 2 ? o[2] : o[3];
-          const float re = (lane & 2) ? oq : vq, im = (lane & 2) ? vq : oq;
-          const __nv_bfloat162 h2 = __floats2bfloat162_rn(re, im);
-          const float2 hf = __bfloat1622float2(h2);
-          const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
-          const uint32_t off = offs[i * 8 + j0 / 4];
+          for (int e = 0; e < 4; ++e) {
+            const float a = v[s2 * 4 + e], z = v[(2 + s2) * 4 + e];
+            const float keep = csel ? z : a, send = csel ? a : z;
+            const float recv = __shfl_xor_sync(0xffffffffu, send, 2);
+            const float re = csel ? recv : keep, im = csel ? keep : recv;
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(re, im);
+            const float2 hf = __bfloat1622float2(h2);
+            const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+            hi[e] = *reinterpret_cast<const uint32_t*>(&h2);
+            lo[e] = *reinterpret_cast<const uint32_t*>(&l2);
+          }
+          const uint32_t off = offs[i * 2 + s2];
           if (off != 0xffffffffu) {
             // explicit shared-space stores (the aligned base pointer is generic)
-            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_hi + shift + off),
-                         "r"(*reinterpret_cast<const uint32_t*>(&h2))
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(sh_hi + shift + off), "r"(hi[0]),
+                         "r"(hi[1]), "r"(hi[2]), "r"(hi[3])
                          : "memory");
-            asm volatile("st.shared.b32 [%0], %1;" ::"r"(sh_lo + shift + off),
-                         "r"(*reinterpret_cast<const uint32_t*>(&l2))
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(sh_lo + shift + off), "r"(lo[0]),
+                         "r"(lo[1]), "r"(lo[2]), "r"(lo[3])
                          : "memory");
           }
         }
@@ -772,7 +794,8 @@ bool fused_eligible(const S3& s, int nvec, const TermGroups& tg) {
   const int64_t L = s.l0 * s.l1, K23 = s.k2 * s.k3;
   const int64_t NA = (int64_t)nvec * K23 * s.d, NB = (int64_t)nvec * L * s.d;
   return L <= 32 && 32 % L == 0 && K23 == L && NA % 16 == 0 && NA <= 256 && NB % 16 == 0 && NB <= 256 &&
-         (int)tg.i1.size() <= FU_MAXG && 4 * s.l2 * s.l3 <= 128 && (s.x0 * s.x1 * L) % 32 == 0;
+         (int)tg.i1.size() <= FU_MAXG && 4 * s.l2 * s.l3 <= 128 && (s.x0 * s.x1 * L) % 32 == 0 &&
+         L % 4 == 0 && 8 % s.d == 0;
 }
 
 }  // namespace
@@ -881,11 +904,20 @@ int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, con
   static std::once_flag once;
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
-    attr = cudaFuncSetAttribute(stage3_fused_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM_BIG);
+    for (auto k : {stage3_fused_kernel<1>, stage3_fused_kernel<2>, stage3_fused_kernel<4>, stage3_fused_kernel<8>}) {
+      const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM_BIG);
+      if (e != cudaSuccess) attr = e;
+    }
   });
   if (attr != cudaSuccess) return fail(CARC_CUDA_ERROR, "fused matvec: %s", cudaGetErrorString(attr));
   PhaseScope ph(PH_TC_STEP_A, stream);
-  stage3_fused_kernel<<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp);
+  switch (fp.d) {
+    case 1: stage3_fused_kernel<1><<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp); break;
+    case 2: stage3_fused_kernel<2><<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp); break;
+    case 4: stage3_fused_kernel<4><<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp); break;
+    case 8: stage3_fused_kernel<8><<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp); break;
+    default: return fail(CARC_BAD_ARG, "fused matvec: d = %d is not 1, 2, 4 or 8", fp.d);
+  }
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }

@@ -113,7 +113,9 @@ def test_stage3_tensorcore_matches_fp64(lib, D, c_ket, c_bra, nvec):
             assert err < 5e-5, err
 
 
-@pytest.mark.parametrize("D,c_ket,c_bra,nvec", [(2, 2, 2, 8), (4, 4, 4, 2), (4, 8, 4, 8)])
+# (2, 2, 2, 2) and (2, 2, 2, 6): step-A column counts 16 and 48, a partial
+# 32-column chunk in the fold
+@pytest.mark.parametrize("D,c_ket,c_bra,nvec", [(2, 2, 2, 8), (4, 4, 4, 2), (4, 8, 4, 8), (2, 2, 2, 2), (2, 2, 2, 6)])
 def test_fused_matvec_matches_unfused_and_fp64(lib, D, c_ket, c_bra, nvec):
     """The fused step-A/step-B kernel (W kept on chip) against the two-kernel
     path (forced through the autotune cache) and the FP64 path."""
