@@ -404,13 +404,14 @@ namespace {
 
 constexpr int FU_THREADS = 608;  // warps: 0 A loads, 1 MMA, 2..17 fold, 18 B loads
 constexpr int FU_MAXG = 8;
-constexpr int FU_STAGES = 3;
+constexpr int FU_STAGES = 4;
 constexpr int FU_STAGE_A = 128 * 128;        // A tile: 128 rows x 64 bf16
 constexpr int FU_STAGE_V = 256 * 128;        // Vin tile: up to 256 rows x 64 bf16
-constexpr int FU_STAGE = FU_STAGE_A + FU_STAGE_V;
 constexpr int FU_BB_ATOM = 256 * 128;        // B_B atom: up to 256 rows x 128 B
 constexpr int FU_AB_ATOM = 128 * 128;        // A_B atom: 128 rows x 128 B
-constexpr int FU_SMEM_BIG = 1024 + 2 * FU_STAGE + 2 * FU_BB_ATOM + 2 * FU_AB_ATOM + 256 * 8 + 32 * 8 + 512;
+constexpr int FU_SMEM_MAX = 227 * 1024;      // dynamic shared memory opt-in limit per CTA
+constexpr int FU_FIXED = 1024 + 2 * FU_BB_ATOM + 2 * FU_AB_ATOM + 256;  // alignment, B_B, A_B, barriers
+constexpr int FU_PF_PAIRS = 2;                // L2 prefetch distance of the S2_0 tiles, in pairs
 
 struct FusedMaps {
   CUtensorMap a[FU_MAXG];    // packed S2_0 tags of group g: rows (x0,x1,l0,l1, re/im, hi/lo), K (terms, k0 k1)
@@ -448,9 +449,10 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   uint8_t* stage = sm;                                   // stages x (A tile, Vin part)
   uint8_t* bB = sm + p.stages * p.stage_bytes;           // 2 atoms (hi, lo), rows of part h at h NBh
   uint8_t* aB = bB + 2 * FU_BB_ATOM;                     // 2 atoms (hi, lo)
-  int2* tabN = reinterpret_cast<int2*>(aB + 2 * FU_AB_ATOM);
+  // the fold's setup tables live in B_B until the fold warps have read them
+  int2* tabN = reinterpret_cast<int2*>(bB);
   int2* tabM = tabN + 256;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tabM + 32);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(aB + 2 * FU_AB_ATOM);
   uint64_t* full = bars;             // [FU_STAGES]
   uint64_t* empty = bars + 4;        // [FU_STAGES]
   uint64_t* accA_full = bars + 8;    // [2] per TMEM_A buffer
@@ -510,7 +512,27 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       int issued = 0, s = 0, t = (int)blockIdx.x / p.G, g = (int)blockIdx.x % p.G, part = 0;
       uint32_t ph = 0;
       bool ok = true;
+      // L2 prefetch of the S2_0 tiles FU_PF_PAIRS pairs ahead: (pt, pg) is
+      // pair pf; pairs 1 .. FU_PF_PAIRS - 1 are prefetched up front
+      int pf = 0, pt = t, pg = g;
+      auto next_pair = [&](int& tt, int& gg) {
+        tt += t_step;
+        if ((gg += g_step) >= p.G) {
+          gg -= p.G;
+          ++tt;
+        }
+      };
+      auto prefetch_pair = [&]() {
+        if (pf < my_pairs)
+          for (int kb = 0; kb < p.nkb[pg]; ++kb) tma_prefetch_2d(&maps.a[pg], kb * 64, pt * 128);
+        ++pf;
+        next_pair(pt, pg);
+      };
+      next_pair(pt, pg);
+      pf = 1;
+      for (int k = 1; k < FU_PF_PAIRS; ++k) prefetch_pair();
       for (int uc = 0; ok && uc < n_units; ++uc) {
+        if (part == 0) prefetch_pair();
         const int nkb = p.nkb[g];
         for (int kb = 0; kb < nkb; ++kb) {
           if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
@@ -555,6 +577,11 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         if ((g += g_step) >= p.G) {
           g -= p.G;
           ++t;
+        }
+        if (pc + 1 < my_pairs) {  // the next pair's slice into L2 while this one is used
+          const int64_t kn = (int64_t)t * p.XP * p.K23;
+          tma_prefetch_2d(&maps.b, (int)(g * p.regB + 2 * kn), 0);
+          tma_prefetch_2d(&maps.b, (int)(g * p.regB + 2 * p.kcB + 2 * kn), 0);
         }
       }
       if (*abort_flag && issued > 0)
@@ -688,6 +715,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         }
         offs[i * 2 + s2] = off;
       }
+    asm volatile("bar.sync 1, 512;" ::: "memory");  // tables read: B_B may be written
     // chunk column of element e of set S: (S / d) 4d + e d + S % d
     auto setcol = [](int S, int e) { return (S / DD) * 4 * DD + e * DD + S % DD; };
     bool ok = true;
@@ -893,9 +921,8 @@ int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, con
   fp.n_pairs = fp.x_tiles * G;
   fp.nbuf = 2 * fp.NAh <= 256 ? 2 : 1;
   fp.stage_bytes = FU_STAGE_A + fp.NAh * 128;
-  const int fixed = 1024 + 2 * FU_BB_ATOM + 2 * FU_AB_ATOM + 256 * 8 + 32 * 8 + 512;
-  fp.stages = fixed + FU_STAGES * fp.stage_bytes <= FU_SMEM_BIG ? FU_STAGES : 2;
-  const int smem = fixed + fp.stages * fp.stage_bytes;
+  fp.stages = std::min(FU_STAGES, (FU_SMEM_MAX - FU_FIXED) / fp.stage_bytes);
+  const int smem = FU_FIXED + fp.stages * fp.stage_bytes;
   fp.regB = g.regB;
   fp.kcB = g.kcB;
   fp.live_rows = (int)round_up(4 * s.l2 * s.l3, 32);
@@ -905,7 +932,7 @@ int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, con
   static cudaError_t attr = cudaSuccess;
   std::call_once(once, [] {
     for (auto k : {stage3_fused_kernel<1>, stage3_fused_kernel<2>, stage3_fused_kernel<4>, stage3_fused_kernel<8>}) {
-      const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM_BIG);
+      const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, FU_SMEM_MAX);
       if (e != cudaSuccess) attr = e;
     }
   });
