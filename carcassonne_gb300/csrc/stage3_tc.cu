@@ -339,34 +339,45 @@ struct VinTerms {
   int64_t pitch[kVinTermsPerLaunch];  // row pitch in bf16 pairs
 };
 
+// grid (blocks over one term's rows_out x reg4 slots, terms): 32-bit index
+// arithmetic (the host checks that a term's slot count fits)
 __global__ void pack_vin_kernel(const double2* __restrict__ x, uint32_t* __restrict__ out,
                                 const __grid_constant__ VinTerms p) {
-  const int64_t per_term = p.rows_out * p.reg4;
-  const int64_t total = (int64_t)p.n * per_term;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int term = (int)(t / per_term);
-    const int64_t rem = t % per_term;
-    const int64_t n = rem / p.reg4, slot = rem % p.reg4;
-    uint32_t* row = out + p.dst[term] + n * p.pitch[term];
-    if (slot >= p.kc) {  // padding columns [4 kc, reg)
+  const int term = blockIdx.y;
+  const int reg4 = (int)p.reg4, kc = (int)p.kc, k23 = (int)p.k23, d = (int)p.d;
+  const int per_term = (int)p.rows_out * reg4;
+  uint32_t* base = out + p.dst[term];
+  const double2* O = p.op[term];
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < per_term; t += gridDim.x * blockDim.x) {
+    const int n = t / reg4, slot = t - n * reg4;
+    uint32_t* row = base + (int64_t)n * p.pitch[term];
+    if (slot >= kc) {  // padding columns [4 kc, reg)
       row[2 * slot] = 0u;
       row[2 * slot + 1] = 0u;
       continue;
     }
     uint32_t hi = 0u, lo = 0u;
     if (n < p.rows_valid) {
-      const int64_t pp = n % p.d, q = n / p.d;
-      const int64_t k23 = q % p.k23, vec = q / p.k23;
-      const double2* xv = x + ((vec * p.kc + slot) * p.k23 + k23) * p.d;
-      double2 b;
-      const double2* O = p.op[term];
+      const int q = n / d, pp = n - q * d;
+      const int vec = q / k23, kk = q - vec * k23;
+      const double2* xv = x + (((int64_t)vec * kc + slot) * k23 + kk) * d;
+      // the operator application in FP32: its rounding (2^-24) is far below
+      // the hi + lo split that follows (2^-17)
+      float fr, fi;
       if (O == nullptr) {
-        b = xv[pp];
+        const double2 v = xv[pp];
+        fr = (float)v.x;
+        fi = (float)v.y;
       } else {
-        b = make_double2(0.0, 0.0);
-        for (int64_t qq = 0; qq < p.d; ++qq) b = cadd(b, cmul(O[pp * p.d + qq], xv[qq]));
+        fr = 0.f;
+        fi = 0.f;
+        for (int qq = 0; qq < d; ++qq) {
+          const double2 o = O[pp * d + qq], v = xv[qq];
+          const float orr = (float)o.x, oi = (float)o.y, vr = (float)v.x, vi = (float)v.y;
+          fr = fmaf(orr, vr, fmaf(-oi, vi, fr));
+          fi = fmaf(orr, vi, fmaf(oi, vr, fi));
+        }
       }
-      const float fr = (float)b.x, fi = (float)b.y;
       const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hm = __float2bfloat16_rn(fi);
       const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
       const __nv_bfloat16 lm = __float2bfloat16_rn(fi - __bfloat162float(hm));
@@ -375,7 +386,7 @@ __global__ void pack_vin_kernel(const double2* __restrict__ x, uint32_t* __restr
       lo = *reinterpret_cast<const uint32_t*>(&l2);
     }
     row[slot] = hi;
-    row[p.kc + slot] = lo;
+    row[kc + slot] = lo;
   }
 }
 
@@ -987,8 +998,11 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
     vt.d = s.d;
     auto flush = [&]() -> int {
       if (vt.n == 0) return CARC_OK;
-      pack_vin_kernel<<<grid_of((int64_t)vt.n * vt.rows_out * vt.reg4), 256, 0, stream>>>(
-          static_cast<const double2*>(x), reinterpret_cast<uint32_t*>(w.vin), vt);
+      const int64_t per_term = vt.rows_out * vt.reg4;
+      if (per_term >= (1ll << 31)) return fail(CARC_TOO_LARGE, "tensor-core matvec: Vin operand too large");
+      const dim3 grid((unsigned)std::min<int64_t>((per_term + 255) / 256, 1024), (unsigned)vt.n);
+      pack_vin_kernel<<<grid, 256, 0, stream>>>(static_cast<const double2*>(x), reinterpret_cast<uint32_t*>(w.vin),
+                                                 vt);
       CARC_CHECK_LAUNCH();
       vt.n = 0;
       return CARC_OK;

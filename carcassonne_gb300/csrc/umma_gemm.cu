@@ -509,18 +509,37 @@ struct ReduceParams {
   double2 alpha;
 };
 
+// Compensated FP32 accumulation (Knuth's TwoSum): s + c carries the running
+// sum of FP32 terms with an error of order n u^2 sum |x| (u = 2^-24), as
+// accurate as an FP64 sum of the same terms for n in the hundreds, without
+// FP64 arithmetic in the loop (FP64 issue rate is low on this part).
+// __fadd_rn keeps the compiler from reassociating or contracting the terms.
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    s = t;
+    c = __fadd_rn(c, err);
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 // C[m,n] (+)= alpha * sum_z sum_s (P[z][4m+s][n] + i P[z][4m+2+s][n])
 __global__ void reduce_kernel(const float* __restrict__ P, double2* __restrict__ C, const __grid_constant__ ReduceParams p) {
   const int64_t total = p.Mc * p.Nc;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t m = t / p.Nc, n = t % p.Nc;
-    double re = 0.0, im = 0.0;
+    Kahan re, im;
     for (int z = 0; z < p.ksplit; ++z) {
       const float* b = P + z * p.split_stride + (4 * m) * p.ld + n;
-      re += (double)b[0] + (double)b[p.ld];
-      im += (double)b[2 * p.ld] + (double)b[3 * p.ld];
+      re.add(b[0]);
+      re.add(b[p.ld]);
+      im.add(b[2 * p.ld]);
+      im.add(b[3 * p.ld]);
     }
-    double2 v = cmul(p.alpha, make_double2(re, im));
+    double2 v = cmul(p.alpha, make_double2(re.value(), im.value()));
     const int64_t off = pdecomp(m, p.nm, p.m_ext, p.m_str) + pdecomp(n, p.nn, p.n_ext, p.n_str);
     if (p.accumulate) v = cadd(v, C[off]);
     C[off] = v;
@@ -532,6 +551,10 @@ __global__ void reduce_kernel(const float* __restrict__ P, double2* __restrict__
 // consecutive n (lanes: coalesced 128-byte rows), its 8 warps take the planes
 // z = w, w+8, ... and the 8 partial sums are added in warp order.
 constexpr int RP_WARPS = 8;
+
+// Row-major planes P[z][r][n] (r = 4m + 2c + s): a block covers 32 columns of
+// one complex row m, its 8 warps take planes z = w, w+8, ...; the warps'
+// compensated partial sums are added in FP64 in warp order.
 __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const float* __restrict__ P,
                                                                        double2* __restrict__ C,
                                                                        const __grid_constant__ ReduceParams p) {
@@ -539,15 +562,29 @@ __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const floa
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t m = blockIdx.y;
   const int64_t n = (int64_t)blockIdx.x * 32 + lane;
-  double re = 0.0, im = 0.0;
+  Kahan re, im;
   if (n < p.Nc) {
-    for (int z = w; z < p.ksplit; z += RP_WARPS) {
-      const float* b = P + z * p.split_stride + (4 * m) * p.ld + n;
-      re += (double)b[0] + (double)b[p.ld];
-      im += (double)b[2 * p.ld] + (double)b[3 * p.ld];
+    // four planes (16 loads) in flight per thread before they are summed (in plane order)
+    const float* base = P + (4 * m) * p.ld + n;
+    for (int z0 = w; z0 < p.ksplit; z0 += 4 * RP_WARPS) {
+      float v[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int z = z0 + u * RP_WARPS;
+        const float* b = base + z * p.split_stride;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[u][q] = z < p.ksplit ? __ldcg(b + q * p.ld) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        re.add(v[u][0]);
+        re.add(v[u][1]);
+        im.add(v[u][2]);
+        im.add(v[u][3]);
+      }
     }
   }
-  part[w][lane] = make_double2(re, im);
+  part[w][lane] = make_double2(re.value(), im.value());
   __syncthreads();
   if (w == 0 && n < p.Nc) {
     double2 v = part[0][lane];
@@ -561,8 +598,9 @@ __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const floa
 
 // Column-major planes P[z][n][r] (r = 4m + 2c + s over `rows` rows): a block
 // covers one column n and 32 consecutive rows (8 complex m), its 8 warps take
-// planes z = w, w+8, ... (coalesced 128-byte loads), partial sums added in
-// warp order, then each quad of lanes folds its 4 rows into C[m, n].
+// planes z = w, w+8, ... (coalesced 128-byte loads) with compensated FP32
+// sums, the partials are added in FP64 in warp order, then each quad of lanes
+// folds its 4 rows into C[m, n].
 __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_cm_kernel(const float* __restrict__ P,
                                                                           double2* __restrict__ C, int64_t rows,
                                                                           const __grid_constant__ ReduceParams p) {
@@ -570,10 +608,23 @@ __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_cm_kernel(const f
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t n = blockIdx.x;
   const int64_t r = (int64_t)blockIdx.y * 32 + lane;
-  double acc = 0.0;
-  if (r < rows)
-    for (int z = w; z < p.ksplit; z += RP_WARPS) acc += (double)P[z * p.split_stride + n * rows + r];
-  part[w][lane] = acc;
+  Kahan acc;
+  if (r < rows) {
+    // up to 24 plane loads in flight per thread (one round trip for 192
+    // planes) before they are summed in plane order
+    const float* src = P + n * rows + r;
+    for (int z0 = w; z0 < p.ksplit; z0 += 24 * RP_WARPS) {
+      float v[24];
+#pragma unroll
+      for (int u = 0; u < 24; ++u) {
+        const int z = z0 + u * RP_WARPS;
+        v[u] = z < p.ksplit ? __ldcg(src + z * p.split_stride) : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 24; ++u) acc.add(v[u]);
+    }
+  }
+  part[w][lane] = acc.value();
   __syncthreads();
   if (w == 0) {
     double v = part[0][lane];
