@@ -339,55 +339,60 @@ struct VinTerms {
   int64_t pitch[kVinTermsPerLaunch];  // row pitch in bf16 pairs
 };
 
-// grid (blocks over one term's rows_out x reg4 slots, terms): 32-bit index
-// arithmetic (the host checks that a term's slot count fits)
+// One packed Vin slot: slot `t` of term `term` (row n = t / reg4, column
+// slot = t % reg4), the site operator applied to x and the result split into
+// (hi | lo) bf16 pairs.  32-bit index arithmetic (the host checks that a
+// term's slot count fits).
+__device__ __forceinline__ void pack_vin_slot(const double2* __restrict__ x, uint32_t* __restrict__ out,
+                                              const VinTerms& p, int term, int t) {
+  const int reg4 = (int)p.reg4, kc = (int)p.kc, k23 = (int)p.k23, d = (int)p.d;
+  const double2* O = p.op[term];
+  const int n = t / reg4, slot = t - n * reg4;
+  uint32_t* row = out + p.dst[term] + (int64_t)n * p.pitch[term];
+  if (slot >= kc) {  // padding columns [4 kc, reg)
+    row[2 * slot] = 0u;
+    row[2 * slot + 1] = 0u;
+    return;
+  }
+  uint32_t hi = 0u, lo = 0u;
+  if (n < p.rows_valid) {
+    const int q = n / d, pp = n - q * d;
+    const int vec = q / k23, kk = q - vec * k23;
+    const double2* xv = x + (((int64_t)vec * kc + slot) * k23 + kk) * d;
+    // the operator application in FP32: its rounding (2^-24) is far below
+    // the hi + lo split that follows (2^-17)
+    float fr, fi;
+    if (O == nullptr) {
+      const double2 v = xv[pp];
+      fr = (float)v.x;
+      fi = (float)v.y;
+    } else {
+      fr = 0.f;
+      fi = 0.f;
+      for (int qq = 0; qq < d; ++qq) {
+        const double2 o = O[pp * d + qq], v = xv[qq];
+        const float orr = (float)o.x, oi = (float)o.y, vr = (float)v.x, vi = (float)v.y;
+        fr = fmaf(orr, vr, fmaf(-oi, vi, fr));
+        fi = fmaf(orr, vi, fmaf(oi, vr, fi));
+      }
+    }
+    const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hm = __float2bfloat16_rn(fi);
+    const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
+    const __nv_bfloat16 lm = __float2bfloat16_rn(fi - __bfloat162float(hm));
+    const __nv_bfloat162 h2 = __halves2bfloat162(hr, hm), l2 = __halves2bfloat162(lr, lm);
+    hi = *reinterpret_cast<const uint32_t*>(&h2);
+    lo = *reinterpret_cast<const uint32_t*>(&l2);
+  }
+  row[slot] = hi;
+  row[kc + slot] = lo;
+}
+
+// grid (blocks over one term's rows_out x reg4 slots, terms)
 __global__ void pack_vin_kernel(const double2* __restrict__ x, uint32_t* __restrict__ out,
                                 const __grid_constant__ VinTerms p) {
-  const int term = blockIdx.y;
-  const int reg4 = (int)p.reg4, kc = (int)p.kc, k23 = (int)p.k23, d = (int)p.d;
-  const int per_term = (int)p.rows_out * reg4;
-  uint32_t* base = out + p.dst[term];
-  const double2* O = p.op[term];
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < per_term; t += gridDim.x * blockDim.x) {
-    const int n = t / reg4, slot = t - n * reg4;
-    uint32_t* row = base + (int64_t)n * p.pitch[term];
-    if (slot >= kc) {  // padding columns [4 kc, reg)
-      row[2 * slot] = 0u;
-      row[2 * slot + 1] = 0u;
-      continue;
-    }
-    uint32_t hi = 0u, lo = 0u;
-    if (n < p.rows_valid) {
-      const int q = n / d, pp = n - q * d;
-      const int vec = q / k23, kk = q - vec * k23;
-      const double2* xv = x + (((int64_t)vec * kc + slot) * k23 + kk) * d;
-      // the operator application in FP32: its rounding (2^-24) is far below
-      // the hi + lo split that follows (2^-17)
-      float fr, fi;
-      if (O == nullptr) {
-        const double2 v = xv[pp];
-        fr = (float)v.x;
-        fi = (float)v.y;
-      } else {
-        fr = 0.f;
-        fi = 0.f;
-        for (int qq = 0; qq < d; ++qq) {
-          const double2 o = O[pp * d + qq], v = xv[qq];
-          const float orr = (float)o.x, oi = (float)o.y, vr = (float)v.x, vi = (float)v.y;
-          fr = fmaf(orr, vr, fmaf(-oi, vi, fr));
-          fi = fmaf(orr, vi, fmaf(oi, vr, fi));
-        }
-      }
-      const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hm = __float2bfloat16_rn(fi);
-      const __nv_bfloat16 lr = __float2bfloat16_rn(fr - __bfloat162float(hr));
-      const __nv_bfloat16 lm = __float2bfloat16_rn(fi - __bfloat162float(hm));
-      const __nv_bfloat162 h2 = __halves2bfloat162(hr, hm), l2 = __halves2bfloat162(lr, lm);
-      hi = *reinterpret_cast<const uint32_t*>(&h2);
-      lo = *reinterpret_cast<const uint32_t*>(&l2);
-    }
-    row[slot] = hi;
-    row[kc + slot] = lo;
-  }
+  const int per_term = (int)(p.rows_out * p.reg4);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < per_term; t += gridDim.x * blockDim.x)
+    pack_vin_slot(x, out, p, (int)blockIdx.y, t);
 }
 
 }  // namespace
@@ -444,7 +449,57 @@ struct FusedParams {
   int live_rows;  // rows of TMEM_B that carry data (4 l2 l3, rounded to 32)
   float* planes;  // [grid][NB][live_rows], column-major per CTA
   int* err;
+  // single-launch mode (cooperative launch, all CTAs resident): the kernel
+  // also packs Vin before step A and reduces the planes into y after step B,
+  // the phases separated by grid-wide barriers on `sync` (zero at launch)
+  int coop;
+  VinTerms vt;
+  const double2* x;
+  uint32_t* vin;
+  double2* y;
+  int accumulate;
+  int nvec, l0, l1, l2, l3;
+  int64_t yv, yl0, yl1, yl2, yl3;
+  unsigned int* sync;
 };
+
+// Pair pr = blockIdx.x + pc * gridDim.x of a CTA, tag-major (g = pr / x_tiles,
+// t = pr % x_tiles), so that every CTA takes about the same share of each
+// S2_1 tag; advanced incrementally, without divisions.
+struct PairWalk {
+  int t, g, t_inc, g_inc, x_tiles;
+  __device__ PairWalk(int pr0, int step, int xt)
+      : t(pr0 % xt), g(pr0 / xt), t_inc(step % xt), g_inc(step / xt), x_tiles(xt) {}
+  __device__ void next() {
+    t += t_inc;
+    g += g_inc;
+    if (t >= x_tiles) {
+      t -= x_tiles;
+      ++g;
+    }
+  }
+};
+
+// Grid-wide barrier of a cooperative launch: every CTA adds one arrival, then
+// thread 0 polls (bounded) until all gridDim.x have arrived.  Release/acquire
+// at GPU scope order the phases' global-memory writes before the reads.
+__device__ bool grid_barrier(unsigned int* ctr, volatile int* abort) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    uint32_t i = 0;
+    for (; i < (1u << 22); ++i) {
+      unsigned int v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+      if (v >= gridDim.x) break;
+      __nanosleep(64);
+    }
+    if (i == (1u << 22)) *abort = 1;
+  }
+  __syncthreads();
+  return *abort == 0;
+}
 
 // Unit uc of a CTA (local counter) is part (uc % VH) of its pair (uc / VH);
 // the CTA takes pairs blockIdx.x, blockIdx.x + gridDim.x, ... so that both
@@ -476,8 +531,6 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int my_pairs = blockIdx.x < p.n_pairs ? (p.n_pairs - 1 - blockIdx.x) / gridDim.x + 1 : 0;
-  const int n_units = my_pairs * p.VH;
   if (threadIdx.x == 0) {
     for (int s = 0; s < FU_STAGES; ++s) {
       mbar_init(&full[s], 1);
@@ -509,9 +562,31 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   const uint32_t tmem = *tmem_slot;
   const uint32_t tB = tmem + 256;
 
-  // Per-CTA walk over pairs pr = blockIdx.x + pc * gridDim.x, t = pr / G,
-  // g = pr % G, advanced incrementally (no division in the loops).
-  const int t_step = (int)gridDim.x / p.G, g_step = (int)gridDim.x % p.G;
+  if (threadIdx.x == 0 && blockIdx.x < p.n_pairs) {
+    // the first pair's S2_0 tiles and S2_1 slice into L2 while Vin is packed
+    const PairWalk w0((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+    for (int kb = 0; kb < p.nkb[w0.g]; ++kb) tma_prefetch_2d(&maps.a[w0.g], kb * 64, w0.t * 128);
+    const int64_t k0 = (int64_t)w0.t * p.XP * p.K23;
+    tma_prefetch_2d(&maps.b, (int)(w0.g * p.regB + 2 * k0), 0);
+    tma_prefetch_2d(&maps.b, (int)(w0.g * p.regB + 2 * p.kcB + 2 * k0), 0);
+  }
+  if (p.coop) {
+    // ---- phase 0: Vin of every term packed by the whole grid; the async
+    // proxy (TMA) of every CTA reads it after the barrier
+    const int per_term = (int)(p.vt.rows_out * p.vt.reg4), total = per_term * p.vt.n;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+      const int term = e / per_term;
+      pack_vin_slot(p.x, p.vin, p.vt, term, e - term * per_term);
+    }
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    grid_barrier(p.sync, abort_flag);
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  // a CTA whose phase 0 failed takes no units (the status word reports it)
+  const int my_pairs =
+      (blockIdx.x < p.n_pairs && *abort_flag == 0) ? (p.n_pairs - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int n_units = my_pairs * p.VH;
+
   if (warp == 0) {
     if (lane == 0) {
       // ---- TMA producer of step A: the unit's S2_0 tile and its Vin part
@@ -520,31 +595,25 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         prefetch_tensormap(&maps.vin[q]);
       }
       prefetch_tensormap(&maps.b);
-      int issued = 0, s = 0, t = (int)blockIdx.x / p.G, g = (int)blockIdx.x % p.G, part = 0;
+      int issued = 0, s = 0, part = 0;
       uint32_t ph = 0;
       bool ok = true;
-      // L2 prefetch of the S2_0 tiles FU_PF_PAIRS pairs ahead: (pt, pg) is
-      // pair pf; pairs 1 .. FU_PF_PAIRS - 1 are prefetched up front
-      int pf = 0, pt = t, pg = g;
-      auto next_pair = [&](int& tt, int& gg) {
-        tt += t_step;
-        if ((gg += g_step) >= p.G) {
-          gg -= p.G;
-          ++tt;
-        }
-      };
+      PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+      // L2 prefetch of the S2_0 tiles FU_PF_PAIRS pairs ahead (pairs 1 ..
+      // FU_PF_PAIRS - 1 up front; pair 0 was prefetched before phase 0)
+      int pf = 1;
+      PairWalk pw = cw;
+      pw.next();
       auto prefetch_pair = [&]() {
         if (pf < my_pairs)
-          for (int kb = 0; kb < p.nkb[pg]; ++kb) tma_prefetch_2d(&maps.a[pg], kb * 64, pt * 128);
+          for (int kb = 0; kb < p.nkb[pw.g]; ++kb) tma_prefetch_2d(&maps.a[pw.g], kb * 64, pw.t * 128);
         ++pf;
-        next_pair(pt, pg);
+        pw.next();
       };
-      next_pair(pt, pg);
-      pf = 1;
       for (int k = 1; k < FU_PF_PAIRS; ++k) prefetch_pair();
       for (int uc = 0; ok && uc < n_units; ++uc) {
         if (part == 0) prefetch_pair();
-        const int nkb = p.nkb[g];
+        const int g = cw.g, t = cw.t, nkb = p.nkb[g];
         for (int kb = 0; kb < nkb; ++kb) {
           if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
           uint8_t* st = stage + s * p.stage_bytes;
@@ -559,11 +628,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         }
         if (++part == p.VH) {
           part = 0;
-          t += t_step;
-          if ((g += g_step) >= p.G) {
-            g -= p.G;
-            ++t;
-          }
+          cw.next();
         }
       }
       if (*abort_flag) {
@@ -576,23 +641,20 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   } else if (warp == 18) {
     if (lane == 0) {
       // ---- TMA producer of step B's S2_1 slice, one per pair
-      int issued = 0, t = (int)blockIdx.x / p.G, g = (int)blockIdx.x % p.G;
+      int issued = 0;
+      PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
       for (int pc = 0; pc < my_pairs; ++pc) {
         if (!mbar_wait_sleep(aB_empty, (uint32_t)((pc & 1) ^ 1), abort_flag)) break;
         mbar_arrive_expect_tx(aB_full, (uint32_t)(2 * p.a_rows * 128));
-        const int64_t kk0 = (int64_t)t * p.XP * p.K23;
-        tma_load_2d(aB, &maps.b, (int)(g * p.regB + 2 * kk0), 0, aB_full);
-        tma_load_2d(aB + FU_AB_ATOM, &maps.b, (int)(g * p.regB + 2 * p.kcB + 2 * kk0), 0, aB_full);
+        const int64_t kk0 = (int64_t)cw.t * p.XP * p.K23;
+        tma_load_2d(aB, &maps.b, (int)(cw.g * p.regB + 2 * kk0), 0, aB_full);
+        tma_load_2d(aB + FU_AB_ATOM, &maps.b, (int)(cw.g * p.regB + 2 * p.kcB + 2 * kk0), 0, aB_full);
         ++issued;
-        t += t_step;
-        if ((g += g_step) >= p.G) {
-          g -= p.G;
-          ++t;
-        }
+        cw.next();
         if (pc + 1 < my_pairs) {  // the next pair's slice into L2 while this one is used
-          const int64_t kn = (int64_t)t * p.XP * p.K23;
-          tma_prefetch_2d(&maps.b, (int)(g * p.regB + 2 * kn), 0);
-          tma_prefetch_2d(&maps.b, (int)(g * p.regB + 2 * p.kcB + 2 * kn), 0);
+          const int64_t kn = (int64_t)cw.t * p.XP * p.K23;
+          tma_prefetch_2d(&maps.b, (int)(cw.g * p.regB + 2 * kn), 0);
+          tma_prefetch_2d(&maps.b, (int)(cw.g * p.regB + 2 * p.kcB + 2 * kn), 0);
         }
       }
       if (*abort_flag && issued > 0)
@@ -647,7 +709,8 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       __syncwarp();
       return true;
     };
-    int s = 0, g = (int)blockIdx.x % p.G;
+    int s = 0;
+    PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
     uint32_t ph = 0;
     bool ok = true;
     Unit cur{0, 0, 0, 0u}, prev{0, 0, 0, 0u};
@@ -656,7 +719,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       // two buffers step_b(uc - 2) of the previous iteration waited for it
       if (p.nbuf == 1 && uc > 0 && !(ok = mbar_wait_sleep(&bB_ready[0], prev.bph, abort_flag))) break;
       const uint32_t tA = tmem + (uint32_t)(cur.b * p.NAh);
-      const int nkb = p.nkb[g];
+      const int nkb = p.nkb[cw.g];
       for (int kb = 0; kb < nkb; ++kb) {
         if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
         tc_fence_after();
@@ -679,7 +742,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       if (uc > 0 && !(ok = step_b(prev))) break;
       prev = cur;
       cur = advance(cur);
-      if (cur.part == 0 && (g += g_step) >= p.G) g -= p.G;
+      if (cur.part == 0) cw.next();
     }
     if (ok && n_units > 0) ok = step_b(prev);
     if (leader) mma_commit(doneB);
@@ -817,11 +880,58 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   }
   tc_fence_before();
   __syncthreads();
-  if (threadIdx.x == 0 && *abort_flag) atomicExch(p.err, CARC_NOT_CONVERGED);
   if (warp == 1) {
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
+  if (p.coop && grid_barrier(p.sync + 1, abort_flag) && warp >= 2 && warp <= 17) {
+    // ---- phase 2: the planes of all CTAs summed into y, the same arithmetic
+    // as reduce_planes_cm_kernel: a unit is (column n, 32 rows); two groups
+    // of 8 warps, warp w of a group takes planes w, w + 8, ... (compensated
+    // FP32), partials added in FP64 in warp order, quads fold their 4 rows
+    const int grp = (warp - 2) >> 3, wq = (warp - 2) & 7;
+    double* part = reinterpret_cast<double*>(stage) + grp * 256;
+    const int rgs = p.live_rows / 32, n_red = p.NB * rgs, L = p.live_rows;
+    const int64_t pstride = (int64_t)L * p.NB;
+    for (int ur = blockIdx.x * 2 + grp; ur < n_red; ur += 2 * gridDim.x) {
+      const int n = ur / rgs, r = (ur - n * rgs) * 32 + lane;
+      const float* src = p.planes + (int64_t)n * L + r;
+      Kahan acc;
+      for (int z0 = wq; z0 < (int)gridDim.x; z0 += 24 * 8) {
+        float v[24];
+#pragma unroll
+        for (int u = 0; u < 24; ++u) {
+          const int z = z0 + u * 8;
+          v[u] = z < (int)gridDim.x ? __ldcg(src + z * pstride) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 24; ++u) acc.add(v[u]);
+      }
+      part[wq * 32 + lane] = acc.value();
+      asm volatile("bar.sync %0, 256;" ::"r"(2 + grp) : "memory");
+      if (wq == 0) {
+        double v = part[lane];
+        for (int q = 1; q < 8; ++q) v += part[q * 32 + lane];
+        v += __shfl_xor_sync(0xffffffffu, v, 1);            // hi + lo
+        const double o = __shfl_xor_sync(0xffffffffu, v, 2);  // the other of re / im
+        const int m = r >> 2;
+        if ((lane & 3) == 0 && m < p.l2 * p.l3) {
+          int nn = n;
+          const int pi = nn % DD;
+          nn /= DD;
+          const int l1i = nn % p.l1;
+          nn /= p.l1;
+          const int l0i = nn % p.l0, vec = nn / p.l0;
+          const int64_t off = (m / p.l3) * p.yl2 + (m % p.l3) * p.yl3 + vec * p.yv + l0i * p.yl0 + l1i * p.yl1 + pi;
+          double2 val = make_double2(v, o);
+          if (p.accumulate) val = cadd(val, p.y[off]);
+          p.y[off] = val;
+        }
+      }
+      asm volatile("bar.sync %0, 256;" ::"r"(2 + grp) : "memory");
+    }
+  }
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(p.err, CARC_NOT_CONVERGED);
 }
 
 int fused_grid(const S3& s, const TermGroups& tg) {
@@ -897,8 +1007,14 @@ int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, co
   return CARC_OK;
 }
 
+// With vt (single-launch mode) the kernel is launched cooperatively and also
+// packs Vin and reduces into y; *coop_done tells whether that launch was
+// accepted (when not, nothing was enqueued but a memset and the caller runs
+// the three-kernel sequence).
 int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, const Geo& g, const void* plan,
-                 const MvWs& w, int* status, cudaStream_t stream) {
+                 const MvWs& w, const VinTerms* vt, const void* x, void* y, int accumulate, bool* coop_done,
+                 int* status, cudaStream_t stream) {
+  if (coop_done) *coop_done = false;
   const int G = (int)tg.i1.size();
   FusedMaps maps;
   memset(&maps, 0, sizeof(maps));
@@ -949,6 +1065,52 @@ int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, con
   });
   if (attr != cudaSuccess) return fail(CARC_CUDA_ERROR, "fused matvec: %s", cudaGetErrorString(attr));
   PhaseScope ph(PH_TC_STEP_A, stream);
+  if (vt) {
+    if (fp.d != 1 && fp.d != 2 && fp.d != 4 && fp.d != 8) return CARC_OK;
+    fp.coop = 1;
+    fp.vt = *vt;
+    fp.x = static_cast<const double2*>(x);
+    fp.vin = reinterpret_cast<uint32_t*>(w.vin);
+    fp.y = static_cast<double2*>(y);
+    fp.accumulate = accumulate;
+    fp.nvec = nvec;
+    fp.l0 = (int)s.l0;
+    fp.l1 = (int)s.l1;
+    fp.l2 = (int)s.l2;
+    fp.l3 = (int)s.l3;
+    fp.yl3 = s.d;
+    fp.yl2 = s.l3 * fp.yl3;
+    fp.yl1 = s.l2 * fp.yl2;
+    fp.yl0 = s.l1 * fp.yl1;
+    fp.yv = s.l0 * fp.yl0;
+    fp.sync = reinterpret_cast<unsigned int*>(w.red);
+    CARC_CHECK_CUDA(cudaMemsetAsync(w.red, 0, 16, stream));
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)w.ksB);
+    cfg.blockDim = dim3(FU_THREADS);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute la[1];
+    la[0].id = cudaLaunchAttributeCooperative;
+    la[0].val.cooperative = 1;
+    cfg.attrs = la;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (fp.d) {
+      case 1: e = cudaLaunchKernelEx(&cfg, stage3_fused_kernel<1>, maps, fp); break;
+      case 2: e = cudaLaunchKernelEx(&cfg, stage3_fused_kernel<2>, maps, fp); break;
+      case 4: e = cudaLaunchKernelEx(&cfg, stage3_fused_kernel<4>, maps, fp); break;
+      case 8: e = cudaLaunchKernelEx(&cfg, stage3_fused_kernel<8>, maps, fp); break;
+    }
+    if (e == cudaSuccess) {
+      ::carc::count_launch();
+      *coop_done = true;
+      return CARC_OK;
+    }
+    (void)cudaGetLastError();  // not co-resident here: the caller runs the three kernels
+    return CARC_OK;
+  }
   switch (fp.d) {
     case 1: stage3_fused_kernel<1><<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp); break;
     case 2: stage3_fused_kernel<2><<<w.ksB, FU_THREADS, smem, stream>>>(maps, fp); break;
@@ -985,9 +1147,9 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
   MvWs w;
   mv_layout(s, s0_shape, s1_shape, nvec, tg, &w, ws);
   const int G = (int)tg.i1.size();
-  // Vin of every term, operator applied and packed, in launches of up to 64 terms
+  // Vin of every term, operator applied and packed: up to 64 terms per launch
+  std::vector<VinTerms> chunks;
   {
-    PhaseScope ph(PH_TC_PACK, stream);
     VinTerms vt;
     memset(&vt, 0, sizeof(vt));
     vt.rows_out = g.rowsA_b;
@@ -996,17 +1158,8 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
     vt.reg4 = g.regA / 4;
     vt.k23 = s.k2 * s.k3;
     vt.d = s.d;
-    auto flush = [&]() -> int {
-      if (vt.n == 0) return CARC_OK;
-      const int64_t per_term = vt.rows_out * vt.reg4;
-      if (per_term >= (1ll << 31)) return fail(CARC_TOO_LARGE, "tensor-core matvec: Vin operand too large");
-      const dim3 grid((unsigned)std::min<int64_t>((per_term + 255) / 256, 1024), (unsigned)vt.n);
-      pack_vin_kernel<<<grid, 256, 0, stream>>>(static_cast<const double2*>(x), reinterpret_cast<uint32_t*>(w.vin),
-                                                 vt);
-      CARC_CHECK_LAUNCH();
-      vt.n = 0;
-      return CARC_OK;
-    };
+    if (vt.rows_out * vt.reg4 * kVinTermsPerLaunch >= (1ll << 31))
+      return fail(CARC_TOO_LARGE, "tensor-core matvec: Vin operand too large");
     for (int q = 0; q < G; ++q) {
       const int nt = (int)tg.terms[q].size();
       for (int j = 0; j < nt; ++j) {
@@ -1014,15 +1167,34 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
         vt.op[vt.n] = io < 0 ? nullptr : static_cast<const double2*>(op_ptrs[io]);
         vt.dst[vt.n] = w.vin_off[q] / 4 + (int64_t)j * g.regA / 2;
         vt.pitch[vt.n] = g.regA * nt / 2;
-        if (++vt.n == kVinTermsPerLaunch) CARC_RETURN_IF(flush());
+        if (++vt.n == kVinTermsPerLaunch) {
+          chunks.push_back(vt);
+          vt.n = 0;
+        }
       }
     }
-    CARC_RETURN_IF(flush());
+    if (vt.n > 0) chunks.push_back(vt);
+  }
+  // the fused kernel as one cooperative launch (pack, step A + B, reduce)
+  if (w.fused && chunks.size() == 1) {
+    bool done = false;
+    CARC_RETURN_IF(launch_fused(s, nvec, tg, g1, g, plan, w, &chunks[0], x, y, accumulate, &done, status, stream));
+    if (done) return CARC_OK;
+  }
+  {
+    PhaseScope ph(PH_TC_PACK, stream);
+    for (const VinTerms& vt : chunks) {
+      const int64_t per_term = vt.rows_out * vt.reg4;
+      const dim3 grid((unsigned)std::min<int64_t>((per_term + 255) / 256, 1024), (unsigned)vt.n);
+      pack_vin_kernel<<<grid, 256, 0, stream>>>(static_cast<const double2*>(x), reinterpret_cast<uint32_t*>(w.vin),
+                                                 vt);
+      CARC_CHECK_LAUNCH();
+    }
   }
   const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
   int64_t plane_ld, plane_stride;
   if (w.fused) {
-    CARC_RETURN_IF(launch_fused(s, nvec, tg, g1, g, plan, w, status, stream));
+    CARC_RETURN_IF(launch_fused(s, nvec, tg, g1, g, plan, w, nullptr, nullptr, nullptr, 0, nullptr, status, stream));
     plane_ld = rows_valid_w;
     plane_stride = round_up(4 * s.l2 * s.l3, 32) * rows_valid_w;
   } else {

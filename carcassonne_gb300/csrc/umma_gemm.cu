@@ -509,23 +509,6 @@ struct ReduceParams {
   double2 alpha;
 };
 
-// Compensated FP32 accumulation (Knuth's TwoSum): s + c carries the running
-// sum of FP32 terms with an error of order n u^2 sum |x| (u = 2^-24), as
-// accurate as an FP64 sum of the same terms for n in the hundreds, without
-// FP64 arithmetic in the loop (FP64 issue rate is low on this part).
-// __fadd_rn keeps the compiler from reassociating or contracting the terms.
-struct Kahan {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float x) {
-    const float t = __fadd_rn(s, x);
-    const float bp = __fsub_rn(t, s);
-    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
-    s = t;
-    c = __fadd_rn(c, err);
-  }
-  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
-};
-
 // C[m,n] (+)= alpha * sum_z sum_s (P[z][4m+s][n] + i P[z][4m+2+s][n])
 __global__ void reduce_kernel(const float* __restrict__ P, double2* __restrict__ C, const __grid_constant__ ReduceParams p) {
   const int64_t total = p.Mc * p.Nc;
