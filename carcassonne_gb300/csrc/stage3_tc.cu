@@ -538,7 +538,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&accA_full[b], 1);
-      mbar_init(&bB_ready[b], 16);
+      mbar_init(&bB_ready[b], (p.VH == 2 && p.nbuf == 2) ? 8 : 16);  // the fold warps of the buffer's team
       mbar_init(&bB_free[b], 1);
     }
     mbar_init(aB_full, 1);
@@ -748,8 +748,13 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     if (leader) mma_commit(doneB);
     __syncwarp();
   } else if (warp >= 2 && warp <= 17) {
-    // ---- fold epilogue: warps 2..17; quadrant = warp % 4, column quarter = (warp - 2) / 4
+    // ---- fold epilogue: warps 2..17; quadrant = warp % 4.  With two vector
+    // parts and two TMEM_A buffers the warps form two teams of 8 (team =
+    // part = buffer) that fold alternate units concurrently; otherwise one
+    // team of 16.  A warp takes the 32-column chunks cgi, cgi + ncg, ...
     const int quad = warp & 3, quarter = (warp - 2) >> 2;
+    const int nteams = (p.VH == 2 && p.nbuf == 2) ? 2 : 1, ncg = 4 / nteams;
+    const int team = nteams == 2 ? (quarter & 1) : 0, cgi = nteams == 2 ? (quarter >> 1) : quarter;
     const int et = threadIdx.x - 64;  // 0..511
     // tables over the columns of part 0 (part h shifts the B_B rows by h NBh):
     // per step-A column n = (vec, k23, p): {B_B row part, k part}; per tile row m = (xp, l)
@@ -771,7 +776,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     // 4h + 2c + s2, s2 = 0, 1.  Set S holds chunk columns (S / d) 4d + e d + S % d.
     const int hsel = lane & 1, csel = (lane >> 1) & 1;
     const int nchunks = (p.NAh + 31) / 32;
-    const int nch = (nchunks - quarter + 3) / 4;  // chunks quarter, quarter + 4
+    const int nch = (nchunks - cgi + ncg - 1) / ncg;  // at most 2 (NAh <= 128 with two teams)
     // This lane's B_B byte offsets are the same in every unit (plus the part's
     // row shift): computed once, so no shared-memory load sits between stores.
     uint32_t offs[4];
@@ -780,7 +785,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
 #pragma unroll
       for (int s2 = 0; s2 < 2; ++s2) {
         const int S = 4 * hsel + 2 * csel + s2;
-        const int col = (quarter + 4 * i) * 32 + (S / DD) * 4 * DD + S % DD;
+        const int col = (cgi + ncg * i) * 32 + (S / DD) * 4 * DD + S % DD;
         uint32_t off = 0xffffffffu;
         if (i < nch && col < p.NAh) {
           const int2 tn = tabN[col];
@@ -795,7 +800,18 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     bool ok = true;
     int b = 0, part = 0, pc = 0;
     uint32_t bph = 0;
-    for (int uc = 0; uc < n_units; ++uc) {
+    auto step_unit = [&]() {
+      if (++b == p.nbuf) {
+        b = 0;
+        bph ^= 1u;
+      }
+      if (++part == p.VH) {
+        part = 0;
+        ++pc;
+      }
+    };
+    if (team == 1) step_unit();
+    for (int uc = team; uc < n_units; uc += nteams) {
       if (!(ok = mbar_wait_sleep(&accA_full[b], bph, abort_flag))) break;
       // B_B part `part` was last read by the MMA-B of unit uc - VH (pair pc - 1)
       if (pc > 0 && !(ok = mbar_wait_sleep(&bB_free[part], (uint32_t)((pc & 1) ^ 1), abort_flag))) break;
@@ -807,7 +823,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       for (int i = 0; i < 2; ++i) {
         if (i >= nch) break;
         uint32_t r[32];
-        tmem_ld_32x32b_x32(tA + lanes + (uint32_t)((quarter + 4 * i) * 32), r);
+        tmem_ld_32x32b_x32(tA + lanes + (uint32_t)((cgi + ncg * i) * 32), r);
         tmem_ld_wait();
         // stage 1 (lane ^ 1): sum the hi/lo rows; lane h keeps sets 4h..4h+3
         float v[16];
@@ -850,14 +866,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&bB_ready[b]);
-      if (++b == p.nbuf) {
-        b = 0;
-        bph ^= 1u;
-      }
-      if (++part == p.VH) {
-        part = 0;
-        ++pc;
-      }
+      for (int k = 0; k < nteams; ++k) step_unit();
     }
     // ---- TMEM_B -> this CTA's split-K plane (zeros when the CTA had no unit)
     const bool done = ok && mbar_wait_sleep(doneB, 0, abort_flag);
