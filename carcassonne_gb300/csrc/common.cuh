@@ -36,7 +36,11 @@ void count_launch();
 // Optional per-phase device timing: when enabled (carc_phase_timing_enable),
 // a PhaseScope records a CUDA event pair on the launching stream around the
 // launches of one phase; carc_phase_timing_read sums the elapsed times.
-enum Phase { PH_TC_PACK = 0, PH_TC_STEP_A = 1, PH_TC_STEP_B = 2, PH_TC_REDUCE = 3, PH_COUNT = 8 };
+enum Phase {
+  PH_TC_PACK = 0, PH_TC_STEP_A = 1, PH_TC_STEP_B = 2, PH_TC_REDUCE = 3,  // tensor-core matvec
+  PH_HEGV_POTRF = 4, PH_HEGV_TRTRI = 5, PH_HEGV_REDUCE = 6, PH_HEGV_LANCZOS = 7,  // hegv_lowest
+  PH_COUNT = 8
+};
 bool phase_timing_on();
 void phase_record(int phase, cudaStream_t stream, bool start);
 

@@ -338,6 +338,150 @@ __global__ void perturb_start_kernel(int n, double2* __restrict__ u, double eps)
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// Lanczos iterations j0 .. j1-1 as one cooperative launch.  CTA c owns rows
+// [c rpc, (c+1) rpc) of every vector: it forms its rows of w = C q_j (a warp
+// per row), and every inner product is a fixed-order two-level sum (per-CTA
+// partials, then one CTA per coefficient, or every CTA for a scalar)
+// between bounded grid-wide barriers: 7 barriers per iteration (alpha, two
+// reorthogonalisation passes of two, beta, q_{j+1} published) instead of
+// about ten kernel launches.
+// ---------------------------------------------------------------------------
+constexpr int LZ_THREADS = 256;
+
+struct LzParams {
+  int n, j0, j1, rpc;
+  const double2* C;
+  double2* Q;       // (mk + 1) x n Krylov basis
+  double* alpha;
+  double* beta;
+  double2* pscal;   // [G] per-CTA partial of a scalar inner product
+  double2* part;    // [(mk + 1) x G] per-CTA partials of the projections
+  double2* h;       // (mk + 1) projections
+  double scale_ref;
+  int* breakdown;
+  unsigned int* sync;  // barrier arrivals (zero at launch)
+  int* abort;          // set by a CTA whose barrier wait ran out (zero at launch)
+};
+
+__device__ bool lz_grid_sync(unsigned int* ctr, unsigned int target, int* abort) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    int good = 0;
+    for (uint32_t i = 0; i < (1u << 22); ++i) {
+      unsigned int v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+      if (v >= target) {
+        good = 1;
+        break;
+      }
+      if ((i & 255u) == 255u && *reinterpret_cast<volatile int*>(abort)) break;
+      __nanosleep(32);
+    }
+    if (!good) atomicExch(abort, 1);
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+__global__ __launch_bounds__(LZ_THREADS) void lanczos_chunk_kernel(const __grid_constant__ LzParams p) {
+  extern __shared__ double2 lz_w[];  // this CTA's rows of w
+  __shared__ double s_alpha, s_bprev, s_beta;
+  const int G = (int)gridDim.x, c = (int)blockIdx.x, n = p.n;
+  const int r0 = c * p.rpc, r1 = min(n, r0 + p.rpc), nr = max(0, r1 - r0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  unsigned int bar = 0;
+  auto gsync = [&]() { return lz_grid_sync(p.sync, ++bar * (unsigned)G, p.abort); };
+  for (int j = p.j0; j < p.j1; ++j) {
+    const double2* qj = p.Q + (int64_t)j * n;
+    // w = C q_j on this CTA's rows (the four-chain row dot of gemv_kernel)
+    for (int rl = warp; rl < nr; rl += nw) {
+      const double2* a = p.C + (int64_t)(r0 + rl) * n;
+      double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+      int k = lane;
+      for (; k + 96 < n; k += 128) {
+        cfma(s0, a[k], qj[k]);
+        cfma(s1, a[k + 32], qj[k + 32]);
+        cfma(s2, a[k + 64], qj[k + 64]);
+        cfma(s3, a[k + 96], qj[k + 96]);
+      }
+      for (; k < n; k += 32) cfma(s0, a[k], qj[k]);
+      double2 sum = warp_sum2(cadd(cadd(s0, s1), cadd(s2, s3)));
+      if (lane == 0) lz_w[rl] = sum;
+    }
+    __syncthreads();
+    // alpha_j = Re(q_j^H w)
+    if (threadIdx.x == 0) {
+      double2 acc = make_double2(0.0, 0.0);
+      for (int rl = 0; rl < nr; ++rl) acc = cadd(acc, cmulc(qj[r0 + rl], lz_w[rl]));
+      p.pscal[c] = acc;
+    }
+    if (!gsync()) return;
+    if (threadIdx.x == 0) {
+      double a = 0.0;
+      for (int q = 0; q < G; ++q) a += p.pscal[q].x;
+      s_alpha = a;
+      s_bprev = j > 0 ? p.beta[j - 1] : 0.0;
+    }
+    __syncthreads();
+    for (int rl = threadIdx.x; rl < nr; rl += blockDim.x) {
+      double2 v = csub(lz_w[rl], cscale(qj[r0 + rl], s_alpha));
+      if (j > 0) v = csub(v, cscale(p.Q[(int64_t)(j - 1) * n + r0 + rl], s_bprev));
+      lz_w[rl] = v;
+    }
+    __syncthreads();
+    // two classical Gram-Schmidt passes against q_0 .. q_j
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int i = threadIdx.x; i <= j; i += blockDim.x) {
+        double2 acc = make_double2(0.0, 0.0);
+        const double2* qi = p.Q + (int64_t)i * n + r0;
+        for (int rl = 0; rl < nr; ++rl) acc = cadd(acc, cmulc(qi[rl], lz_w[rl]));
+        p.part[(int64_t)i * G + c] = acc;
+      }
+      if (!gsync()) return;
+      for (int i = c + (int)threadIdx.x * G; i <= j; i += (int)blockDim.x * G) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int q = 0; q < G; ++q) acc = cadd(acc, p.part[(int64_t)i * G + q]);
+        p.h[i] = acc;
+      }
+      if (!gsync()) return;
+      for (int rl = warp; rl < nr; rl += nw) {
+        double2 acc = make_double2(0.0, 0.0);
+        for (int i = lane; i <= j; i += 32) cfma(acc, p.h[i], p.Q[(int64_t)i * n + r0 + rl]);
+        acc = warp_sum2(acc);
+        if (lane == 0) lz_w[rl] = csub(lz_w[rl], acc);
+      }
+      __syncthreads();
+    }
+    // beta_j = ||w||, q_{j+1} = w / beta_j
+    if (threadIdx.x == 0) {
+      double acc = 0.0;
+      for (int rl = 0; rl < nr; ++rl) acc += cabs2(lz_w[rl]);
+      p.pscal[c] = make_double2(acc, 0.0);
+    }
+    if (!gsync()) return;
+    if (threadIdx.x == 0) {
+      double b2 = 0.0;
+      for (int q = 0; q < G; ++q) b2 += p.pscal[q].x;
+      s_beta = sqrt(fmax(b2, 0.0));
+      if (c == 0) {
+        p.alpha[j] = s_alpha;
+        p.beta[j] = s_beta;
+        if (s_beta <= 1e-13 * p.scale_ref) *p.breakdown = 1;
+      }
+    }
+    __syncthreads();
+    const double inv = s_beta > 0 ? 1.0 / s_beta : 0.0;
+    for (int rl = threadIdx.x; rl < nr; rl += blockDim.x) p.Q[(int64_t)(j + 1) * n + r0 + rl] = cscale(lz_w[rl], inv);
+    if (j + 1 < p.j1 && !gsync()) return;  // q_{j+1} complete before the next product
+  }
+}
+
 inline int comb_blocks(int n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, COMB_I), 4 * 152)); }
 
 inline int blocks_for(int64_t n, int threads = 256) {
@@ -357,7 +501,12 @@ struct LanczosWs {
   int* breakdown;
   void* dot_ws;
   int64_t dot_ws_bytes;
+  double2* pscal;     // cooperative path: [LZ_MAX_CTAS]
+  double2* part;      // [(mk + 1) x LZ_MAX_CTAS]
+  unsigned int* sync; // [0] barrier arrivals, [1] abort flag
 };
+
+constexpr int LZ_MAX_CTAS = 152;
 
 int64_t lanczos_ws_layout(int n, int mk, LanczosWs* L, void* base) {
   char* p = static_cast<char*>(base);
@@ -380,6 +529,9 @@ int64_t lanczos_ws_layout(int n, int mk, LanczosWs* L, void* base) {
   t.breakdown = (int*)take(16);
   t.dot_ws_bytes = dot_workspace_size(n);
   t.dot_ws = take(t.dot_ws_bytes);
+  t.pscal = (double2*)take((int64_t)LZ_MAX_CTAS * 16);
+  t.part = (double2*)take((int64_t)(mk + 1) * LZ_MAX_CTAS * 16);
+  t.sync = (unsigned int*)take(16);
   if (L) *L = t;
   return off;
 }
@@ -401,6 +553,16 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
   const double2* C = static_cast<const double2*>(Cv);
   const int gb = blocks_for((int64_t)n * 32);
   const int eb = blocks_for(n);
+  // cooperative chunks: about 8 rows per CTA (a warp per row), at most one CTA per SM
+  static int sm_count = 0;
+  if (sm_count == 0) {
+    int dev = 0;
+    CARC_CHECK_CUDA(cudaGetDevice(&dev));
+    CARC_CHECK_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int lz_ctas = (int)std::max<int64_t>(1, std::min<int64_t>({ceil_div(n, 8), (int64_t)sm_count, LZ_MAX_CTAS}));
+  const int lz_rpc = (int)ceil_div(n, lz_ctas);
+  bool coop = true;
   // start vector
   CARC_CHECK_CUDA(cudaMemcpyAsync(W.Q, u0, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
   CARC_RETURN_IF(dot_launch(n, W.Q, W.Q, 1, W.nrm, W.dot_ws, W.dot_ws_bytes, stream));
@@ -425,6 +587,67 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
       scale_ref = std::max(sqrt(std::max(hn.x, 0.0)), 1e-300);
     }
     for (int j = 0; j < mk; ++j) {
+      if (coop && j % 8 == 0) {
+        // iterations j .. j1-1 in one cooperative launch (per-iteration kernels below otherwise)
+        const int j1 = std::min(mk, j + 8);
+        LzParams lp;
+        lp.n = n;
+        lp.j0 = j;
+        lp.j1 = j1;
+        lp.rpc = lz_rpc;
+        lp.C = C;
+        lp.Q = W.Q;
+        lp.alpha = W.alpha;
+        lp.beta = W.beta;
+        lp.pscal = W.pscal;
+        lp.part = W.part;
+        lp.h = W.h;
+        lp.scale_ref = scale_ref;
+        lp.breakdown = W.breakdown;
+        lp.sync = W.sync;
+        lp.abort = reinterpret_cast<int*>(W.sync + 1);
+        CARC_CHECK_CUDA(cudaMemsetAsync(W.sync, 0, 8, stream));
+        cudaLaunchConfig_t cfg;
+        memset(&cfg, 0, sizeof(cfg));
+        cfg.gridDim = dim3((unsigned)lz_ctas);
+        cfg.blockDim = dim3(LZ_THREADS);
+        cfg.dynamicSmemBytes = (size_t)lz_rpc * 16;
+        cfg.stream = stream;
+        cudaLaunchAttribute la[1];
+        la[0].id = cudaLaunchAttributeCooperative;
+        la[0].val.cooperative = 1;
+        cfg.attrs = la;
+        cfg.numAttrs = 1;
+        if (cudaLaunchKernelEx(&cfg, lanczos_chunk_kernel, lp) == cudaSuccess) {
+          count_launch();
+          total += j1 - j - 1;
+          j = j1 - 1;
+          m = j1;
+          ++total;
+          const bool last = (j + 1 == mk);
+          if ((m % 8) == 0 || last || m == n) {
+            tridiag_lowest_kernel<<<1, TRI_THREADS, 0, stream>>>(m, W.alpha, W.beta, W.tri_out, W.s);
+            CARC_CHECK_LAUNCH();
+            double hv[3];
+            int bd[3] = {0, 0, 0};
+            CARC_CHECK_CUDA(cudaMemcpyAsync(hv, W.tri_out, 24, cudaMemcpyDeviceToHost, stream));
+            CARC_CHECK_CUDA(cudaMemcpyAsync(&bd[0], W.breakdown, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            CARC_CHECK_CUDA(cudaMemcpyAsync(&bd[1], W.sync + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+            CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+            if (bd[1]) return fail(CARC_NOT_CONVERGED, "lanczos: a grid barrier wait timed out");
+            lam = hv[0];
+            res = hv[1];
+            lam2 = hv[2];
+            if (bd[0] || res <= tol * std::max(fabs(lam), 1e-300) || m == n) {
+              converged = true;
+              break;
+            }
+          }
+          continue;
+        }
+        (void)cudaGetLastError();  // not co-resident here: per-iteration kernels from now on
+        coop = false;
+      }
       double2* qj = W.Q + (int64_t)j * n;
       double2* qn = W.Q + (int64_t)(j + 1) * n;
       gemv_kernel<<<gb, 256, 0, stream>>>(n, C, qj, W.w);
@@ -548,33 +771,42 @@ int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, d
   void* sub = p + 4 * mat + 2 * a256((int64_t)n * 16) + a256(64);
   int64_t sub_bytes = ws_bytes - (4 * mat + 2 * a256((int64_t)n * 16) + a256(64));
 
-  CARC_CHECK_CUDA(cudaMemcpyAsync(Lm, Nm, (int64_t)n * n * 16, cudaMemcpyDeviceToDevice, stream));
-  CARC_RETURN_IF(potrf(n, Lm, status, sub, sub_bytes, stream));
+  {
+    PhaseScope ph(PH_HEGV_POTRF, stream);
+    CARC_CHECK_CUDA(cudaMemcpyAsync(Lm, Nm, (int64_t)n * n * 16, cudaMemcpyDeviceToDevice, stream));
+    CARC_RETURN_IF(potrf(n, Lm, status, sub, sub_bytes, stream));
+  }
   int hstat = 0;
   CARC_CHECK_CUDA(cudaMemcpyAsync(&hstat, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
   CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
   if (hstat != CARC_OK) return fail(CARC_NOT_POSDEF, "hegv: the normalization matrix is not positive definite");
-  CARC_RETURN_IF(trtri_lower(n, Lm, Li, sub, sub_bytes, stream));
+  {
+    PhaseScope ph(PH_HEGV_TRTRI, stream);
+    CARC_RETURN_IF(trtri_lower(n, Lm, Li, sub, sub_bytes, stream));
+  }
   // T1 = Linv H ; C = T1 Linv^H
-  if (flags & CARC_HEGV_TENSOR_CORE) {
-    // T1[m][n] = sum_k Li[m][k] H[k][n];  C[m][n] = sum_k T1[m][k] conj(Li[n][k])
-    CARC_RETURN_IF(zgemm_tc(hegv_view(Li, n, n, 1, 0), hegv_view(H, n, 1, n, 0), hegv_out(T1, n), make_double2(1, 0),
-                            0, HEGV_TC_KSPLIT, sub, sub_bytes, status, stream));
-    CARC_RETURN_IF(zgemm_tc(hegv_view(T1, n, n, 1, 0), hegv_view(Li, n, n, 1, 1), hegv_out(Cm, n),
-                            make_double2(1, 0), 0, HEGV_TC_KSPLIT, sub, sub_bytes, status, stream));
-  } else {
-    carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
-    const void* pa[1] = {Li};
-    const void* pb[1] = {H};
-    void* pc[1] = {T1};
-    int32_t e[3] = {0, 0, 0};
-    CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
-    carc_contract_desc d2 = DescBuilder().m(n, n, n).n(n, n, 1).k(n, 1, 1).d;
-    d2.conj_b = 1;
-    const void* pa2[1] = {T1};
-    const void* pb2[1] = {Li};
-    void* pc2[1] = {Cm};
-    CARC_RETURN_IF(gett_launch(d2, pa2, 1, pb2, 1, pc2, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+  {
+    PhaseScope ph(PH_HEGV_REDUCE, stream);
+    if (flags & CARC_HEGV_TENSOR_CORE) {
+      // T1[m][n] = sum_k Li[m][k] H[k][n];  C[m][n] = sum_k T1[m][k] conj(Li[n][k])
+      CARC_RETURN_IF(zgemm_tc(hegv_view(Li, n, n, 1, 0), hegv_view(H, n, 1, n, 0), hegv_out(T1, n), make_double2(1, 0),
+                              0, HEGV_TC_KSPLIT, sub, sub_bytes, status, stream));
+      CARC_RETURN_IF(zgemm_tc(hegv_view(T1, n, n, 1, 0), hegv_view(Li, n, n, 1, 1), hegv_out(Cm, n),
+                              make_double2(1, 0), 0, HEGV_TC_KSPLIT, sub, sub_bytes, status, stream));
+    } else {
+      carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
+      const void* pa[1] = {Li};
+      const void* pb[1] = {H};
+      void* pc[1] = {T1};
+      int32_t e[3] = {0, 0, 0};
+      CARC_RETURN_IF(gett_launch(d, pa, 1, pb, 1, pc, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+      carc_contract_desc d2 = DescBuilder().m(n, n, n).n(n, n, 1).k(n, 1, 1).d;
+      d2.conj_b = 1;
+      const void* pa2[1] = {T1};
+      const void* pb2[1] = {Li};
+      void* pc2[1] = {Cm};
+      CARC_RETURN_IF(gett_launch(d2, pa2, 1, pb2, 1, pc2, 1, e, 1, make_double2(1, 0), 0, sub, sub_bytes, stream));
+    }
   }
   // start vector u0 = L^H x0 (or a fixed vector)
   if (x0) {
@@ -593,7 +825,11 @@ int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, d
   // previous center) would otherwise keep Lanczos out of its sector.
   perturb_start_kernel<<<1, 256, 0, stream>>>(n, u0, x0 ? 1e-3 : 1.0);  // one block: reads finish before writes
   CARC_CHECK_LAUNCH();
-  int st = lanczos_lowest(n, Cm, u0, u, eigenvalues, max_krylov, max_restarts, tol, iterations, sub, sub_bytes, stream);
+  int st;
+  {
+    PhaseScope ph(PH_HEGV_LANCZOS, stream);
+    st = lanczos_lowest(n, Cm, u0, u, eigenvalues, max_krylov, max_restarts, tol, iterations, sub, sub_bytes, stream);
+  }
   if (st != CARC_OK && st != CARC_NOT_CONVERGED) return st;
   if (flags & CARC_HEGV_TENSOR_CORE) {
     CARC_CHECK_CUDA(cudaMemcpyAsync(&hstat, status, sizeof(int), cudaMemcpyDeviceToHost, stream));

@@ -49,8 +49,10 @@ int64_t carc_launch_counter(void);
 /* Per-phase device timing of the tensor-core stage-3 operator (no counterpart
  * in the reference; instrumentation for benchmarks).  While enabled, each
  * phase's launches are bracketed by a CUDA event pair on the launching stream.
- * Phases: 0 operand packing, 1 step-A GEMMs (folding epilogue), 2 step-B
- * GEMM, 3 split-K reductions.  carc_phase_timing_read, called after the
+ * Phases: 0 operand packing, 1 step-A GEMMs (folding epilogue; the fused
+ * kernel), 2 step-B GEMM, 3 split-K reductions; of carc_zhegv_lowest: 4 the
+ * Cholesky factorization, 5 the triangular inverse, 6 the pencil reduction,
+ * 7 the Lanczos iteration.  carc_phase_timing_read, called after the
  * stream is synchronized, returns the summed milliseconds and the number of
  * bracketed intervals of one phase and drops its records. */
 int carc_phase_timing_enable(int32_t on);
