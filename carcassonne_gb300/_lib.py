@@ -13,6 +13,7 @@ import threading
 from . import build as _build
 
 CARC_HEGV_TENSOR_CORE = 1
+CARC_HEGV_SINGLE = 2
 CARC_OK = 0
 CARC_BAD_SHAPE = 1
 CARC_BAD_ARG = 2

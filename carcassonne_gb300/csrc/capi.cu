@@ -166,7 +166,7 @@ int carc_zhegv_lowest(int32_t n, const void* H, const void* N, const void* x0, v
                       int32_t max_krylov, int32_t max_restarts, double tol, int32_t flags, int32_t* iterations,
                       void* factors, void* workspace, int64_t workspace_bytes, void* stream) {
   if (!H || !N || !x) return fail(CARC_BAD_ARG, "carc_zhegv_lowest: NULL argument");
-  if (flags & ~CARC_HEGV_TENSOR_CORE) return fail(CARC_BAD_ARG, "carc_zhegv_lowest: unknown flags 0x%x", flags);
+  if (flags & ~(CARC_HEGV_TENSOR_CORE | CARC_HEGV_SINGLE)) return fail(CARC_BAD_ARG, "carc_zhegv_lowest: unknown flags 0x%x", flags);
   int it = 0;
   int st = hegv_lowest(n, H, N, x0, x, eigenvalues, max_krylov, max_restarts, tol, flags, &it, factors, workspace,
                        workspace_bytes, as_stream(stream));

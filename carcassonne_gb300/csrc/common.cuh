@@ -95,6 +95,45 @@ __device__ __forceinline__ double2 warp_sum2(double2 v) {
   return v;
 }
 
+// ---- complex float (complex64) overloads ------------------------------------
+__host__ __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__host__ __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ void cfma(float2& a, float2 b, float2 c) {
+  a.x = fmaf(b.x, c.x, a.x);
+  a.x = fmaf(-b.y, c.y, a.x);
+  a.y = fmaf(b.x, c.y, a.y);
+  a.y = fmaf(b.y, c.x, a.y);
+}
+__host__ __device__ __forceinline__ float2 cmulc(float2 b, float2 c) {
+  return make_float2(b.x * c.x + b.y * c.y, b.x * c.y - b.y * c.x);
+}
+__host__ __device__ __forceinline__ float cabs2(float2 a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float2 warp_sum2(float2 v) {
+  v.x = warp_sum(v.x);
+  v.y = warp_sum(v.y);
+  return v;
+}
+// zero of a complex type; widening to complex128
+template <typename Z>
+__host__ __device__ __forceinline__ Z czero() {
+  Z z;
+  z.x = 0;
+  z.y = 0;
+  return z;
+}
+__host__ __device__ __forceinline__ double2 to_d2(double2 a) { return a; }
+__host__ __device__ __forceinline__ double2 to_d2(float2 a) { return make_double2(a.x, a.y); }
+
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }

@@ -292,8 +292,17 @@ __global__ void gett_reduce_kernel(const __grid_constant__ GettParams p) {
     int64_t t = i / p.N;
     int64_t m = t % p.M;
     int out = (int)(t / p.M);
+    // eight partials in flight, added in split order
+    const double2* src = p.partial + (int64_t)out * p.M * p.N + m * p.N + n;
+    const int64_t stride = (int64_t)p.n_out * p.M * p.N;
     double2 s = make_double2(0.0, 0.0);
-    for (int ks = 0; ks < p.ksplit; ++ks) s = cadd(s, p.partial[((int64_t)ks * p.n_out + out) * p.M * p.N + m * p.N + n]);
+    for (int k0 = 0; k0 < p.ksplit; k0 += 8) {
+      double2 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = k0 + u < p.ksplit ? src[(k0 + u) * stride] : make_double2(0.0, 0.0);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) s = cadd(s, v[u]);
+    }
     int64_t off = decompose(m, p.nm, p.m_ext, p.c_m) + decompose(n, p.nn, p.n_ext, p.c_n);
     double2* C = p.c[out];
     double2 v = cmul(p.alpha, s);
@@ -341,7 +350,7 @@ static int choose_ksplit(int64_t M, int64_t N, int64_t K, int n_out, int64_t* kc
   if (tiles < target && K >= 256) {
     int64_t want = ceil_div(target, tiles);
     int64_t maxk = K / 128;
-    ks = (int)std::max<int64_t>(1, std::min<int64_t>({want, maxk, (int64_t)64}));
+    ks = (int)std::max<int64_t>(1, std::min<int64_t>({want, maxk, (int64_t)512}));
   }
   int64_t chunk = ceil_div(K, ks);
   chunk = ceil_div(chunk, t.kstep) * t.kstep;

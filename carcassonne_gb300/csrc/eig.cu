@@ -352,14 +352,15 @@ constexpr int LZ_THREADS = 256;
 
 struct LzParams {
   int n, j0, j1, rpc;
-  const double2* C;
-  double2* Q;       // (mk + 1) x n Krylov basis
+  const void* C;    // n x n, complex128 or complex64
+  void* Q;          // (mk + 1) x n Krylov basis, same type
   double* alpha;
   double* beta;
   double2* pscal;   // [G] per-CTA partial of a scalar inner product
   double2* part;    // [(mk + 1) x G] per-CTA partials of the projections
   double2* h;       // (mk + 1) projections
   double scale_ref;
+  double breakdown_tol;  // beta_j <= breakdown_tol * scale_ref ends the Krylov space
   int* breakdown;
   unsigned int* sync;  // barrier arrivals (zero at launch)
   int* abort;          // set by a CTA whose barrier wait ran out (zero at launch)
@@ -389,20 +390,34 @@ __device__ bool lz_grid_sync(unsigned int* ctr, unsigned int target, int* abort)
   return ok != 0;
 }
 
+template <typename Z>
+__device__ __forceinline__ Z from_d2(double2 a);
+template <>
+__device__ __forceinline__ double2 from_d2<double2>(double2 a) { return a; }
+template <>
+__device__ __forceinline__ float2 from_d2<float2>(double2 a) { return make_float2((float)a.x, (float)a.y); }
+
+// Z = double2 (complex128) or float2 (complex64: the basis, the products and
+// the per-CTA partials in FP32; the cross-CTA sums, alpha and beta in FP64)
+template <typename Z>
 __global__ __launch_bounds__(LZ_THREADS) void lanczos_chunk_kernel(const __grid_constant__ LzParams p) {
-  extern __shared__ double2 lz_w[];  // this CTA's rows of w
+  using R = decltype(Z{}.x);
+  extern __shared__ __align__(16) unsigned char lz_raw[];
+  Z* lz_w = reinterpret_cast<Z*>(lz_raw);  // this CTA's rows of w
   __shared__ double s_alpha, s_bprev, s_beta;
+  const Z* C = static_cast<const Z*>(p.C);
+  Z* Q = static_cast<Z*>(p.Q);
   const int G = (int)gridDim.x, c = (int)blockIdx.x, n = p.n;
   const int r0 = c * p.rpc, r1 = min(n, r0 + p.rpc), nr = max(0, r1 - r0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   unsigned int bar = 0;
   auto gsync = [&]() { return lz_grid_sync(p.sync, ++bar * (unsigned)G, p.abort); };
   for (int j = p.j0; j < p.j1; ++j) {
-    const double2* qj = p.Q + (int64_t)j * n;
+    const Z* qj = Q + (int64_t)j * n;
     // w = C q_j on this CTA's rows (the four-chain row dot of gemv_kernel)
     for (int rl = warp; rl < nr; rl += nw) {
-      const double2* a = p.C + (int64_t)(r0 + rl) * n;
-      double2 s0 = make_double2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+      const Z* a = C + (int64_t)(r0 + rl) * n;
+      Z s0 = czero<Z>(), s1 = s0, s2 = s0, s3 = s0;
       int k = lane;
       for (; k + 96 < n; k += 128) {
         cfma(s0, a[k], qj[k]);
@@ -411,48 +426,57 @@ __global__ __launch_bounds__(LZ_THREADS) void lanczos_chunk_kernel(const __grid_
         cfma(s3, a[k + 96], qj[k + 96]);
       }
       for (; k < n; k += 32) cfma(s0, a[k], qj[k]);
-      double2 sum = warp_sum2(cadd(cadd(s0, s1), cadd(s2, s3)));
+      Z sum = warp_sum2(cadd(cadd(s0, s1), cadd(s2, s3)));
       if (lane == 0) lz_w[rl] = sum;
     }
     __syncthreads();
     // alpha_j = Re(q_j^H w)
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
       double2 acc = make_double2(0.0, 0.0);
-      for (int rl = 0; rl < nr; ++rl) acc = cadd(acc, cmulc(qj[r0 + rl], lz_w[rl]));
-      p.pscal[c] = acc;
+      for (int rl = lane; rl < nr; rl += 32) acc = cadd(acc, to_d2(cmulc(qj[r0 + rl], lz_w[rl])));
+      acc = warp_sum2(acc);
+      if (lane == 0) p.pscal[c] = acc;
     }
     if (!gsync()) return;
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
+      // the G partials in lane order, then a fixed shuffle tree: the same sum in every CTA
       double a = 0.0;
-      for (int q = 0; q < G; ++q) a += p.pscal[q].x;
-      s_alpha = a;
-      s_bprev = j > 0 ? p.beta[j - 1] : 0.0;
+      for (int q = lane; q < G; q += 32) a += p.pscal[q].x;
+      a = warp_sum(a);
+      if (lane == 0) {
+        s_alpha = a;
+        s_bprev = j > 0 ? p.beta[j - 1] : 0.0;
+      }
     }
     __syncthreads();
     for (int rl = threadIdx.x; rl < nr; rl += blockDim.x) {
-      double2 v = csub(lz_w[rl], cscale(qj[r0 + rl], s_alpha));
-      if (j > 0) v = csub(v, cscale(p.Q[(int64_t)(j - 1) * n + r0 + rl], s_bprev));
+      Z v = csub(lz_w[rl], cscale(qj[r0 + rl], (R)s_alpha));
+      if (j > 0) v = csub(v, cscale(Q[(int64_t)(j - 1) * n + r0 + rl], (R)s_bprev));
       lz_w[rl] = v;
     }
     __syncthreads();
     // two classical Gram-Schmidt passes against q_0 .. q_j
     for (int pass = 0; pass < 2; ++pass) {
       for (int i = threadIdx.x; i <= j; i += blockDim.x) {
-        double2 acc = make_double2(0.0, 0.0);
-        const double2* qi = p.Q + (int64_t)i * n + r0;
+        Z acc = czero<Z>();
+        const Z* qi = Q + (int64_t)i * n + r0;
+#pragma unroll 8
         for (int rl = 0; rl < nr; ++rl) acc = cadd(acc, cmulc(qi[rl], lz_w[rl]));
-        p.part[(int64_t)i * G + c] = acc;
+        p.part[(int64_t)i * G + c] = to_d2(acc);
       }
       if (!gsync()) return;
-      for (int i = c + (int)threadIdx.x * G; i <= j; i += (int)blockDim.x * G) {
+      // coefficient i by warp (i / G) % nw of CTA i % G: lane-strided partials, fixed shuffle tree
+      for (int i = c + warp * G; i <= j; i += nw * G) {
         double2 acc = make_double2(0.0, 0.0);
-        for (int q = 0; q < G; ++q) acc = cadd(acc, p.part[(int64_t)i * G + q]);
-        p.h[i] = acc;
+        for (int q = lane; q < G; q += 32) acc = cadd(acc, p.part[(int64_t)i * G + q]);
+        acc = warp_sum2(acc);
+        if (lane == 0) p.h[i] = acc;
       }
       if (!gsync()) return;
       for (int rl = warp; rl < nr; rl += nw) {
-        double2 acc = make_double2(0.0, 0.0);
-        for (int i = lane; i <= j; i += 32) cfma(acc, p.h[i], p.Q[(int64_t)i * n + r0 + rl]);
+        Z acc = czero<Z>();
+#pragma unroll 4
+        for (int i = lane; i <= j; i += 32) cfma(acc, from_d2<Z>(p.h[i]), Q[(int64_t)i * n + r0 + rl]);
         acc = warp_sum2(acc);
         if (lane == 0) lz_w[rl] = csub(lz_w[rl], acc);
       }
@@ -461,23 +485,27 @@ __global__ __launch_bounds__(LZ_THREADS) void lanczos_chunk_kernel(const __grid_
     // beta_j = ||w||, q_{j+1} = w / beta_j
     if (threadIdx.x == 0) {
       double acc = 0.0;
-      for (int rl = 0; rl < nr; ++rl) acc += cabs2(lz_w[rl]);
+      for (int rl = 0; rl < nr; ++rl) acc += (double)cabs2(lz_w[rl]);
       p.pscal[c] = make_double2(acc, 0.0);
     }
     if (!gsync()) return;
-    if (threadIdx.x == 0) {
+    if (warp == 0) {
       double b2 = 0.0;
-      for (int q = 0; q < G; ++q) b2 += p.pscal[q].x;
+      for (int q = lane; q < G; q += 32) b2 += p.pscal[q].x;
+      b2 = warp_sum(b2);
       s_beta = sqrt(fmax(b2, 0.0));
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
       if (c == 0) {
         p.alpha[j] = s_alpha;
         p.beta[j] = s_beta;
-        if (s_beta <= 1e-13 * p.scale_ref) *p.breakdown = 1;
+        if (s_beta <= p.breakdown_tol * p.scale_ref) *p.breakdown = 1;
       }
     }
     __syncthreads();
-    const double inv = s_beta > 0 ? 1.0 / s_beta : 0.0;
-    for (int rl = threadIdx.x; rl < nr; rl += blockDim.x) p.Q[(int64_t)(j + 1) * n + r0 + rl] = cscale(lz_w[rl], inv);
+    const R inv = s_beta > 0 ? (R)(1.0 / s_beta) : (R)0;
+    for (int rl = threadIdx.x; rl < nr; rl += blockDim.x) Q[(int64_t)(j + 1) * n + r0 + rl] = cscale(lz_w[rl], inv);
     if (j + 1 < p.j1 && !gsync()) return;  // q_{j+1} complete before the next product
   }
 }
@@ -603,6 +631,7 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
         lp.part = W.part;
         lp.h = W.h;
         lp.scale_ref = scale_ref;
+        lp.breakdown_tol = 1e-13;
         lp.breakdown = W.breakdown;
         lp.sync = W.sync;
         lp.abort = reinterpret_cast<int*>(W.sync + 1);
@@ -618,7 +647,7 @@ int lanczos_lowest(int n, const void* Cv, const void* u0, void* u, double* eigen
         la[0].val.cooperative = 1;
         cfg.attrs = la;
         cfg.numAttrs = 1;
-        if (cudaLaunchKernelEx(&cfg, lanczos_chunk_kernel, lp) == cudaSuccess) {
+        if (cudaLaunchKernelEx(&cfg, lanczos_chunk_kernel<double2>, lp) == cudaSuccess) {
           count_launch();
           total += j1 - j - 1;
           j = j1 - 1;
@@ -740,6 +769,482 @@ constexpr int HEGV_TC_KSPLIT = 4;
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Single-precision reduction and Lanczos (CARC_HEGV_SINGLE), for the pencils
+// of the mixed-precision solve: they carry the tensor-core forming error
+// (about 1e-5 relative) already, and GB300 issues FP32 some 30 times faster
+// than FP64.  N = L L^H and L^-1 in complex64 (blocked, NB = 32: diagonal
+// block in shared memory, panel by forward substitution, trailing updates by
+// a tiled complex64 GEMM), C = L^-1 H L^-H on the tensor cores (as with
+// CARC_HEGV_TENSOR_CORE), and the cooperative Lanczos in complex64 with
+// FP64 cross-CTA sums, alpha and beta.  The caller's eigenvalue comes from
+// the tridiagonal in FP64; the solve's Rayleigh quotient with exact H x, N x
+// makes the energy error second order in this eigenvector's error.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int NB32 = 32;
+constexpr int TRSM32_COLS = 16, TRSM32_ROWG = 16;
+
+__global__ void c128_to_c64_kernel(int64_t count, const double2* __restrict__ a, float2* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = make_float2((float)a[i].x, (float)a[i].y);
+}
+
+__global__ void c64_to_c128_kernel(int64_t count, const float2* __restrict__ a, double2* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = make_double2(a[i].x, a[i].y);
+}
+
+__global__ void potrf32_diag_kernel(int n, float2* __restrict__ A, int k0, int nb, int* status, float scale) {
+  __shared__ float2 T[NB32][NB32 + 1];
+  __shared__ float djj;
+  const int tx = threadIdx.x, ty = threadIdx.y;  // 32 x 32
+  if (tx < nb && ty < nb) T[ty][tx] = A[(int64_t)(k0 + ty) * n + k0 + tx];
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (tx == 0 && ty == 0) {
+      float d = T[j][j].x;
+      if (!(d > 1e-30f * scale) || isnan(d)) {
+        atomicExch(status, CARC_NOT_POSDEF);
+        d = 1.0f;
+      }
+      djj = sqrtf(d);
+      T[j][j] = make_float2(djj, 0.0f);
+    }
+    __syncthreads();
+    if (ty == 0 && tx > j && tx < nb) T[tx][j] = cscale(T[tx][j], 1.0f / djj);
+    __syncthreads();
+    if (ty > j && ty < nb && tx > j && tx <= ty) T[ty][tx] = csub(T[ty][tx], cmul(T[ty][j], cconj(T[tx][j])));
+    __syncthreads();
+  }
+  if (tx < nb && ty < nb) A[(int64_t)(k0 + ty) * n + k0 + tx] = tx <= ty ? T[ty][tx] : make_float2(0.0f, 0.0f);
+}
+
+// L21 = A21 L11^{-H}: a warp per row, forward substitution with shuffles
+__global__ void potrf32_panel_kernel(int n, float2* __restrict__ A, int k0, int nb) {
+  __shared__ float2 L11[NB32][NB32 + 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) L11[idx / nb][idx % nb] = A[(int64_t)(k0 + idx / nb) * n + k0 + idx % nb];
+  __syncthreads();
+  for (int row = k0 + nb + blockIdx.x * nwarps + warp; row < n; row += gridDim.x * nwarps) {
+    float2* a = A + (int64_t)row * n + k0;
+    float2 x = lane < nb ? a[lane] : make_float2(0.0f, 0.0f);
+    for (int j = 0; j < nb; ++j) {
+      float2 xj = make_float2(__shfl_sync(0xffffffffu, x.x, j), __shfl_sync(0xffffffffu, x.y, j));
+      xj = cscale(xj, 1.0f / L11[j][j].x);
+      if (lane == j) x = xj;
+      if (lane > j && lane < nb) x = csub(x, cmul(xj, cconj(L11[lane][j])));
+    }
+    if (lane < nb) a[lane] = x;
+  }
+}
+
+// C[i][j] += alpha sum_k A[i][k] op(B)[k][j] over an M x N block, complex64
+// row-major with leading dimensions: op(B)[k][j] = conj(B[j][k]) (BH) or
+// B[k][j].  32 x 32 output tile per block of 256 threads (4 outputs each),
+// K in steps of 16 through shared memory.
+template <bool BH>
+__global__ __launch_bounds__(256) void cgemm32_kernel(int M, int N, int K, float alpha, const float2* __restrict__ A,
+                                                      int lda, const float2* __restrict__ B, int ldb,
+                                                      float2* __restrict__ C, int ldc) {
+  __shared__ float2 As[32][17], Bs[16][33];
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // ty 0..7 -> rows ty, ty+8, ty+16, ty+24
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  float2 acc[4] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int idx = threadIdx.x; idx < 32 * 16; idx += 256) {
+      const int r = idx / 16, kk = idx % 16;
+      As[r][kk] = (i0 + r < M && k0 + kk < K) ? A[(int64_t)(i0 + r) * lda + k0 + kk] : make_float2(0.f, 0.f);
+      const int kb = idx / 32, cc = idx % 32;
+      float2 bv = make_float2(0.f, 0.f);
+      if (k0 + kb < K && j0 + cc < N)
+        bv = BH ? cconj(B[(int64_t)(j0 + cc) * ldb + k0 + kb]) : B[(int64_t)(k0 + kb) * ldb + j0 + cc];
+      Bs[kb][cc] = bv;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      const float2 b = Bs[kk][tx];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) cfma(acc[q], As[ty + 8 * q][kk], b);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = i0 + ty + 8 * q, j = j0 + tx;
+    if (i < M && j < N) C[(int64_t)i * ldc + j] = cadd(C[(int64_t)i * ldc + j], cscale(acc[q], alpha));
+  }
+}
+
+template <bool BH>
+int cgemm32(int M, int N, int K, float alpha, const float2* A, int lda, const float2* B, int ldb, float2* C, int ldc,
+            cudaStream_t stream) {
+  if (M <= 0 || N <= 0 || K <= 0) return CARC_OK;
+  cgemm32_kernel<BH><<<dim3((unsigned)ceil_div(N, 32), (unsigned)ceil_div(M, 32)), 256, 0, stream>>>(
+      M, N, K, alpha, A, lda, B, ldb, C, ldc);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+__global__ void zero_upper32_kernel(int n, float2* __restrict__ A) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)n * n;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    if ((int)(idx % n) > (int)(idx / n)) A[idx] = make_float2(0.f, 0.f);
+}
+
+int potrf32(int n, float2* A, int* status, cudaStream_t stream) {
+  CARC_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int), stream));
+  for (int k0 = 0; k0 < n; k0 += NB32) {
+    const int nb = std::min(NB32, n - k0);
+    potrf32_diag_kernel<<<1, dim3(32, 32), 0, stream>>>(n, A, k0, nb, status, 1.0f);
+    CARC_CHECK_LAUNCH();
+    const int rest = n - k0 - nb;
+    if (rest <= 0) break;
+    potrf32_panel_kernel<<<(int)std::min<int64_t>(ceil_div(rest, 8), 4 * 152), 256, 0, stream>>>(n, A, k0, nb);
+    CARC_CHECK_LAUNCH();
+    // A22 -= L21 L21^H (the full square; the strict upper part is zeroed at the end)
+    float2* L21 = A + (int64_t)(k0 + nb) * n + k0;
+    CARC_RETURN_IF(cgemm32<true>(rest, rest, nb, -1.0f, L21, n, L21, n, A + (int64_t)(k0 + nb) * n + k0 + nb, n, stream));
+  }
+  zero_upper32_kernel<<<(int)std::min<int64_t>(ceil_div((int64_t)n * n, 256), 1216), 256, 0, stream>>>(n, A);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+// X[k0:k0+nb, 0:k0+nb] = L_kk^{-1} X[k0:k0+nb, 0:k0+nb] (the FP64 trsm_diag_kernel in complex64)
+__global__ __launch_bounds__(TRSM32_COLS * TRSM32_ROWG) void trsm32_diag_kernel(int n, const float2* __restrict__ Lm,
+                                                                                float2* __restrict__ X, int k0, int nb) {
+  __shared__ float2 Lk[NB32][NB32 + 1];
+  __shared__ float2 Li[NB32][NB32 + 1];
+  __shared__ float2 dinv[NB32];
+  __shared__ float2 Xs[NB32][TRSM32_COLS + 1];
+  for (int idx = threadIdx.x; idx < nb * nb; idx += blockDim.x) Lk[idx / nb][idx % nb] = Lm[(int64_t)(k0 + idx / nb) * n + k0 + idx % nb];
+  __syncthreads();
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    const float2 d = Lk[i][i];
+    const float den = cabs2(d);
+    dinv[i] = make_float2(d.x / den, -d.y / den);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nb; c += blockDim.x) {
+    for (int i = 0; i < c; ++i) Li[i][c] = make_float2(0.f, 0.f);
+    Li[c][c] = dinv[c];
+    for (int i = c + 1; i < nb; ++i) {
+      float2 acc = make_float2(0.f, 0.f);
+      for (int j = c; j < i; ++j) acc = cadd(acc, cmul(Lk[i][j], Li[j][c]));
+      Li[i][c] = cmul(dinv[i], make_float2(-acc.x, -acc.y));
+    }
+  }
+  const int tc = threadIdx.x % TRSM32_COLS, tr = threadIdx.x / TRSM32_COLS;
+  const int cols = k0 + nb;
+  for (int c0 = blockIdx.x * TRSM32_COLS; c0 < cols; c0 += gridDim.x * TRSM32_COLS) {
+    const int col = c0 + tc;
+    __syncthreads();
+    for (int i = tr; i < nb; i += TRSM32_ROWG) Xs[i][tc] = col < cols ? X[(int64_t)(k0 + i) * n + col] : make_float2(0.f, 0.f);
+    __syncthreads();
+    if (col < cols)
+      for (int i = tr; i < nb; i += TRSM32_ROWG) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int j = 0; j <= i; ++j) cfma(acc, Li[i][j], Xs[j][tc]);
+        X[(int64_t)(k0 + i) * n + col] = acc;
+      }
+  }
+}
+
+__global__ void set_identity32_kernel(int n, float2* __restrict__ X) {
+  for (int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; idx < (int64_t)n * n;
+       idx += (int64_t)gridDim.x * blockDim.x)
+    X[idx] = make_float2((idx / n) == (idx % n) ? 1.f : 0.f, 0.f);
+}
+
+int trtri32(int n, const float2* Lm, float2* X, cudaStream_t stream) {
+  set_identity32_kernel<<<(int)std::min<int64_t>(ceil_div((int64_t)n * n, 256), 1216), 256, 0, stream>>>(n, X);
+  CARC_CHECK_LAUNCH();
+  for (int k0 = 0; k0 < n; k0 += NB32) {
+    const int nb = std::min(NB32, n - k0);
+    // X[k0:k0+nb, 0:k0] -= L[k0:k0+nb, 0:k0] X[0:k0, 0:k0]
+    if (k0 > 0) CARC_RETURN_IF(cgemm32<false>(nb, k0, k0, -1.0f, Lm + (int64_t)k0 * n, n, X, n, X + (int64_t)k0 * n, n, stream));
+    const int cols = k0 + nb;
+    trsm32_diag_kernel<<<(int)std::max<int64_t>(1, ceil_div(cols, TRSM32_COLS)), TRSM32_COLS * TRSM32_ROWG, 0, stream>>>(
+        n, Lm, X, k0, nb);
+    CARC_CHECK_LAUNCH();
+  }
+  return CARC_OK;
+}
+
+// out[j] = sum_i conj(M[i][j]) v[i] (M n x n complex64, v complex128 or complex64), FP64 accumulation
+template <typename V>
+__global__ void mhv32_kernel(int n, const float2* __restrict__ M, const V* __restrict__ v, double2* __restrict__ out) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int i = 0; i < n; ++i) acc = cadd(acc, cmulc(to_d2(M[(int64_t)i * n + j]), to_d2(v[i])));
+    out[j] = acc;
+  }
+}
+
+// One block: v (complex64) scaled to unit norm (FP64 sum); *norm_out = |v| when given.
+__global__ void normalize32_kernel(int n, float2* __restrict__ v, double* norm_out) {
+  __shared__ double part[32];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += (double)cabs2(v[i]);
+  acc = warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+    part[0] = t;
+    if (norm_out) *norm_out = sqrt(t);
+  }
+  __syncthreads();
+  const float inv = part[0] > 0 ? (float)(1.0 / sqrt(part[0])) : 0.f;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v[i] = cscale(v[i], inv);
+}
+
+// out[i] = sum_r s[r] Q[r][i] (the Ritz vector), complex64
+__global__ void ritz32_kernel(int n, int m, const float2* __restrict__ Q, const double* __restrict__ s,
+                              float2* __restrict__ out) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    float2 acc = make_float2(0.f, 0.f);
+    for (int r = 0; r < m; ++r) acc = cadd(acc, cscale(Q[(int64_t)r * n + i], (float)s[r]));
+    out[i] = acc;
+  }
+}
+
+// ||C q|| for the breakdown scale (one block; C, q complex64)
+__global__ void cq_norm32_kernel(int n, const float2* __restrict__ C, const float2* __restrict__ q, double* out) {
+  __shared__ double part[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double acc = 0.0;
+  for (int r = warp; r < n; r += nw) {
+    float2 s = make_float2(0.f, 0.f);
+    for (int k = lane; k < n; k += 32) cfma(s, C[(int64_t)r * n + k], q[k]);
+    s = warp_sum2(s);
+    if (lane == 0) acc += (double)cabs2(s);
+  }
+  if (lane == 0) part[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += part[w];
+    *out = sqrt(t);
+  }
+}
+
+struct Hegv32Ws {
+  float2 *A, *Li, *C32, *Q;
+  double2 *Li64, *T1, *C64, *u0, *u;
+  double *alpha, *beta, *tri_out, *s, *scal;
+  double2 *pscal, *part, *h;
+  int *status, *breakdown;
+  unsigned int* sync;
+  void* tc;
+  int64_t tc_bytes;
+};
+
+int64_t hegv32_layout(int n, int mk, Hegv32Ws* W, void* base) {
+  char* p = static_cast<char*>(base);
+  int64_t off = 0;
+  auto take = [&](int64_t bytes) {
+    void* r = p ? p + off : nullptr;
+    off += a256(bytes);
+    return r;
+  };
+  const int64_t nn = (int64_t)n * n;
+  Hegv32Ws t;
+  t.A = (float2*)take(nn * 8);
+  t.Li = (float2*)take(nn * 8);
+  t.C32 = (float2*)take(nn * 8);
+  t.Q = (float2*)take((int64_t)(mk + 1) * n * 8);
+  t.Li64 = (double2*)take(nn * 16);
+  t.T1 = (double2*)take(nn * 16);
+  t.C64 = (double2*)take(nn * 16);
+  t.u0 = (double2*)take((int64_t)n * 16);
+  t.u = (double2*)take((int64_t)n * 16);
+  t.alpha = (double*)take((int64_t)(mk + 1) * 8);
+  t.beta = (double*)take((int64_t)(mk + 1) * 8);
+  t.tri_out = (double*)take(4 * 8);
+  t.s = (double*)take((int64_t)MAXM * 8);
+  t.scal = (double*)take(2 * 8);
+  t.pscal = (double2*)take((int64_t)LZ_MAX_CTAS * 16);
+  t.part = (double2*)take((int64_t)(mk + 1) * LZ_MAX_CTAS * 16);
+  t.h = (double2*)take((int64_t)(mk + 1) * 16);
+  t.status = (int*)take(16);
+  t.breakdown = (int*)take(16);
+  t.sync = (unsigned int*)take(16);
+  const ZView a = hegv_view(nullptr, n, n, 1, 0), b = hegv_view(nullptr, n, 1, n, 0);
+  t.tc_bytes = zgemm_tc_workspace(a, b, HEGV_TC_KSPLIT);
+  t.tc = take(t.tc_bytes);
+  if (W) *W = t;
+  return off;
+}
+
+inline int cast_blocks(int64_t count) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(count, 256), 1216)); }
+
+constexpr int HEGV32_UNAVAILABLE = -1;  // cooperative launch refused: the caller takes the FP64 path
+
+int hegv_lowest_single(int n, const void* H, const void* Nm, const void* x0, void* x, double* eigenvalues,
+                       int max_krylov, int max_restarts, double tol, int* iterations, void* factors, void* ws,
+                       cudaStream_t stream) {
+  const int mk = std::max(1, std::min(max_krylov, std::min(n, MAXM)));
+  Hegv32Ws W;
+  hegv32_layout(n, mk, &W, ws);
+  const int64_t nn = (int64_t)n * n;
+  {
+    PhaseScope ph(PH_HEGV_POTRF, stream);
+    c128_to_c64_kernel<<<cast_blocks(nn), 256, 0, stream>>>(nn, static_cast<const double2*>(Nm), W.A);
+    CARC_CHECK_LAUNCH();
+    CARC_RETURN_IF(potrf32(n, W.A, W.status, stream));
+  }
+  int hstat = 0;
+  CARC_CHECK_CUDA(cudaMemcpyAsync(&hstat, W.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+  if (hstat != CARC_OK) return fail(CARC_NOT_POSDEF, "hegv: the normalization matrix is not positive definite");
+  {
+    PhaseScope ph(PH_HEGV_TRTRI, stream);
+    CARC_RETURN_IF(trtri32(n, W.A, W.Li, stream));
+  }
+  {
+    PhaseScope ph(PH_HEGV_REDUCE, stream);
+    c64_to_c128_kernel<<<cast_blocks(nn), 256, 0, stream>>>(nn, W.Li, W.Li64);
+    CARC_CHECK_LAUNCH();
+    CARC_RETURN_IF(zgemm_tc(hegv_view(W.Li64, n, n, 1, 0), hegv_view(H, n, 1, n, 0), hegv_out(W.T1, n),
+                            make_double2(1, 0), 0, HEGV_TC_KSPLIT, W.tc, W.tc_bytes, W.status, stream));
+    CARC_RETURN_IF(zgemm_tc(hegv_view(W.T1, n, n, 1, 0), hegv_view(W.Li64, n, n, 1, 1), hegv_out(W.C64, n),
+                            make_double2(1, 0), 0, HEGV_TC_KSPLIT, W.tc, W.tc_bytes, W.status, stream));
+    c128_to_c64_kernel<<<cast_blocks(nn), 256, 0, stream>>>(nn, W.C64, W.C32);
+    CARC_CHECK_LAUNCH();
+  }
+  // start vector u0 = L^H x0 (or a fixed vector), perturbed as in the FP64 path
+  if (x0) {
+    mhv32_kernel<double2><<<(int)ceil_div(n, 128), 128, 0, stream>>>(n, W.A, static_cast<const double2*>(x0), W.u0);
+    CARC_CHECK_LAUNCH();
+  } else {
+    CARC_RETURN_IF(fill_launch(n, make_double2(0.0, 0.0), W.u0, stream));
+  }
+  perturb_start_kernel<<<1, 256, 0, stream>>>(n, W.u0, x0 ? 1e-3 : 1.0);
+  CARC_CHECK_LAUNCH();
+  c128_to_c64_kernel<<<cast_blocks(n), 256, 0, stream>>>(n, W.u0, W.Q);
+  CARC_CHECK_LAUNCH();
+  normalize32_kernel<<<1, 1024, 0, stream>>>(n, W.Q, nullptr);
+  CARC_CHECK_LAUNCH();
+  // Lanczos in complex64 (cooperative chunks of eight iterations)
+  static int sm_count = 0;
+  if (sm_count == 0) {
+    int dev = 0;
+    CARC_CHECK_CUDA(cudaGetDevice(&dev));
+    CARC_CHECK_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int lz_ctas = (int)std::max<int64_t>(1, std::min<int64_t>({ceil_div(n, 8), (int64_t)sm_count, LZ_MAX_CTAS}));
+  const int lz_rpc = (int)ceil_div(n, lz_ctas);
+  // FP32 arithmetic: the residual estimate is trusted to about 1e-6
+  tol = std::max(tol, 2e-6);
+  double lam = 0.0, res = 0.0, lam2 = nan("");
+  int total = 0, m = 0;
+  bool converged = false;
+  {
+  PhaseScope ph_lz(PH_HEGV_LANCZOS, stream);
+  for (int restart = 0; restart <= max_restarts && !converged; ++restart) {
+    CARC_CHECK_CUDA(cudaMemsetAsync(W.breakdown, 0, sizeof(int), stream));
+    cq_norm32_kernel<<<1, 1024, 0, stream>>>(n, W.C32, W.Q, W.scal);
+    CARC_CHECK_LAUNCH();
+    double scale_ref = 1.0;
+    CARC_CHECK_CUDA(cudaMemcpyAsync(&scale_ref, W.scal, 8, cudaMemcpyDeviceToHost, stream));
+    CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+    scale_ref = std::max(scale_ref, 1e-300);
+    m = 0;
+    for (int j = 0; j < mk; j += 8) {
+      const int j1 = std::min(mk, j + 8);
+      LzParams lp;
+      lp.n = n;
+      lp.j0 = j;
+      lp.j1 = j1;
+      lp.rpc = lz_rpc;
+      lp.C = W.C32;
+      lp.Q = W.Q;
+      lp.alpha = W.alpha;
+      lp.beta = W.beta;
+      lp.pscal = W.pscal;
+      lp.part = W.part;
+      lp.h = W.h;
+      lp.scale_ref = scale_ref;
+      lp.breakdown_tol = 1e-6;
+      lp.breakdown = W.breakdown;
+      lp.sync = W.sync;
+      lp.abort = reinterpret_cast<int*>(W.sync + 1);
+      CARC_CHECK_CUDA(cudaMemsetAsync(W.sync, 0, 8, stream));
+      cudaLaunchConfig_t cfg;
+      memset(&cfg, 0, sizeof(cfg));
+      cfg.gridDim = dim3((unsigned)lz_ctas);
+      cfg.blockDim = dim3(LZ_THREADS);
+      cfg.dynamicSmemBytes = (size_t)lz_rpc * 8;
+      cfg.stream = stream;
+      cudaLaunchAttribute la[1];
+      la[0].id = cudaLaunchAttributeCooperative;
+      la[0].val.cooperative = 1;
+      cfg.attrs = la;
+      cfg.numAttrs = 1;
+      if (cudaLaunchKernelEx(&cfg, lanczos_chunk_kernel<float2>, lp) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return HEGV32_UNAVAILABLE;
+      }
+      count_launch();
+      total += j1 - j;
+      m = j1;
+      tridiag_lowest_kernel<<<1, TRI_THREADS, 0, stream>>>(m, W.alpha, W.beta, W.tri_out, W.s);
+      CARC_CHECK_LAUNCH();
+      double hv[3];
+      int bd[2] = {0, 0};
+      CARC_CHECK_CUDA(cudaMemcpyAsync(hv, W.tri_out, 24, cudaMemcpyDeviceToHost, stream));
+      CARC_CHECK_CUDA(cudaMemcpyAsync(&bd[0], W.breakdown, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      CARC_CHECK_CUDA(cudaMemcpyAsync(&bd[1], W.sync + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+      if (bd[1]) return fail(CARC_NOT_CONVERGED, "lanczos: a grid barrier wait timed out");
+      lam = hv[0];
+      res = hv[1];
+      lam2 = hv[2];
+      if (bd[0] || res <= tol * std::max(fabs(lam), 1e-300) || m == n) {
+        converged = true;
+        break;
+      }
+    }
+    // Ritz vector (the restart vector, or the result)
+    ritz32_kernel<<<(int)ceil_div(n, 256), 256, 0, stream>>>(n, m, W.Q, W.s, W.Q + (int64_t)mk * n);
+    CARC_CHECK_LAUNCH();
+    normalize32_kernel<<<1, 1024, 0, stream>>>(n, W.Q + (int64_t)mk * n, nullptr);
+    CARC_CHECK_LAUNCH();
+    CARC_CHECK_CUDA(cudaMemcpyAsync(W.Q, W.Q + (int64_t)mk * n, (int64_t)n * 8, cudaMemcpyDeviceToDevice, stream));
+  }
+  }
+  c64_to_c128_kernel<<<cast_blocks(n), 256, 0, stream>>>(n, W.Q, W.u);
+  CARC_CHECK_LAUNCH();
+  // x = L^-H u
+  mhv32_kernel<double2><<<(int)ceil_div(n, 128), 128, 0, stream>>>(n, W.Li, W.u, static_cast<double2*>(x));
+  CARC_CHECK_LAUNCH();
+  if (factors) {
+    double2* f = static_cast<double2*>(factors);
+    CARC_CHECK_CUDA(cudaMemcpyAsync(f, W.C64, nn * 16, cudaMemcpyDeviceToDevice, stream));
+    CARC_CHECK_CUDA(cudaMemcpyAsync(f + nn, W.Li64, nn * 16, cudaMemcpyDeviceToDevice, stream));
+    CARC_CHECK_CUDA(cudaMemcpyAsync(f + 2 * nn, W.u, (int64_t)n * 16, cudaMemcpyDeviceToDevice, stream));
+  }
+  int tcstat = 0;
+  CARC_CHECK_CUDA(cudaMemcpyAsync(&tcstat, W.status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+  CARC_CHECK_CUDA(cudaStreamSynchronize(stream));
+  if (tcstat != CARC_OK) return fail(CARC_NOT_CONVERGED, "hegv: a tensor-core pipeline wait timed out");
+  if (eigenvalues) {
+    eigenvalues[0] = lam;
+    eigenvalues[1] = lam2;
+  }
+  if (iterations) *iterations = total;
+  if (!converged)
+    return fail(CARC_NOT_CONVERGED, "lanczos: residual %.3e after %d iterations (tolerance %.1e)", res, total, tol);
+  return CARC_OK;
+}
+
+}  // namespace
+
 int64_t hegv_workspace_size(int n, int max_krylov, int flags) {
   int64_t mat = a256((int64_t)n * n * 16);
   carc_contract_desc d = DescBuilder().m(n, n, n).n(n, 1, 1).k(n, 1, n).d;
@@ -751,7 +1256,10 @@ int64_t hegv_workspace_size(int n, int max_krylov, int flags) {
   }
   int64_t sub = std::max({potrf_workspace_size(n), trtri_workspace_size(n), a256(g), a256(tc),
                           lanczos_workspace_size(n, max_krylov)});
-  return 4 * mat + 2 * a256((int64_t)n * 16) + a256(64) + sub;
+  const int64_t fp64 = 4 * mat + 2 * a256((int64_t)n * 16) + a256(64) + sub;
+  if (flags & CARC_HEGV_SINGLE)
+    return std::max(fp64, hegv32_layout(n, std::max(1, std::min(max_krylov, std::min(n, MAXM))), nullptr, nullptr));
+  return fp64;
 }
 
 int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, double* eigenvalues, int max_krylov,
@@ -759,6 +1267,12 @@ int hegv_lowest(int n, const void* H, const void* Nm, const void* x0, void* x, d
                 cudaStream_t stream) {
   if (n < 1) return fail(CARC_BAD_SHAPE, "hegv: n = %d", n);
   if (ws_bytes < hegv_workspace_size(n, max_krylov, flags)) return fail(CARC_BAD_ARG, "hegv: workspace too small");
+  if (flags & CARC_HEGV_SINGLE) {
+    const int st = hegv_lowest_single(n, H, Nm, x0, x, eigenvalues, max_krylov, max_restarts, tol, iterations, factors,
+                                      ws, stream);
+    if (st != HEGV32_UNAVAILABLE) return st;
+    flags |= CARC_HEGV_TENSOR_CORE;  // not co-resident here: the FP64 path on the same tensor-core pencil
+  }
   char* p = static_cast<char*>(ws);
   int64_t mat = a256((int64_t)n * n * 16);
   double2* Lm = (double2*)p;

@@ -153,13 +153,15 @@ def tri_inverse_lower(L):
 
 
 def hegv_lowest(H, N, x0=None, tol=1e-13, max_krylov=256, max_restarts=8, tensor_core=False, with_second=False,
-                factors=None):
+                factors=None, single=False):
     """Lowest eigenpair of H x = l N x; returns (l, x, iterations), x N-normalized
     (with_second: (l, x, iterations, l2), l2 the second-lowest Ritz value, a
     gap estimate to about 1e-6).  factors: a complex128 device tensor of
     2 n^2 + n elements that receives [C = L^-1 H L^-H | L^-1 | u].
     tensor_core: reduce the pencil with the split-BF16 tensor-core GEMM
-    (~1e-5 relative; for pencils that are tensor-core approximations)."""
+    (~1e-5 relative; for pencils that are tensor-core approximations).
+    single: also factor, invert and iterate in complex64 (residual test
+    clamped to tol >= 2e-6); for the same pencils."""
     Ht = (H._t if isinstance(H, TorchData) else TorchData(H)._t).contiguous()
     Nt = (N._t if isinstance(N, TorchData) else TorchData(N)._t).contiguous()
     n = Ht.shape[0]
@@ -168,7 +170,7 @@ def hegv_lowest(H, N, x0=None, tol=1e-13, max_krylov=256, max_restarts=8, tensor
     x0t = None
     if x0 is not None:
         x0t = (x0._t if isinstance(x0, TorchData) else TorchData(x0)._t).reshape(-1).contiguous()
-    flags = _lib.CARC_HEGV_TENSOR_CORE if tensor_core else 0
+    flags = (_lib.CARC_HEGV_TENSOR_CORE if tensor_core else 0) | (_lib.CARC_HEGV_SINGLE if single else 0)
     ws_bytes = lib.carc_zhegv_lowest_workspace_size(n, max_krylov, flags)
     ws = engine.Workspace.get(ws_bytes, Ht.device)
     lam = (ctypes.c_double * 2)(0.0, 0.0)

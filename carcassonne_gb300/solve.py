@@ -3,12 +3,15 @@
 plain  : H_eff and N_eff formed in FP64 on the CUDA cores, lowest generalized
          eigenpair by the Cholesky-reduced restarted Lanczos (linalg.hegv_lowest).
 mixed  : H_eff and N_eff formed on the tensor cores from split-BF16 operands
-         (~1e-5 relative), the pencil reduced with tensor-core GEMMs and the
-         same Lanczos on it (to 1e-7); then one FP64 application of H and N
-         gives the exact residual of that eigenvector, one Newton step against
-         the tensor-core pencil (MINRES on its reduced form) corrects the
-         vector, and the energy is the Rayleigh quotient of the corrected
-         vector (exact first-order terms, tensor-core second-order terms).
+         (~1e-5 relative), N factored and L inverted in complex64, the pencil
+         reduced with tensor-core GEMMs and the Lanczos iteration run in
+         complex64 on it; then one FP64 application of H and N gives the
+         exact residual of that eigenvector, one Newton step against the
+         tensor-core pencil (MINRES on its reduced form) corrects the vector,
+         and the energy is the Rayleigh quotient of the corrected vector
+         (exact first-order terms, tensor-core second-order terms).  Without
+         the Newton step (newton=False) the energy is the Rayleigh quotient of
+         the tensor-core eigenvector itself, with the exact H x and N x.
 
 Both return the energy, the N-normalized center and a breakdown of where the
 time went (CUDA events on the current stream).
@@ -102,15 +105,30 @@ def _correct(Hop, Nop, x, Ht, Nt, factors):
     return num / den, _lin(1.0 / abs(den) ** 0.5, x2, 0.0, x2), e
 
 
-def solve_center(H, N, x0=None, precision="plain", tol=None):
+def _rayleigh(Hop, Nop, x):
+    """Rayleigh quotient of x with one FP64 application of H and N, and x
+    N-normalized."""
+    xf = x.reshape(-1)
+    hx, nx = _apply(Hop, xf), _apply(Nop, xf)
+    nn = _dot(xf, nx).real
+    return _dot(xf, hx).real / nn, _lin(1.0 / abs(nn) ** 0.5, xf, 0.0, xf)
+
+
+def solve_center(H, N, x0=None, precision="plain", tol=None, newton=True):
     """Lowest eigenpair of (H_eff, N_eff) given the two stage-3 Multipliers.
 
     mixed: the eigenvector of the tensor-core pencil is accurate to about the
     operands' 1e-5 over the gap; one Newton correction against the same
     pencil with the exact FP64 residual (``_correct``) recovers FP64-level
-    energies.  ``tol`` is the Lanczos residual tolerance (default 1e-13
-    plain; 1e-7 mixed: the tensor-core pencil's own error, which the Newton
-    correction removes, dominates the eigenvector's below that)."""
+    energies.  The pencil is reduced and iterated in complex64
+    (linalg.hegv_lowest single=True).  newton=False skips the correction:
+    the energy is then the Rayleigh quotient of the tensor-core eigenvector
+    with the exact H x and N x, whose error is second order in the
+    eigenvector's (about 1e-9 relative on the benchmark pencil), and the
+    center is that eigenvector.  ``tol`` is the Lanczos residual tolerance
+    (default 1e-13 plain; 1e-7 mixed, clamped to 2e-6 by the complex64
+    iteration: the tensor-core pencil's own error dominates the
+    eigenvector's below that)."""
     Hop, Nop = getattr(H, "operator", None), N.operator
     timer = _Timer()
     timer.mark("start")
@@ -138,7 +156,8 @@ def solve_center(H, N, x0=None, precision="plain", tol=None):
         n = Hm.shape[0]
         factors = torch.empty(2 * n * n + n, dtype=CDT, device=Hm.device)
     lam, x, iters = linalg.hegv_lowest(TorchData(Hm), TorchData(Nm), x0=x0, tol=tol,
-                                       tensor_core=(precision == "mixed"), factors=factors)
+                                       tensor_core=(precision == "mixed"), factors=factors,
+                                       single=(precision == "mixed"))
     timer.mark("eigensolve")
     xt = x._t
     energy = lam
@@ -146,7 +165,11 @@ def solve_center(H, N, x0=None, precision="plain", tol=None):
     if precision == "mixed":
         Hop.check_status()
         Nop.check_status()
-        energy, xt, rq0 = _correct(Hop, Nop, xt, Hm, Nm, factors)
+        if newton:
+            energy, xt, rq0 = _correct(Hop, Nop, xt, Hm, Nm, factors)
+        else:
+            energy, xt = _rayleigh(Hop, Nop, xt)
+            rq0 = energy
         energy = float(energy)
         timer.mark("refine")
     out = TorchData(xt.reshape(Hop.in_shape))

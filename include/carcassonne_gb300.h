@@ -306,8 +306,14 @@ int64_t carc_ztrtri_lower_workspace_size(int32_t n);
  * flags: CARC_HEGV_TENSOR_CORE forms C = L^-1 H L^-H with the split-BF16
  * tensor-core GEMM (about 1e-5 relative) instead of FP64 -- for pencils that
  * are themselves tensor-core approximations (the mixed-precision solve).
+ * CARC_HEGV_SINGLE also factors N and inverts L in complex64 and runs the
+ * Lanczos iteration in complex64 (FP64 cross-block sums, alpha, beta and
+ * tridiagonal); its residual test is clamped to tol >= 2e-6.  For the
+ * same tensor-core pencils, whose energy the caller takes as the Rayleigh
+ * quotient of exact H x and N x.
  */
 #define CARC_HEGV_TENSOR_CORE 1
+#define CARC_HEGV_SINGLE 2
 int carc_zhegv_lowest(int32_t n, const void* H, const void* N, const void* x0, void* x, double* eigenvalues,
                       int32_t max_krylov, int32_t max_restarts, double tol, int32_t flags, int32_t* iterations,
                       void* factors, void* workspace, int64_t workspace_bytes, void* stream);
