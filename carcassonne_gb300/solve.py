@@ -124,8 +124,9 @@ def solve_center(H, N, x0=None, precision="plain", tol=None, newton=True):
     (linalg.hegv_lowest single=True).  newton=False skips the correction:
     the energy is then the Rayleigh quotient of the tensor-core eigenvector
     with the exact H x and N x, whose error is second order in the
-    eigenvector's (about 1e-9 relative on the benchmark pencil), and the
-    center is that eigenvector.  ``tol`` is the Lanczos residual tolerance
+    eigenvector's error and so grows as the spectral gap shrinks (6.5e-10
+    relative on the benchmark pencil, 3.7e-8 on a small-gap golden case),
+    and the center is that eigenvector.  ``tol`` is the Lanczos residual tolerance
     (default 1e-13 plain; 1e-7 mixed, clamped to 2e-6 by the complex64
     iteration: the tensor-core pencil's own error dominates the
     eigenvector's below that)."""
