@@ -49,14 +49,15 @@ BATCHED = dict(workload="batched center-site matvecs, TI, D in 2..6, chi in 16..
 PHASE_NAMES = ("pack", "step_a", "step_b", "reduce")
 KERNEL_OF_PHASE = dict(pack="pack_vin_kernel", step_a="gemm_bf16_tn_kernel<256,1> (folding epilogue)",
                        step_b="gemm_bf16_tn_kernel<256,0> (split-K)", reduce="reduce_planes_kernel",
-                       fused="stage3_fused_kernel (step A + fold + step B, W on chip)")
+                       fused="stage3_fused_kernel (one cooperative launch: Vin packing, step A + fold + step B "
+                             "with W on chip, plane reduction)")
 # DRAM bytes (read + write) per launch from one ncu capture of this workload
 # (profiles/ holds the summary and the command that produced it)
 NCU_TRAFFIC = {
     ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "fused"): dict(
-        bytes_per_launch=129.5e6,
-        source="profiles/stage3_fused_matvec_D4_chi32_nvec8.md: one fused launch, dram read 126.2 MB + write "
-               "3.2 MB"),
+        bytes_per_launch=129.9e6,
+        source="profiles/stage3_fused_matvec_D4_chi32_nvec8.md: one cooperative fused launch (packing, both "
+               "steps, plane reduction), dram read 126.1 MB + write 3.9 MB"),
     ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "step_a"): dict(
         bytes_per_launch=8.97e6,
         source="profiles/stage3_tc_matvec_D4_chi32_nvec8.md: one step-A launch (1-term group, 41.9 MB "
