@@ -400,25 +400,32 @@ __global__ void pack_vin_kernel(const double2* __restrict__ x, uint32_t* __restr
 // ---------------------------------------------------------------------------
 // Fused matvec: step A and step B in one persistent kernel, W kept on chip.
 //
-// A unit of work is (x-tile t, S2_1 tag g): 32 complex rows of step A (XP
-// x-pairs x all L = l0 l1 rows) against the group's Vin.  Per unit:
-//   MMA-A   TMEM_A[128 x NA] = packed S2_0 tile . Vin_g      (TMA-fed, 2 stages)
+// A pair is (x-tile t, S2_1 tag g): 32 complex rows of step A (XP x values x
+// all L = l0 l1 rows) against the tag's Vin; a unit is one vector part of a
+// pair (VH = 2 parts when the halves stay MMA-shaped).  Per unit:
+//   MMA-A   TMEM_A[u % nbuf][128 x NA/VH] = packed S2_0 tile . Vin part
+//           (TMA-fed, up to 4 stages)
 //   fold    epilogue warps read TMEM_A, fold (hi+lo, re/im) and write the
 //           unit's W slice straight into shared memory as step B's K-major
 //           128B-swizzled operand B_B (rows (vec,l0,l1,p), 32 complex k)
-//   MMA-B   TMEM_B[128 x NB] += S2_1[g] K-slice (TMA) . B_B
-// TMEM_B accumulates over all units of the CTA and becomes one split-K plane;
-// the planes are summed by the FP64 two-level reduction.  Warp 0 issues the
-// step-A TMA loads, warp 10 the step-B slice loads, warp 1 the MMAs (one
-// thread each); warps 2..17 run the fold, four per TMEM lane quadrant.  Every wait is bounded; on expiry the CTA aborts, lets its
-// copies land, frees TMEM and flags the caller's status word.
-// Shapes: L divides 32, k2 k3 == l0 l1 (so a unit's K slice is 128 bf16
-// columns: two swizzle atoms), NA = nvec k2 k3 d and NB = nvec l0 l1 d
-// multiples of 16 up to 256, at most 8 S2_1 tags with terms.
+//   MMA-B   TMEM_B[128 x NB/VH] += S2_1[g] K-slice (TMA) . B_B part
+// TMEM_B accumulates over all units of the CTA and becomes one split-K plane.
+// Roles: warp 0 issues the step-A TMA loads, warp 18 the step-B slice loads,
+// warp 1 the MMA-A and warp 19 the MMA-B instructions (one elected lane
+// each), warps 2..17 run the fold, four per TMEM lane quadrant, in two teams
+// when TMEM_A is double-buffered.  In single-launch (cooperative) mode the
+// grid also packs Vin before the units and sums the planes into y after
+// them, between bounded grid barriers.  Every wait is bounded; on expiry the
+// CTA aborts, lets its copies land, frees TMEM and flags the caller's status
+// word.
+// Shapes: L divides 32 and is a multiple of 4, k2 k3 == l0 l1 (a unit's K
+// slice is 128 bf16 columns: two swizzle atoms), d in {1, 2, 4, 8}, NA = nvec
+// k2 k3 d and NB = nvec l0 l1 d multiples of 16 up to 256, at most 8 S2_1
+// tags with terms.
 // ---------------------------------------------------------------------------
 namespace {
 
-constexpr int FU_THREADS = 608;  // warps: 0 A loads, 1 MMA, 2..17 fold, 18 B loads
+constexpr int FU_THREADS = 640;  // warps: 0 A loads, 1 MMA-A, 2..17 fold, 18 B loads, 19 MMA-B
 constexpr int FU_MAXG = 8;
 constexpr int FU_STAGES = 4;
 constexpr int FU_STAGE_A = 128 * 128;        // A tile: 128 rows x 64 bf16
@@ -661,24 +668,19 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         for (uint32_t q = 0; q < (1u << 20); ++q)
           if (mbar_try_wait(aB_full, (uint32_t)((issued - 1) & 1))) break;
     }
-  } else if (warp == 1) {
-    // ---- MMA issuer.  Iteration uc issues MMA-A(uc) into TMEM_A buffer
-    // uc % nbuf, then MMA-B(uc - 1) once its fold is done: the tensor pipe
-    // works on unit uc while the epilogue warps fold unit uc - 1.  The whole
-    // warp runs the loop (its values stay warp-uniform) and one elected lane
-    // issues each MMA and commit; per MMA the descriptors only advance their
+  } else if (warp == 1 || warp == 19) {
+    // ---- MMA issuers: warp 1 issues every unit's MMA-A into TMEM_A buffer
+    // u % nbuf, warp 19 every unit's MMA-B once its fold is done, so that
+    // neither's waits hold up the other's MMAs.  Each warp runs its loop
+    // converged (its values stay warp-uniform) and one elected lane issues
+    // each MMA and commit; per MMA the descriptors only advance their
     // start-address field (bytes >> 4).
     const bool leader = elect_one();
-    const uint32_t idA = idesc_bf16_f32(128, p.NAh), idB = idesc_bf16_f32(128, p.NBh);
-    const uint64_t dStage = smem_desc_sw128(smem_u32(stage));
-    const uint64_t dAB = smem_desc_sw128(smem_u32(aB)), dBB = smem_desc_sw128(smem_u32(bB));
-    const uint32_t dStageStep = (uint32_t)p.stage_bytes >> 4, dPartB = (uint32_t)(p.NBh * 128) >> 4;
-    constexpr uint32_t dV = FU_STAGE_A >> 4, dAtomAB = FU_AB_ATOM >> 4, dAtomBB = FU_BB_ATOM >> 4;
     struct Unit {
       int b, part, pc;
       uint32_t bph;  // phase parity of the unit's use of TMEM_A buffer b
     };
-    auto advance = [&](Unit u) {
+    auto advance = [&](Unit& u) {
       if (++u.part == p.VH) {
         u.part = 0;
         ++u.pc;
@@ -687,66 +689,72 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         u.b = 0;
         u.bph ^= 1u;
       }
-      return u;
     };
-    auto step_b = [&](const Unit& u) -> bool {
-      // MMA-B of unit u: its fold wrote B_B part u.part; the pair's S2_1 slice is loaded
-      if (!mbar_wait_sleep(&bB_ready[u.b], u.bph, abort_flag)) return false;
-      if (u.part == 0 && !mbar_wait_sleep(aB_full, (uint32_t)(u.pc & 1), abort_flag)) return false;
-      tc_fence_after();
-      if (leader) {
-        const uint32_t d = tB + (uint32_t)(u.part * p.NBh);
-        const uint64_t bb = dBB + u.part * dPartB;
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(d, dAB + (h * dAtomAB + kk * 2), bb + (h * dAtomBB + kk * 2), idB,
-                     (u.pc > 0 || h > 0 || kk > 0) ? 1u : 0u);
-        mma_commit(&bB_free[u.part]);
-        if (u.part == p.VH - 1) mma_commit(aB_empty);
-      }
-      __syncwarp();
-      return true;
-    };
-    int s = 0;
-    PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
-    uint32_t ph = 0;
     bool ok = true;
-    Unit cur{0, 0, 0, 0u}, prev{0, 0, 0, 0u};
-    for (int uc = 0; ok && uc < n_units; ++uc) {
-      // TMEM_A buffer cur.b was last read by the fold of unit uc - nbuf: with
-      // two buffers step_b(uc - 2) of the previous iteration waited for it
-      if (p.nbuf == 1 && uc > 0 && !(ok = mbar_wait_sleep(&bB_ready[0], prev.bph, abort_flag))) break;
-      const uint32_t tA = tmem + (uint32_t)(cur.b * p.NAh);
-      const int nkb = p.nkb[cw.g];
-      for (int kb = 0; kb < nkb; ++kb) {
-        if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
+    Unit u{0, 0, 0, 0u};
+    if (warp == 1) {
+      const uint32_t idA = idesc_bf16_f32(128, p.NAh);
+      const uint64_t dStage = smem_desc_sw128(smem_u32(stage));
+      const uint32_t dStageStep = (uint32_t)p.stage_bytes >> 4;
+      constexpr uint32_t dV = FU_STAGE_A >> 4;
+      int s = 0;
+      PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+      uint32_t ph = 0;
+      for (int uc = 0; ok && uc < n_units; ++uc) {
+        // TMEM_A buffer u.b was last read by the fold of unit uc - nbuf
+        if (uc >= p.nbuf && !(ok = mbar_wait_sleep(&bB_ready[u.b], u.bph ^ 1u, abort_flag))) break;
+        const uint32_t tA = tmem + (uint32_t)(u.b * p.NAh);
+        const int nkb = p.nkb[cw.g];
+        for (int kb = 0; kb < nkb; ++kb) {
+          if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
+          tc_fence_after();
+          if (leader) {
+            const uint64_t da = dStage + s * dStageStep;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+              mma_bf16(tA, da + kk * 2, da + (dV + kk * 2), idA, (kb > 0 || kk > 0) ? 1u : 0u);
+            mma_commit(&empty[s]);
+          }
+          __syncwarp();
+          if (++s == p.stages) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (!ok) break;
+        if (leader) mma_commit(&accA_full[u.b]);
+        __syncwarp();
+        advance(u);
+        if (u.part == 0) cw.next();
+      }
+    } else {
+      const uint32_t idB = idesc_bf16_f32(128, p.NBh);
+      const uint64_t dAB = smem_desc_sw128(smem_u32(aB)), dBB = smem_desc_sw128(smem_u32(bB));
+      const uint32_t dPartB = (uint32_t)(p.NBh * 128) >> 4;
+      constexpr uint32_t dAtomAB = FU_AB_ATOM >> 4, dAtomBB = FU_BB_ATOM >> 4;
+      for (int uc = 0; ok && uc < n_units; ++uc) {
+        // MMA-B of unit uc: its fold wrote B_B part u.part; the pair's S2_1 slice is loaded
+        if (!(ok = mbar_wait_sleep(&bB_ready[u.b], u.bph, abort_flag))) break;
+        if (u.part == 0 && !(ok = mbar_wait_sleep(aB_full, (uint32_t)(u.pc & 1), abort_flag))) break;
         tc_fence_after();
         if (leader) {
-          const uint64_t da = dStage + s * dStageStep;
+          const uint32_t d = tB + (uint32_t)(u.part * p.NBh);
+          const uint64_t bb = dBB + u.part * dPartB;
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_bf16(tA, da + kk * 2, da + (dV + kk * 2), idA, (kb > 0 || kk > 0) ? 1u : 0u);
-          mma_commit(&empty[s]);
+          for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+              mma_bf16(d, dAB + (h * dAtomAB + kk * 2), bb + (h * dAtomBB + kk * 2), idB,
+                       (u.pc > 0 || h > 0 || kk > 0) ? 1u : 0u);
+          mma_commit(&bB_free[u.part]);
+          if (u.part == p.VH - 1) mma_commit(aB_empty);
         }
         __syncwarp();
-        if (++s == p.stages) {
-          s = 0;
-          ph ^= 1u;
-        }
+        advance(u);
       }
-      if (!ok) break;
-      if (leader) mma_commit(&accA_full[cur.b]);
+      if (leader) mma_commit(doneB);
       __syncwarp();
-      if (uc > 0 && !(ok = step_b(prev))) break;
-      prev = cur;
-      cur = advance(cur);
-      if (cur.part == 0) cw.next();
     }
-    if (ok && n_units > 0) ok = step_b(prev);
-    if (leader) mma_commit(doneB);
-    __syncwarp();
   } else if (warp >= 2 && warp <= 17) {
     // ---- fold epilogue: warps 2..17; quadrant = warp % 4.  With two vector
     // parts and two TMEM_A buffers the warps form two teams of 8 (team =
