@@ -569,13 +569,45 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   const uint32_t tmem = *tmem_slot;
   const uint32_t tB = tmem + 256;
 
-  if (threadIdx.x == 0 && blockIdx.x < p.n_pairs) {
-    // the first pair's S2_0 tiles and S2_1 slice into L2 while Vin is packed
-    const PairWalk w0((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
-    for (int kb = 0; kb < p.nkb[w0.g]; ++kb) tma_prefetch_2d(&maps.a[w0.g], kb * 64, w0.t * 128);
-    const int64_t k0 = (int64_t)w0.t * p.XP * p.K23;
-    tma_prefetch_2d(&maps.b, (int)(w0.g * p.regB + 2 * k0), 0);
-    tma_prefetch_2d(&maps.b, (int)(w0.g * p.regB + 2 * p.kcB + 2 * k0), 0);
+  // Loads that do not depend on Vin start before phase 0: the S2_0 tiles of
+  // the first `pre` step-A stages (their Vin parts follow after the barrier,
+  // on the same full barrier) and the first pair's S2_1 slice.
+  const int my_pairs0 = blockIdx.x < p.n_pairs ? (p.n_pairs - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  int pre = 0;
+  PairWalk cwB((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+  int issuedB = 0, pcB0 = 0;
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < p.G; ++q) {
+      prefetch_tensormap(&maps.a[q]);
+      prefetch_tensormap(&maps.vin[q]);
+    }
+    prefetch_tensormap(&maps.b);
+    PairWalk w((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+    for (int uc = 0, part = 0, kb = 0; pre < p.stages && uc < my_pairs0 * p.VH; ++pre) {
+      mbar_arrive_expect_tx(&full[pre], (uint32_t)(FU_STAGE_A + p.NAh * 128));
+      tma_load_2d(stage + pre * p.stage_bytes, &maps.a[w.g], kb * 64, w.t * 128, &full[pre]);
+      if (++kb == p.nkb[w.g]) {
+        kb = 0;
+        ++uc;
+        if (++part == p.VH) {
+          part = 0;
+          w.next();
+        }
+      }
+    }
+  } else if (threadIdx.x == 18 * 32 && my_pairs0 > 0) {
+    mbar_arrive_expect_tx(aB_full, (uint32_t)(2 * p.a_rows * 128));
+    const int64_t kk0 = (int64_t)cwB.t * p.XP * p.K23;
+    tma_load_2d(aB, &maps.b, (int)(cwB.g * p.regB + 2 * kk0), 0, aB_full);
+    tma_load_2d(aB + FU_AB_ATOM, &maps.b, (int)(cwB.g * p.regB + 2 * p.kcB + 2 * kk0), 0, aB_full);
+    issuedB = 1;
+    pcB0 = 1;
+    cwB.next();
+    if (my_pairs0 > 1) {
+      const int64_t kn = (int64_t)cwB.t * p.XP * p.K23;
+      tma_prefetch_2d(&maps.b, (int)(cwB.g * p.regB + 2 * kn), 0);
+      tma_prefetch_2d(&maps.b, (int)(cwB.g * p.regB + 2 * p.kcB + 2 * kn), 0);
+    }
   }
   if (p.coop) {
     // ---- phase 0: Vin of every term packed by the whole grid; the async
@@ -597,11 +629,6 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
   if (warp == 0) {
     if (lane == 0) {
       // ---- TMA producer of step A: the unit's S2_0 tile and its Vin part
-      for (int q = 0; q < p.G; ++q) {
-        prefetch_tensormap(&maps.a[q]);
-        prefetch_tensormap(&maps.vin[q]);
-      }
-      prefetch_tensormap(&maps.b);
       int issued = 0, s = 0, part = 0;
       uint32_t ph = 0;
       bool ok = true;
@@ -622,10 +649,12 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         if (part == 0) prefetch_pair();
         const int g = cw.g, t = cw.t, nkb = p.nkb[g];
         for (int kb = 0; kb < nkb; ++kb) {
-          if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
           uint8_t* st = stage + s * p.stage_bytes;
-          mbar_arrive_expect_tx(&full[s], (uint32_t)(FU_STAGE_A + p.NAh * 128));
-          tma_load_2d(st, &maps.a[g], kb * 64, t * 128, &full[s]);
+          if (issued >= pre) {  // (the first `pre` stages have their S2_0 tile requested)
+            if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
+            mbar_arrive_expect_tx(&full[s], (uint32_t)(FU_STAGE_A + p.NAh * 128));
+            tma_load_2d(st, &maps.a[g], kb * 64, t * 128, &full[s]);
+          }
           tma_load_2d(st + FU_STAGE_A, &maps.vin[g], kb * 64, part * p.NAh, &full[s]);
           ++issued;
           if (++s == p.stages) {
@@ -639,7 +668,10 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
         }
       }
       if (*abort_flag) {
-        // let copies already in flight land before the CTA exits (bounded)
+        // complete the early stages whose Vin part was never requested (any
+        // in-bounds box), then let copies in flight land (bounded)
+        for (; issued < pre; ++issued)
+          tma_load_2d(stage + issued * p.stage_bytes + FU_STAGE_A, &maps.vin[0], 0, 0, &full[issued]);
         for (int i = max(0, issued - p.stages); i < issued; ++i)
           for (uint32_t q = 0; q < (1u << 20); ++q)
             if (mbar_try_wait(&full[i % p.stages], (uint32_t)((i / p.stages) & 1))) break;
@@ -647,10 +679,11 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     }
   } else if (warp == 18) {
     if (lane == 0) {
-      // ---- TMA producer of step B's S2_1 slice, one per pair
-      int issued = 0;
-      PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
-      for (int pc = 0; pc < my_pairs; ++pc) {
+      // ---- TMA producer of step B's S2_1 slice, one per pair (pair 0's was
+      // requested before phase 0)
+      int issued = issuedB;
+      PairWalk cw = cwB;
+      for (int pc = pcB0; pc < my_pairs; ++pc) {
         if (!mbar_wait_sleep(aB_empty, (uint32_t)((pc & 1) ^ 1), abort_flag)) break;
         mbar_arrive_expect_tx(aB_full, (uint32_t)(2 * p.a_rows * 128));
         const int64_t kk0 = (int64_t)cw.t * p.XP * p.K23;
