@@ -69,6 +69,17 @@ def _round_up(a, b):
     return (a + b - 1) // b * b
 
 
+def _pad_b_rows(n):
+    """Padded rows of a tensor-core B operand (one power-of-two N tile up to
+    256, whole 256-row tiles above), as the library pads them."""
+    if n > 256:
+        return _round_up(n, 256)
+    t = 16
+    while t < n:
+        t *= 2
+    return t
+
+
 def tc_bytes_per_step(opr, nvec):
     """Algorithmic bytes each tensor-core phase must move per operator
     application, from the packed split-BF16 operand geometry: step A reads
@@ -85,9 +96,9 @@ def tc_bytes_per_step(opr, nvec):
         nt = len(terms)
         rows_a = _round_up(4 * x0 * x1 * l0 * l1, 128)
         reg_a = _round_up(4 * k0 * k1, 64)
-        rows_vin = _round_up(nvec * k2 * k3 * d, 16)
+        rows_vin = _pad_b_rows(nvec * k2 * k3 * d)
         reg_b = _round_up(4 * x0 * x1 * k2 * k3, 64)
-        rows_w = _round_up(nvec * l0 * l1 * d, 16)
+        rows_w = _pad_b_rows(nvec * l0 * l1 * d)
         kp_b = reg_b * len(groups)
         out["step_a"] += 2 * (rows_a * reg_a * nt + rows_vin * reg_a * nt + rows_w * kp_b)
         out["launches"]["step_a"] += len(groups)

@@ -107,17 +107,28 @@ struct Geo {
   int64_t kcB;
 };
 
+// Padded row count of a B operand (Vin, W): the GEMMs tile N by the largest
+// of 256/128/64/32/16 dividing it, and every N tile streams the whole A
+// operand again, so pad to one power-of-two tile up to 256 and to whole
+// 256-row tiles above (NA = 400 at D = 5 would otherwise run 25 tiles of 16).
+int64_t pad_b_rows(int64_t n) {
+  if (n > 256) return round_up(n, 256);
+  int64_t t = 16;
+  while (t < n) t *= 2;
+  return t;
+}
+
 Geo geometry(const S3& s, int nvec) {
   Geo g;
   g.MA = s.x0 * s.x1 * s.l0 * s.l1;
   g.NA = (int64_t)nvec * s.k2 * s.k3 * s.d;
   g.rowsA_a = round_up(4 * g.MA, 128);
   g.regA = round_up(4 * s.k0 * s.k1, 64);
-  g.rowsA_b = round_up(g.NA, 16);
+  g.rowsA_b = pad_b_rows(g.NA);
   g.kcB = s.x0 * s.x1 * s.k2 * s.k3;
   g.rowsB_a = round_up(4 * s.l2 * s.l3, 128);
   g.regB = round_up(4 * g.kcB, 64);
-  g.rowsB_b = round_up((int64_t)nvec * s.l0 * s.l1 * s.d, 16);
+  g.rowsB_b = pad_b_rows((int64_t)nvec * s.l0 * s.l1 * s.d);
   return g;
 }
 
