@@ -1026,10 +1026,13 @@ int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, co
   const int G = (int)tg.i1.size();
   const int64_t kpB = g.regB * G;
   const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
-  const int64_t pad_w = rows_valid_w * G * (g.regB - 4 * g.kcB) + (g.rowsB_b - rows_valid_w) * kpB;
+  // only the K padding of the valid rows needs zeros: a padding row of W
+  // (rows past nvec l0 l1 d, there to fill the N tile) feeds only its own
+  // output column, which the reduction never reads
+  const int64_t pad_w = rows_valid_w * G * (g.regB - 4 * g.kcB);
   if (pad_w > 0) {
     clear_w_padding_kernel<<<grid_of(pad_w), 256, 0, stream>>>(reinterpret_cast<__nv_bfloat16*>(w.w_pk), rows_valid_w,
-                                                              g.rowsB_b, 4 * g.kcB, g.regB, G);
+                                                              rows_valid_w, 4 * g.kcB, g.regB, G);
     CARC_CHECK_LAUNCH();
   }
   // step A per group: W_g = sum_{t in g} S2_0[i0_t] . Vin_t, folded straight into region g of the step-B operand
