@@ -1527,6 +1527,28 @@ __global__ void small_eig_min_real_kernel(int k, const double2* __restrict__ A0,
     nr = sqrt(nr);
     for (int i = 0; i < k; ++i) y[i] = cscale(y[i], 1.0 / nr);
   }
+  // LAPACK's convention for eigenvectors of a general matrix (unit norm, the
+  // first component of largest modulus real and positive), which the
+  // reference's projected solve inherits: the Ritz vector's phase then
+  // follows the current iterate, so repeated solves of a converged state
+  // return the same vector
+  {
+    int imax = 0;
+    double amax = -1.0;
+    for (int i = 0; i < k; ++i) {
+      const double a = cabs2(y[i]);
+      if (a > amax) {
+        amax = a;
+        imax = i;
+      }
+    }
+    if (amax > 0.0) {
+      const double m = sqrt(amax);
+      const double2 ph = make_double2(y[imax].x / m, -y[imax].y / m);  // conj(y_max) / |y_max|
+      for (int i = 0; i < k; ++i) y[i] = cmul(y[i], ph);
+      y[imax].y = 0.0;
+    }
+  }
   for (int i = 0; i < k; ++i) vec_out[i] = y[i];
   *lam_out = lam;
 }

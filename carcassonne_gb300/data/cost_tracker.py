@@ -32,6 +32,10 @@ class CostTracker(Data):
         assert len(self.shape) == 0
         return self
 
+    def transpose(self, *perm):
+        perm = perm[0] if len(perm) == 1 and isinstance(perm[0], (tuple, list)) else perm
+        return CostTracker(tuple(self.shape[i] for i in perm), self.cost)
+
     def join(self, *groups):
         groups = [[g] if isinstance(g, (int, np.integer)) else list(g) for g in groups]
         return CostTracker(tuple(int(np.prod([self.shape[i] for i in g], dtype=np.int64)) for g in groups), self.cost)

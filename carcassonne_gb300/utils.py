@@ -112,6 +112,20 @@ def computeNewDimension(old_dimension, by=None, to=None):
 
 
 # -- random samples (utils.py:254-255, :795-796) -----------------------------
+def buildProductTensor(*factors):
+    """Outer product of the factors as a complex128 numpy array (utils.py:241-243)."""
+    from functools import reduce
+    return reduce(np.multiply.outer, (np.asarray(f, dtype=np.complex128) for f in factors))
+
+
+def buildTensor(dimensions, components):
+    """Zero complex128 array with the given {index: value} components (utils.py:244-249)."""
+    t = np.zeros(dimensions, dtype=np.complex128)
+    for index, value in components.items():
+        t[index] = value
+    return t
+
+
 def crand(*shape):
     return np.random.rand(*shape) * 2 - 1 + np.random.rand(*shape) * 2j - 1j
 
@@ -188,5 +202,6 @@ __all__ = [
     "DimensionMismatchError", "InvariantViolatedError", "RelaxFailed", "UnexpectedTensorRankError",
     "Multiplier", "prepend", "Pauli", "O", "L", "R", "A", "OA", "LA", "RA", "dropAt", "replaceAt",
     "computeNewDimension", "crand", "randomComplexSample", "checkForNaNsIn", "multiplyBySingleSiteOperator",
+    "buildProductTensor", "buildTensor",
     "maximumNewBandwidth", "relaxOver", "unitize", "computeCompressor", "computeCompressorForMatrixTimesItsDagger",
 ]

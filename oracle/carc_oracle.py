@@ -701,3 +701,34 @@ class OracleSystem:
             self.corners[corner_id] = mo(lambda x: absorb_matrix_at(absorb_matrix_at(x, 3, P), 4, P.conj()), self.corners[corner_id])
             self.sides[corner_id] = mo(lambda x: absorb_matrix_at(absorb_matrix_at(x, 0, P.conj()), 1, P), self.sides[corner_id])
         return P
+
+
+# ---------------------------------------------------------------------------
+# 1D chain (tensors/_1d.py:12-93); index letters as in the GPU contractors:
+# environments [o, s, t] (operator, ket, bra bonds), O[o_l, o_r, p, q],
+# S[s_l, s_r, q], Sc = conj(S)
+# ---------------------------------------------------------------------------
+def chain_absorb_oss_left(L, O, S, Sc):                 # tensors/_1d.py:12-25
+    return np.einsum("xyz,oxpq,syq,tzp->ost", L, O, S, Sc)
+
+
+def chain_absorb_oss_right(R, O, S, Sc):                # tensors/_1d.py:26-39
+    return np.einsum("xyz,xopq,ysq,ztp->ost", R, O, S, Sc)
+
+
+def chain_absorb_ss_left(L, S, Sc):                     # tensors/_1d.py:40-49
+    return np.einsum("yz,syp,tzp->st", L, S, Sc)
+
+
+def chain_absorb_ss_right(R, S, Sc):                    # tensors/_1d.py:50-59
+    return np.einsum("yz,ysp,ztp->st", R, S, Sc)
+
+
+def chain_multiply(R, L, O, S):                         # tensors/_1d.py:61-93 (multiply)
+    return np.einsum("xar,ubl,xuoq,abq->rlo", R, L, O, S)
+
+
+def chain_form_matrix(R, L, O):                         # tensors/_1d.py:61-93 (formMatrix)
+    m = np.einsum("xar,ubl,xuoq->rloabq", R, L, O)
+    n = R.shape[2] * L.shape[2] * O.shape[2]
+    return m.reshape(n, -1)

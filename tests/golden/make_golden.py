@@ -306,9 +306,49 @@ def numerics():
     np.savez_compressed(os.path.join(HERE, "numerics.npz"), **out)
 
 
+def chain1d():
+    """The 1D chain (tensors/_1d.py, system/_1d.py): the four environment
+    absorptions, the expectation multiplier and its matrix on random tensors,
+    and one-site / total expectations of transverse-Ising and field systems."""
+    if not hasattr(np, "product"):
+        np.product = np.prod  # the reference's numpy 1 spelling
+    from carcassonne.tensors import _1d as r1
+    from carcassonne.system._1d import System as System1D
+    from carcassonne.utils import buildTensor, Pauli
+    rng = np.random.default_rng(20260104)
+    out = {}
+    for case, (o, sd, p) in enumerate([(1, 1, 2), (2, 3, 2), (3, 4, 3), (4, 2, 5)]):
+        L, R = cn(rng, o, sd, sd), cn(rng, o, sd, sd)
+        O, S = cn(rng, o, o, p, p), cn(rng, sd, sd, p)
+        L2, R2 = cn(rng, sd, sd), cn(rng, sd, sd)
+        Sc = S.conj()
+        out[f"c{case}_L"], out[f"c{case}_R"], out[f"c{case}_O"], out[f"c{case}_S"] = L, R, O, S
+        out[f"c{case}_L2"], out[f"c{case}_R2"] = L2, R2
+        out[f"c{case}_ossL"] = r1.absorbCenterOSSIntoLeftEnvironment(D(L), D(O), D(S), D(Sc)).toArray().copy()
+        out[f"c{case}_ossR"] = r1.absorbCenterOSSIntoRightEnvironment(D(R), D(O), D(S), D(Sc)).toArray().copy()
+        out[f"c{case}_ssL"] = r1.absorbCenterSSIntoLeftEnvironment(D(L2), D(S), D(Sc)).toArray().copy()
+        out[f"c{case}_ssR"] = r1.absorbCenterSSIntoRightEnvironment(D(R2), D(S), D(Sc)).toArray().copy()
+        # the multiplier acts on states of shape (R.shape[1], L.shape[1], O.shape[2])
+        m = r1.formExpectationMultiplier(D(R), D(L), D(O))
+        out[f"c{case}_y"] = m(D(S)).toArray().copy()
+        out[f"c{case}_M"] = m.formMatrix().toArray().copy()
+        out[f"c{case}_cost"] = np.array([m.cost_of_multiply, m.cost_of_formMatrix])
+    mpo_ti = lambda h: buildTensor((3, 3, 2, 2), {(0, 0): Pauli.I, (0, 2): h * Pauli.Z, (0, 1): -0.01 * Pauli.X,  # noqa: E731
+                                                   (1, 2): Pauli.X, (2, 2): Pauli.I})
+    for case, (h, sd) in enumerate([(1.0, 2), (0.5, 3), (2.0, 4)]):
+        S, rb, lb = cn(rng, sd, sd, 2), cn(rng, sd), cn(rng, sd)
+        system = System1D([1, 0, 0], [0, 0, 1], mpo_ti(h), S.copy(), rb.copy(), lb.copy())
+        out[f"e{case}_h"], out[f"e{case}_S"], out[f"e{case}_rb"], out[f"e{case}_lb"] = np.array(h), S, rb, lb
+        out[f"e{case}_E"] = np.array(complex(system.computeExpectation()))
+        out[f"e{case}_one"] = np.array(complex(system.computeOneSiteExpectation()))
+    np.savez_compressed(os.path.join(HERE, "chain1d.npz"), **out)
+
+
 if __name__ == "__main__":
-    dense_cases()
-    tables_and_trajectories()
-    numerics()
-    for fn in ("dense.npz", "tables.json", "trajectory.npz", "numerics.npz"):
-        print(fn, os.path.getsize(os.path.join(HERE, fn)))
+    sections = dict(dense=dense_cases, tables=tables_and_trajectories, numerics=numerics, chain1d=chain1d)
+    chosen = sys.argv[1:] or list(sections)
+    for name in chosen:
+        sections[name]()
+    for fn in ("dense.npz", "tables.json", "trajectory.npz", "numerics.npz", "chain1d.npz"):
+        if os.path.exists(os.path.join(HERE, fn)):
+            print(fn, os.path.getsize(os.path.join(HERE, fn)))

@@ -12,6 +12,12 @@ pytestmark = pytest.mark.gpu
 
 def _run(system, bandwidth_policy):
     from carcassonne_gb300 import policies as P
+    count = [0]
+
+    def cap(system):  # ends a run that does not converge
+        count[0] += 1
+        assert count[0] <= 200, "no convergence after 200 optimizations"
+    system.setPolicy("post-optimization hook", P.HookPolicy(cap))
     system.setPolicy("state compression", P.ConstantStateCompressionPolicy(1))
     system.setPolicy("sweep convergence", P.RelativeOneSiteExpectationDifferenceThresholdConvergencePolicy(1e-7))
     system.setPolicy("run convergence", P.RelativeOneSiteExpectationDifferenceThresholdConvergencePolicy(1e-7))
