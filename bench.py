@@ -438,10 +438,8 @@ def main():
     torch.cuda.synchronize()
     e_ms = sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)) / args.steps
 
-    if dist:
-        t = torch.tensor([ms, e_ms], dtype=torch.float64, device=x.device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms, e_ms = float(t[0]), float(t[1])
+    from carcassonne_gb300.replicas import max_over_ranks
+    ms, e_ms = max_over_ranks([ms, e_ms], dist, device=x.device)
     value = world * flops_per_step / (ms * 1e-3) / 1e9
     e2e_value = world * flops_per_step / (e_ms * 1e-3) / 1e9
     if rank != 0:

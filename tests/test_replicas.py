@@ -1,0 +1,66 @@
+"""Replicas and sharding of independent problems over ranks: the cost-based
+schedule, and the control-plane collectives (max of per-rank times, gather of
+per-rank results) on two gloo ranks on the CPU."""
+import os
+import socket
+
+import pytest
+import torch.multiprocessing as mp
+
+from carcassonne_gb300.replicas import gather_to_root, max_over_ranks, problem_cost, shard_by_cost
+
+
+def test_shard_by_cost_is_a_balanced_partition():
+    from carcassonne_gb300 import batched
+    specs = batched.sample_problems(32, 3)
+    costs = [problem_cost(D, chi) for D, chi, _, _ in specs]
+    for world in (1, 2, 3, 8):
+        shards = shard_by_cost(costs, world)
+        assert sorted(i for s in shards for i in s) == list(range(len(costs)))
+        loads = [sum(costs[i] for i in s) for s in shards]
+        # LPT bound: no rank exceeds the mean by more than the largest job
+        assert max(loads) <= sum(costs) / world + max(costs)
+    assert shard_by_cost(costs, 2) == shard_by_cost(list(costs), 2)  # deterministic
+
+
+def test_shard_by_cost_rejects_empty_world():
+    with pytest.raises(ValueError):
+        shard_by_cost([1, 2], 0)
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank_main(rank, world, port, out_path):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        # rank r "measured" (r + 1) ms and 10 (r + 1) ms
+        ms = max_over_ranks([1.0 + rank, 10.0 * (1 + rank)], dist)
+        costs = [problem_cost(D, chi) for D, chi in [(6, 96), (2, 16), (5, 40), (4, 64), (3, 88)]]
+        mine = shard_by_cost(costs, world)[rank]
+        got = gather_to_root({"rank": rank, "problems": mine, "ms": ms}, dist, rank, world)
+        if rank == 0:
+            import json
+            with open(out_path, "w") as f:
+                json.dump(got, f)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_two_gloo_ranks(tmp_path):
+    out = tmp_path / "gathered.json"
+    mp.spawn(_rank_main, args=(2, _free_port(), str(out)), nprocs=2, join=True)
+    import json
+    got = json.loads(out.read_text())
+    assert [g["rank"] for g in got] == [0, 1]
+    assert all(g["ms"] == [2.0, 20.0] for g in got)           # the slowest rank's times everywhere
+    assigned = sorted(i for g in got for i in g["problems"])
+    assert assigned == list(range(5))                          # every problem on exactly one rank
