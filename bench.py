@@ -70,7 +70,7 @@ def _round_up(a, b):
 
 
 def _pad_b_rows(n):
-    """Padded rows of a tensor-core B operand (one power-of-two N tile up to
+    """Padded rows of step A's B operand, Vin (one power-of-two N tile up to
     256, whole 256-row tiles above), as the library pads them."""
     if n > 256:
         return _round_up(n, 256)
@@ -78,6 +78,21 @@ def _pad_b_rows(n):
     while t < n:
         t *= 2
     return t
+
+
+def _gemm_pad_n(n):
+    """Padded rows of W, step B's B operand: ceil(n / 256) equal N tiles of
+    a multiple of 16, as the library pads it."""
+    nt = -(-n // 256)
+    return nt * _round_up(-(-n // nt), 16)
+
+
+def _gemm_tile_n(n):
+    """The N tile the plain tensor-core GEMM takes for a B operand of n rows."""
+    nt = -(-n // 256)
+    if n % nt == 0 and (n // nt) % 16 == 0:
+        return n // nt
+    return next(b for b in (256, 128, 64, 32, 16) if n % b == 0)
 
 
 def tc_bytes_per_step(opr, nvec):
@@ -98,13 +113,13 @@ def tc_bytes_per_step(opr, nvec):
         reg_a = _round_up(4 * k0 * k1, 64)
         rows_vin = _pad_b_rows(nvec * k2 * k3 * d)
         reg_b = _round_up(4 * x0 * x1 * k2 * k3, 64)
-        rows_w = _pad_b_rows(nvec * l0 * l1 * d)
+        rows_w = _gemm_pad_n(nvec * l0 * l1 * d)
         kp_b = reg_b * len(groups)
         out["step_a"] += 2 * (rows_a * reg_a * nt + rows_vin * reg_a * nt + rows_w * kp_b)
         out["launches"]["step_a"] += len(groups)
         live_b = 4 * l2 * l3
         rows_sb = _round_up(live_b, 128)
-        bn = next(b for b in (256, 128, 64, 32, 16) if rows_w % b == 0)
+        bn = _gemm_tile_n(rows_w)
         tiles = (rows_sb // 128) * (rows_w // bn)
         kb = kp_b // 64
         ks_b = max(1, min(1 if tiles >= 152 else 152 // tiles, kb))
@@ -119,7 +134,7 @@ def tc_bytes_per_step(opr, nvec):
         units = (x0 * x1 * l0 * l1 // 32) * len(groups)
         grid = max(1, min(152, units))
         out["fused"] = out.get("fused", 0) + 2 * (rows_a * reg_a * nt + rows_vin * reg_a * nt + live_rows * kp_b) \
-            + 4 * grid * _round_up(live_b, 32) * rows_w
+            + 4 * grid * _round_up(live_b, 32) * nvec * l0 * l1 * d
         out["launches"]["fused"] = out["launches"].get("fused", 0) + 1
     return out
 

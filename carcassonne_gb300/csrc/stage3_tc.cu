@@ -107,10 +107,14 @@ struct Geo {
   int64_t kcB;
 };
 
-// Padded row count of a B operand (Vin, W): the GEMMs tile N by the largest
-// of 256/128/64/32/16 dividing it, and every N tile streams the whole A
-// operand again, so pad to one power-of-two tile up to 256 and to whole
-// 256-row tiles above (NA = 400 at D = 5 would otherwise run 25 tiles of 16).
+// Padded row count of step A's B operand (Vin): the folding GEMM tiles N by
+// the largest of 256/128/64/32/16 dividing it, and every N tile streams the
+// whole A operand again, so pad to one power-of-two tile up to 256 and to
+// whole 256-row tiles above (NA = 400 at D = 5 would otherwise run 25 tiles
+// of 16).  W, step B's B operand, is padded by gemm_pad_n instead: the plain
+// GEMM takes any tile width that is a multiple of 16, so 400 rows become two
+// tiles of 208 (not 512 rows) and 576 three of 192 (not 768), and step B,
+// which streams W from HBM, reads that much less.
 int64_t pad_b_rows(int64_t n) {
   if (n > 256) return round_up(n, 256);
   int64_t t = 16;
@@ -128,7 +132,7 @@ Geo geometry(const S3& s, int nvec) {
   g.kcB = s.x0 * s.x1 * s.k2 * s.k3;
   g.rowsB_a = round_up(4 * s.l2 * s.l3, 128);
   g.regB = round_up(4 * g.kcB, 64);
-  g.rowsB_b = pad_b_rows((int64_t)nvec * s.l0 * s.l1 * s.d);
+  g.rowsB_b = gemm_pad_n((int64_t)nvec * s.l0 * s.l1 * s.d);
   return g;
 }
 
@@ -217,7 +221,8 @@ int choose_ksplit(int64_t tiles, int64_t kp) {
   return (int)ks;
 }
 
-int bn_for(int64_t n) { return n % 256 == 0 ? 256 : n % 128 == 0 ? 128 : n % 64 == 0 ? 64 : n % 32 == 0 ? 32 : 16; }
+// N tile the plain GEMM uses for a B operand of n rows
+int bn_for(int64_t n) { return gemm_tile_n((int)n); }
 
 // plan layout: [per group g: S2_0 step-A operand, rowsA_a x (regA * |T_g|)] [S2_1 step-B operand, rowsB_a x (regB * G)]
 int64_t plan_bytes_for(const Geo& g1, const TermGroups& tg) {
@@ -1331,7 +1336,7 @@ FormGeo form_geometry(const S3& s, int max_terms) {
   f.M = s.l0 * s.l1 * s.k0 * s.k1;
   f.N = s.l2 * s.l3 * s.k2 * s.k3;
   f.rows_a = round_up(4 * f.M, 128);
-  f.rows_b = round_up(f.N, 16);
+  f.rows_b = gemm_pad_n(f.N);
   f.region = round_up(4 * s.x0 * s.x1, 64);
   f.max_terms = max_terms;
   f.kp_max = f.region * max_terms;

@@ -36,25 +36,25 @@ constexpr int A_STAGE_BYTES = BM * BK * 2;
 
 __host__ __device__ constexpr int tmem_cols_for(int bn) { return bn <= 32 ? 32 : (bn <= 64 ? 64 : (bn <= 128 ? 128 : 256)); }
 
-// Pipeline depth: the plain GEMM streams long K ranges (4 stages, one CTA
-// per SM); the folding GEMM has short K and a long epilogue, so it keeps two
-// stages and fits two CTAs per SM, one CTA's epilogue overlapping the other's
-// loads and MMAs.
-__host__ __device__ constexpr int stages_for(int epi) { return epi ? 2 : 4; }
+// The plain GEMM streams long K ranges: 4 pipeline stages, one CTA per SM.
+constexpr int STAGES = 4;
 
-template <int BN, int EPI>
+template <int BN>
 constexpr int smem_bytes() {
-  return 1024 + stages_for(EPI) * (A_STAGE_BYTES + BN * BK * 2) + 256;
+  return 1024 + STAGES * (A_STAGE_BYTES + BN * BK * 2) + 256;
 }
 
 // ---- folding epilogue --------------------------------------------------------
 // The tile's accumulator is 128 rows (4m + 2c + s: complex row m, re/im c,
 // hi/lo s) x BN columns n.  It is staged HC columns at a time as FP32 with a
-// row pitch of HC + 4 floats (conflict-free float4 stores).  After the staged
-// block come two index tables: per complex row m of the tile {row part, k part}
-// of the destination (or -1), and per slot q {n_local, row part, k part,
-// valid}, slots in p-major order so that consecutive slots walk (vec, k2, k3),
-// i.e. consecutive destination k.
+// row pitch of HC + 4 floats (conflict-free float4 stores), the columns in
+// slot order: when the physical dimension d is 2, 4 or 8 (and HC >= 32),
+// p-major (slot (n % d) HC/d + n / d), so that consecutive slots walk (vec,
+// k2, k3), i.e. consecutive destination k, and consecutive lanes read
+// consecutive words; otherwise in column order.  After the staged block come
+// two index tables: per complex row m of the tile the destination offset of
+// its (row part, k part) in bf16 pairs, row part x pitch + k part (-1: past
+// M), and per slot {row part, k part} (row part -1: past N).
 template <int BN>
 __host__ __device__ constexpr int FOLD_HC() { return BN == 256 ? 128 : (BN == 128 ? 64 : BN); }
 
@@ -62,83 +62,127 @@ template <int BN>
 __host__ __device__ constexpr int FOLD_PITCH() { return FOLD_HC<BN>() + 4; }
 
 template <int BN>
-__host__ __device__ constexpr int fold_smem_bytes() { return 128 * FOLD_PITCH<BN>() * 4 + 32 * 8 + FOLD_HC<BN>() * 16; }
+__host__ __device__ constexpr int fold_smem_bytes() { return 128 * FOLD_PITCH<BN>() * 4 + 32 * 8 + FOLD_HC<BN>() * 8; }
+
+// slot-order stride: d when the staged columns are p-major, 1 otherwise
+template <int BN>
+__device__ __forceinline__ int fold_ds(int64_t d) {
+  constexpr int HC = FOLD_HC<BN>();
+  return (HC >= 32 && (d == 2 || d == 4 || d == 8)) ? (int)d : 1;
+}
+
+// one lane's 32 accumulator columns [c0, c0 + 32) of its row into slot order
+template <int BN, int DS>
+__device__ __forceinline__ void fold_stage(float* row, int c0, const uint32_t* r) {
+  constexpr int HC = FOLD_HC<BN>();
+  if constexpr (HC < 32 || DS == 1) {
+#pragma unroll
+    for (int j = 0; j < 32; j += 4) {
+      if (c0 + j >= HC) break;
+      *reinterpret_cast<float4*>(row + c0 + j) = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
+                                                             __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]));
+    }
+  } else {
+    // column c0 + p + DS i goes to slot p HC/DS + c0/DS + i
+#pragma unroll
+    for (int p = 0; p < DS; ++p) {
+#pragma unroll
+      for (int i = 0; i < 32 / DS; i += 4) {
+        *reinterpret_cast<float4*>(row + p * (HC / DS) + c0 / DS + i) =
+            make_float4(__uint_as_float(r[p + DS * i]), __uint_as_float(r[p + DS * (i + 1)]),
+                        __uint_as_float(r[p + DS * (i + 2)]), __uint_as_float(r[p + DS * (i + 3)]));
+      }
+    }
+  }
+}
 
 template <int BN>
-__device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0, int nb, int tid, int nthreads) {
+__device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0, int nb, int ds, int tid,
+                                            int nthreads) {
   constexpr int HC = FOLD_HC<BN>();
-  int2* tabM = reinterpret_cast<int2*>(sP + 128 * FOLD_PITCH<BN>());
-  int4* tabN = reinterpret_cast<int4*>(tabM + 32);
+  long long* tabM = reinterpret_cast<long long*>(sP + 128 * FOLD_PITCH<BN>());
+  int2* tabN = reinterpret_cast<int2*>(tabM + 32);
   const int L0 = (int)fe.l0, L1 = (int)fe.l1, X1 = (int)fe.x1, K2 = (int)fe.k2, K3 = (int)fe.k3, Dp = (int)fe.d;
+  const long long pitch2 = fe.pitch >> 1;
   for (int i = tid; i < 32; i += nthreads) {
     const int64_t m = (int64_t)(m0 >> 2) + i;
-    int2 t = make_int2(-1, 0);
+    long long t = -1;
     if (m < fe.M) {
       int r = (int)m;
       const int ll1 = r % L1; r /= L1;
       const int ll0 = r % L0; r /= L0;
       const int xx1 = r % X1; r /= X1;
-      t = make_int2((ll0 * L1 + ll1) * Dp, (r * X1 + xx1) * K2 * K3);
+      t = (long long)((ll0 * L1 + ll1) * Dp) * pitch2 + (long long)(r * X1 + xx1) * K2 * K3;
     }
     tabM[i] = t;
   }
-  const bool pmajor = (HC % Dp) == 0 && (nb % Dp) == 0;
+  const int per = HC / ds;
   for (int q = tid; q < HC; q += nthreads) {
-    const int nl = pmajor ? (q % (HC / Dp)) * Dp + q / (HC / Dp) : q;
+    const int nl = (q % per) * ds + q / per;
     const int64_t n = (int64_t)nb + nl;
-    int4 t = make_int4(nl, 0, 0, 0);
+    int2 t = make_int2(-1, 0);
     if (n < fe.N) {
       int r = (int)n;
       const int p = r % Dp; r /= Dp;
       const int k3 = r % K3; r /= K3;
       const int k2 = r % K2; r /= K2;
-      t = make_int4(nl, r * L0 * L1 * Dp + p, k2 * K3 + k3, 1);
+      t = make_int2(r * L0 * L1 * Dp + p, k2 * K3 + k3);
     }
     tabN[q] = t;
   }
 }
 
 // W[m, n] = (P[4m] + P[4m+1]) + i (P[4m+2] + P[4m+3]), split into bf16 hi/lo
-// pairs; consecutive threads store consecutive k of one destination row.
+// pairs.  Warp w of nw (nw a multiple of the HC/32 slot groups) takes slot
+// group w % (HC/32) and every (nw / (HC/32))-th complex row: each lane keeps
+// its slot's destination in registers, reads one consecutive staged word per
+// row and stores consecutive k of one destination row with its neighbours.
 template <int BN>
-__device__ __forceinline__ void fold_write(const float* sP, const FoldEpi& fe) {
+__device__ __forceinline__ void fold_write(const float* sP, const FoldEpi& fe, int warp, int nw) {
   constexpr int HC = FOLD_HC<BN>();
-  const int2* tabM = reinterpret_cast<const int2*>(sP + 128 * FOLD_PITCH<BN>());
-  const int4* tabN = reinterpret_cast<const int4*>(tabM + 32);
-  uint32_t* W = static_cast<uint32_t*>(fe.dst);  // bf16 pairs; pitch, col_off and kc are even
-  const int64_t pitch2 = fe.pitch >> 1, off2 = fe.col_off >> 1;
+  constexpr int PITCH = FOLD_PITCH<BN>();
+  constexpr int JQ = (HC + 31) / 32;  // 32-slot groups per row
+  const long long* tabM = reinterpret_cast<const long long*>(sP + 128 * PITCH);
+  const int2* tabN = reinterpret_cast<const int2*>(tabM + 32);
+  const int lane = threadIdx.x & 31;
+  const int q = (warp % JQ) * 32 + lane;
+  const int rstep = nw / JQ;
+  if (q >= HC) return;
+  const int2 tn = tabN[q];
+  if (tn.x < 0) return;
+  // bf16 (re, im) pairs; pitch and col_off are even
+  uint32_t* Wq = static_cast<uint32_t*>(fe.dst) + (fe.col_off >> 1) + (int64_t)tn.x * (fe.pitch >> 1) + tn.y;
   const int kc = (int)fe.kc;
+  const float* col = sP + q;
 #pragma unroll 4
-  for (int e = threadIdx.x; e < 32 * HC; e += blockDim.x) {
-    const int ml = e / HC;
-    const int2 tm = tabM[ml];
-    const int4 tn = tabN[e % HC];
-    if (tm.x < 0 || tn.w == 0) continue;
-    const float* col = sP + 4 * ml * FOLD_PITCH<BN>() + tn.x;
-    const float re = col[0] + col[FOLD_PITCH<BN>()];
-    const float im = col[2 * FOLD_PITCH<BN>()] + col[3 * FOLD_PITCH<BN>()];
+  for (int ml = warp / JQ; ml < 32; ml += rstep) {
+    const long long off = tabM[ml];
+    if (off < 0) continue;
+    const float* c = col + 4 * ml * PITCH;
+    const float re = c[0] + c[PITCH];
+    const float im = c[2 * PITCH] + c[3 * PITCH];
     const __nv_bfloat162 h2 = __floats2bfloat162_rn(re, im);
     const float2 hf = __bfloat1622float2(h2);
     const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
-    uint32_t* rowp = W + (int64_t)(tn.y + tm.x) * pitch2 + off2 + (tm.y + tn.z);
+    uint32_t* rowp = Wq + off;
     rowp[0] = *reinterpret_cast<const uint32_t*>(&h2);
     rowp[kc] = *reinterpret_cast<const uint32_t*>(&l2);
   }
 }
 
-template <int BN, int EPI>
-__global__ __launch_bounds__(THREADS, EPI ? 2 : 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
-                                                                   const __grid_constant__ CUtensorMap tmB,
-                                                                   float* __restrict__ out, int64_t ld_out,
-                                                                   int64_t split_stride, int kb_per_split,
-                                                                   int kb_total, int a_rows, int* __restrict__ err,
-                                                                   const __grid_constant__ FoldEpi fe) {
+// Plain GEMM: out[z][m][n] = sum over split z's K blocks of A[m,:] . B[n,:].
+// The N tile is bn: BN, or (on the BN = 256 instance) any multiple of 16 up
+// to 256 chosen at run time; shared-memory stages and TMEM are sized for BN.
+template <int BN>
+__global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                                  const __grid_constant__ CUtensorMap tmB,
+                                                                  float* __restrict__ out, int64_t ld_out,
+                                                                  int64_t split_stride, int kb_per_split,
+                                                                  int kb_total, int a_rows, int* __restrict__ err,
+                                                                  int bn) {
   using namespace umma;
   constexpr int B_STAGE_BYTES = BN * BK * 2;
   constexpr uint32_t TMEM_COLS = tmem_cols_for(BN);
-  constexpr int STAGES = stages_for(EPI);
-  static_assert(EPI == 0 || fold_smem_bytes<BN>() <= STAGES * (A_STAGE_BYTES + B_STAGE_BYTES),
-                "the staged tile must fit in the pipeline stages");
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
@@ -150,7 +194,7 @@ __global__ __launch_bounds__(THREADS, EPI ? 2 : 1) void gemm_bf16_tn_kernel(cons
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * bn;
   const int kb0 = blockIdx.z * kb_per_split;
   const int kb1 = min(kb_total, kb0 + kb_per_split);
   const int nkb = max(0, kb1 - kb0);
@@ -189,7 +233,7 @@ __global__ __launch_bounds__(THREADS, EPI ? 2 : 1) void gemm_bf16_tn_kernel(cons
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)((i / STAGES) & 1);
         if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag)) break;
-        mbar_arrive_expect_tx(&full[s], (uint32_t)(a_rows * BK * 2 + B_STAGE_BYTES));
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(a_rows * BK * 2 + bn * BK * 2));
         const int kx = (kb0 + i) * BK;
         tma_load_2d(sA + s * A_STAGE_BYTES, &tmA, kx, m0, &full[s]);
         tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, kx, n0, &full[s]);
@@ -207,7 +251,7 @@ __global__ __launch_bounds__(THREADS, EPI ? 2 : 1) void gemm_bf16_tn_kernel(cons
   } else if (warp == 1) {
     if (lane == 0) {
       // single-thread MMA issuer
-      const uint32_t idesc = idesc_bf16_f32(BM, BN);
+      const uint32_t idesc = idesc_bf16_f32(BM, bn);
       for (int i = 0; i < nkb; ++i) {
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)((i / STAGES) & 1);
@@ -226,24 +270,25 @@ __global__ __launch_bounds__(THREADS, EPI ? 2 : 1) void gemm_bf16_tn_kernel(cons
       mma_commit(done);
     }
   } else {
-    // epilogue: warps 2..5 own TMEM lane quadrants (warp % 4)
+    // epilogue: warps 2..5 own TMEM lane quadrants (warp % 4); they wait for
+    // the whole main loop, suspended in hardware so that they take no issue
+    // slots from the producer and the MMA issuer
     const int quad = warp & 3;
-    const bool ok = mbar_wait(done, 0, abort_flag);
+    const bool ok = mbar_wait_sleep(done, 0, abort_flag);
     tc_fence_after();
-    if (EPI == 1) {
-      // the folding epilogue runs below, after the CTA-wide barrier
-    } else if (ok) {
+    if (ok) {
       const int row = m0 + quad * 32 + lane;
       float* dst = out + (int64_t)blockIdx.z * split_stride + (int64_t)row * ld_out + n0;
 #pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
+      for (int c0 = 0; c0 < bn; c0 += 32) {
         uint32_t r[32];
         tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
         tmem_ld_wait();
-        // BN = 16 tiles read 32 allocated columns but own only the first 16
+        // a tile whose width is not a multiple of 32 reads allocated columns
+        // past it but stores only its own
 #pragma unroll
         for (int j = 0; j < 32; j += 4) {
-          if (c0 + j >= BN) break;
+          if (c0 + j >= bn) break;
           *reinterpret_cast<float4*>(dst + c0 + j) =
               nkb > 0 ? make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
                                     __uint_as_float(r[j + 3]))
@@ -254,41 +299,213 @@ __global__ __launch_bounds__(THREADS, EPI ? 2 : 1) void gemm_bf16_tn_kernel(cons
   }
   tc_fence_before();
   __syncthreads();
-  if (EPI == 1) {
-    // Folding epilogue, HC columns at a time: warps 2..5 move the raw FP32
-    // accumulator rows of their TMEM lane quadrant to shared memory (reusing
-    // the pipeline stages: once `done` has fired every load has landed and
-    // every MMA has read its operands), then all threads fold and write them.
-    constexpr int HC = FOLD_HC<BN>();
-    float* sP = reinterpret_cast<float*>(smem);
-    const bool ok = !*abort_flag;
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, CARC_NOT_CONVERGED);
+  if (warp == 1) {
     tc_fence_after();
-#pragma unroll 1
-    for (int h0 = 0; h0 < BN; h0 += HC) {
-      if (ok && warp >= 2) {
-        const int quad = warp & 3;
-#pragma unroll 1
-        for (int c0 = 0; c0 < HC; c0 += 32) {
-          uint32_t r[32];
-          tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(h0 + c0), r);
-          tmem_ld_wait();
-          float4* dst = reinterpret_cast<float4*>(sP + (quad * 32 + lane) * FOLD_PITCH<BN>() + c0);
-#pragma unroll
-          for (int j = 0; j < 32; j += 4) {
-            if (c0 + j >= HC) break;
-            dst[j / 4] = make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
-                                     __uint_as_float(r[j + 3]));
-          }
+    tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+// ---- persistent folding GEMM --------------------------------------------------
+// W = A . B^T folded into the step-B operand (the epilogue above), as a
+// persistent warp-specialised kernel: one CTA per SM walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ... N-tile-fastest (the N tiles of one M tile run
+// on neighbouring SMs at the same time, so the A tile is read from HBM once).
+//   warp 0        TMA producer: A and B K-blocks through FG_STAGES stages,
+//                 running ahead into the next tiles
+//   warp 1        MMA issuer: tile i into TMEM accumulator i % 2
+//   warps 2..9    epilogue: accumulator -> staged FP32 block (two warps per
+//                 TMEM lane quadrant) -> fold -> W; they release the
+//                 accumulator as soon as its last columns are staged, so
+//                 the MMAs of tile i + 2 overlap the fold of tile i.
+// Every wait is bounded; on expiry the CTA raises its abort flag, stops,
+// lets its copies and MMAs land, frees TMEM and reports CARC_NOT_CONVERGED.
+constexpr int FG_EPI_WARPS = 8;
+constexpr int FG_THREADS = 32 * (2 + FG_EPI_WARPS);
+
+template <int BN>
+__host__ __device__ constexpr int fg_stage_bytes() { return A_STAGE_BYTES + BN * BK * 2; }
+
+template <int BN>
+__host__ __device__ constexpr int fg_stages() {
+  // up to 4 stages next to the staged block, within the 227 KB opt-in limit
+  return (227 * 1024 - 1024 - fold_smem_bytes<BN>() - 256) / fg_stage_bytes<BN>() >= 4
+             ? 4
+             : (227 * 1024 - 1024 - fold_smem_bytes<BN>() - 256) / fg_stage_bytes<BN>();
+}
+
+template <int BN>
+__host__ __device__ constexpr int fg_smem_bytes() {
+  return 1024 + fg_stages<BN>() * fg_stage_bytes<BN>() + fold_smem_bytes<BN>() + 256;
+}
+
+// OR of a predicate over the epilogue warps (named barrier 1): every one of
+// them takes the same branch after a wait that may have given up.
+__device__ __forceinline__ bool fg_epilogue_any(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n"
+      ".reg .pred p, q;\n"
+      "setp.ne.u32 q, %1, 0;\n"
+      "bar.red.or.pred p, 1, %2, q;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "n"(32 * FG_EPI_WARPS)
+      : "memory");
+  return r != 0;
+}
+
+template <int BN>
+__global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                                  const __grid_constant__ CUtensorMap tmB,
+                                                                  int n_tiles, int tiles, int nkb, int* __restrict__ err,
+                                                                  const __grid_constant__ FoldEpi fe) {
+  using namespace umma;
+  constexpr int STAGES = fg_stages<BN>();
+  static_assert(STAGES >= 2, "the folding GEMM needs at least two pipeline stages");
+  static_assert(FG_EPI_WARPS % ((FOLD_HC<BN>() + 31) / 32) == 0, "epilogue warps per slot group");
+  constexpr int B_STAGE_BYTES = BN * BK * 2;
+  constexpr uint32_t ACC_COLS = tmem_cols_for(BN);
+  constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
+  constexpr int HC = FOLD_HC<BN>();
+  constexpr int EPI_THREADS = 32 * FG_EPI_WARPS;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + STAGES * A_STAGE_BYTES;
+  float* sP = reinterpret_cast<float*>(sB + STAGES * B_STAGE_BYTES);
+  uint64_t* full = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(sP) + fold_smem_bytes<BN>());
+  uint64_t* empty = full + STAGES;
+  uint64_t* acc_full = empty + STAGES;   // [2] MMAs of the buffer's tile done
+  uint64_t* acc_empty = acc_full + 2;    // [2] the buffer's columns staged (one arrival per epilogue warp)
+  uint64_t* done = acc_empty + 2;        // every MMA issued has completed (abort path)
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int my_tiles = blockIdx.x < tiles ? (tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], FG_EPI_WARPS);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      prefetch_tensormap(&tmA);
+      prefetch_tensormap(&tmB);
+      int c = 0;  // K-blocks issued by this CTA
+      for (int i = 0; i < my_tiles && !*abort_flag; ++i) {
+        const int t = (int)blockIdx.x + i * (int)gridDim.x;
+        const int m0 = (t / n_tiles) * BM, n0 = (t % n_tiles) * BN;
+        for (int kb = 0; kb < nkb; ++kb, ++c) {
+          const int s = c % STAGES;
+          if (!mbar_wait(&empty[s], (uint32_t)(((c / STAGES) & 1) ^ 1), abort_flag)) break;
+          mbar_arrive_expect_tx(&full[s], (uint32_t)(A_STAGE_BYTES + B_STAGE_BYTES));
+          tma_load_2d(sA + s * A_STAGE_BYTES, &tmA, kb * BK, m0, &full[s]);
+          tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, kb * BK, n0, &full[s]);
         }
       }
-      tc_fence_before();
-      fold_tables<BN>(sP, fe, m0, n0 + h0, threadIdx.x, blockDim.x);
-      __syncthreads();
-      if (ok) fold_write<BN>(sP, fe);
-      __syncthreads();
+      if (*abort_flag) {
+        // let the copies in flight land before the CTA exits (bounded)
+        for (int j = max(0, c - STAGES); j < c; ++j) {
+          const int s = j % STAGES;
+          for (uint32_t k = 0; k < (1u << 20); ++k)
+            if (mbar_try_wait(&full[s], (uint32_t)((j / STAGES) & 1))) break;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(BM, BN);
+      int c = 0;
+      for (int i = 0; i < my_tiles && !*abort_flag; ++i) {
+        const int b = i & 1;
+        // the epilogue has staged this buffer's previous tile (i - 2)
+        if (!mbar_wait(&acc_empty[b], (uint32_t)(((i >> 1) & 1) ^ 1), abort_flag)) break;
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)b * ACC_COLS;
+        bool ok = true;
+        for (int kb = 0; kb < nkb; ++kb, ++c) {
+          const int s = c % STAGES;
+          if (!mbar_wait(&full[s], (uint32_t)((c / STAGES) & 1), abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a_base = smem_u32(sA + s * A_STAGE_BYTES);
+          const uint32_t b_base = smem_u32(sB + s * B_STAGE_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; ++kk)
+            mma_bf16(acc, smem_desc_sw128(a_base + kk * 32), smem_desc_sw128(b_base + kk * 32), idesc,
+                     (kb > 0 || kk > 0) ? 1u : 0u);
+          mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&acc_full[b]);
+      }
+      // every MMA issued has landed before TMEM is freed (bounded)
+      mma_commit(done);
+      for (uint32_t k = 0; k < (1u << 22); ++k)
+        if (mbar_try_wait(done, 0)) break;
+    }
+  } else {
+    // epilogue warps: e = 0..7, TMEM lane quadrant warp % 4, column half h
+    const int e = warp - 2, quad = warp & 3, h = e >> 2;
+    const int ds = fold_ds<BN>(fe.d);
+    for (int i = 0; i < my_tiles; ++i) {
+      const int b = i & 1;
+      const int t = (int)blockIdx.x + i * (int)gridDim.x;
+      const int m0 = (t / n_tiles) * BM, n0 = (t % n_tiles) * BN;
+      const bool got = mbar_wait_sleep(&acc_full[b], (uint32_t)((i >> 1) & 1), abort_flag);
+      if (fg_epilogue_any(!got)) break;  // all epilogue warps leave together
       tc_fence_after();
+      const uint32_t acc = tmem + (uint32_t)b * ACC_COLS + ((uint32_t)(quad * 32) << 16);
+      for (int h0 = 0; h0 < BN; h0 += HC) {
+        // the previous block's fold has read the staged block and the tables
+        asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
+        float* row = sP + (quad * 32 + lane) * FOLD_PITCH<BN>();
+#pragma unroll 1
+        for (int c0 = 32 * h; c0 < HC; c0 += 64) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(acc + (uint32_t)(h0 + c0), r);
+          tmem_ld_wait();
+          switch (ds) {
+            case 2: fold_stage<BN, 2>(row, c0, r); break;
+            case 4: fold_stage<BN, 4>(row, c0, r); break;
+            case 8: fold_stage<BN, 8>(row, c0, r); break;
+            default: fold_stage<BN, 1>(row, c0, r); break;
+          }
+        }
+        if (h0 + HC >= BN) {
+          // the accumulator is staged: the MMAs of tile i + 2 may overwrite it
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&acc_empty[b]);
+        }
+        fold_tables<BN>(sP, fe, m0, n0 + h0, ds, threadIdx.x - 64, EPI_THREADS);
+        asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
+        fold_write<BN>(sP, fe, e, FG_EPI_WARPS);
+      }
     }
   }
+  tc_fence_before();
+  __syncthreads();
   if (threadIdx.x == 0 && *abort_flag) atomicExch(err, CARC_NOT_CONVERGED);
   if (warp == 1) {
     tc_fence_after();
@@ -325,39 +542,51 @@ int make_map(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, 
   return CARC_OK;
 }
 
-template <int BN, int EPI>
+template <int BN>
 int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_rows, float* out, int64_t ld_out,
-              int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, const FoldEpi& fe,
-              cudaStream_t stream) {
-  constexpr int SMEM = smem_bytes<BN, EPI>();
+              int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, cudaStream_t stream, int bn) {
+  constexpr int SMEM = smem_bytes<BN>();
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    attr_err = cudaFuncSetAttribute(gemm_bf16_tn_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
   });
   if (attr_err != cudaSuccess) return fail(CARC_CUDA_ERROR, "tensor core GEMM: %s", cudaGetErrorString(attr_err));
-  dim3 grid(M / BM, N / BN, ksplit);
-  gemm_bf16_tn_kernel<BN, EPI><<<grid, THREADS, SMEM, stream>>>(ma, mb, out, ld_out, split_stride, kb_per, kb_total, a_rows,
-                                                                 err, fe);
+  const dim3 grid(M / BM, N / bn, ksplit);
+  gemm_bf16_tn_kernel<BN><<<grid, THREADS, SMEM, stream>>>(ma, mb, out, ld_out, split_stride, kb_per, kb_total, a_rows,
+                                                            err, bn);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }
 
-template <int EPI>
 int launch_any(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_rows, float* out,
-               int64_t ld_out,
-               int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, const FoldEpi& fe,
+               int64_t ld_out, int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err,
                cudaStream_t stream) {
   switch (bn) {
-    case 256: return launch_bn<256, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    case 128: return launch_bn<128, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    case 64: return launch_bn<64, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    case 32: return launch_bn<32, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
-    default: return launch_bn<16, EPI>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, fe, stream);
+    case 256: return launch_bn<256>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
+    case 128: return launch_bn<128>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
+    case 64: return launch_bn<64>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
+    case 32: return launch_bn<32>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
+    case 16: return launch_bn<16>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
+    default:
+      // other widths (multiples of 16 below 256) run on the 256-wide instance
+      if (bn % 16 != 0 || bn < 16 || bn > 256) return fail(CARC_BAD_ARG, "tensor core GEMM: N tile %d", bn);
+      return launch_bn<256>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
   }
 }
 
 }  // namespace
+
+int gemm_tile_n(int N) {
+  const int nt = (N + 255) / 256;
+  if (N > 0 && N % nt == 0 && (N / nt) % 16 == 0) return N / nt;
+  return N % 256 == 0 ? 256 : N % 128 == 0 ? 128 : N % 64 == 0 ? 64 : N % 32 == 0 ? 32 : 16;
+}
+
+int64_t gemm_pad_n(int64_t n) {
+  const int64_t nt = (n + 255) / 256;
+  return nt * round_up((n + nt - 1) / nt, 16);
+}
 
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
                  cudaStream_t stream, int m_live) {
@@ -368,31 +597,62 @@ int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, 
   ksplit = std::max(1, std::min(ksplit, kb_total));
   const int kb_per = (kb_total + ksplit - 1) / ksplit;
   ksplit = (kb_total + kb_per - 1) / kb_per;
-  int bn = N % 256 == 0 ? 256 : N % 128 == 0 ? 128 : N % 64 == 0 ? 64 : N % 32 == 0 ? 32 : 16;
+  const int bn = gemm_tile_n(N);
   // one 128-row tile whose rows >= 64 are zero padding: load only the live half
   const int a_rows = (M == BM && m_live > 0 && m_live <= 64) ? 64 : BM;
   CUtensorMap ma, mb;
   CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, (uint32_t)a_rows));
   CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
   const int64_t split_stride = (int64_t)M * ld_out;
-  FoldEpi none;
-  memset(&none, 0, sizeof(none));
-  return launch_any<0>(bn, ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, none,
-                       stream);
+  return launch_any(bn, ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream);
 }
+
+namespace {
+
+template <int BN>
+int launch_fold(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int nkb, int* err, const FoldEpi& fe,
+                cudaStream_t stream) {
+  constexpr int SMEM = fg_smem_bytes<BN>();
+  static_assert(SMEM <= 227 * 1024, "folding GEMM shared memory");
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(fold_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+  });
+  if (attr_err != cudaSuccess) return fail(CARC_CUDA_ERROR, "folding GEMM: %s", cudaGetErrorString(attr_err));
+  int dev = 0, sms = 0;
+  CARC_CHECK_CUDA(cudaGetDevice(&dev));
+  CARC_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int n_tiles = N / BN;
+  const int64_t tiles = (int64_t)(M / BM) * n_tiles;
+  if (tiles >= (int64_t(1) << 31)) return fail(CARC_TOO_LARGE, "folding GEMM: %lld tiles", (long long)tiles);
+  const int grid = (int)std::min<int64_t>(tiles, std::max(1, sms));
+  fold_gemm_kernel<BN><<<grid, FG_THREADS, SMEM, stream>>>(ma, mb, n_tiles, (int)tiles, nkb, err, fe);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+}  // namespace
 
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
                       cudaStream_t stream) {
   if (M <= 0 || N <= 0 || K <= 0 || M % BM != 0 || K % BK != 0 || N % 16 != 0)
     return fail(CARC_BAD_SHAPE, "tensor core GEMM: shape %d x %d x %d not tileable (M%%128, K%%64, N%%16)", M, N, K);
-  if (fe.M * 4 > M || fe.N > N || (fe.pitch & 1) || (fe.col_off & 1))
+  if (fe.M * 4 > M || fe.N > N || (fe.pitch & 1) || (fe.col_off & 1) || fe.pitch >= (int64_t(1) << 31) ||
+      fe.l0 * fe.l1 * fe.d * fe.nvec >= (int64_t(1) << 31))
     return fail(CARC_BAD_ARG, "tensor core GEMM: folding epilogue does not fit the tile grid");
   const int kb_total = K / BK;
   int bn = N % 256 == 0 ? 256 : N % 128 == 0 ? 128 : N % 64 == 0 ? 64 : N % 32 == 0 ? 32 : 16;
   CUtensorMap ma, mb;
   CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, BM));
   CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
-  return launch_any<1>(bn, ma, mb, M, N, BM, nullptr, N, 0, 1, kb_total, kb_total, err, fe, stream);
+  switch (bn) {
+    case 256: return launch_fold<256>(ma, mb, M, N, kb_total, err, fe, stream);
+    case 128: return launch_fold<128>(ma, mb, M, N, kb_total, err, fe, stream);
+    case 64: return launch_fold<64>(ma, mb, M, N, kb_total, err, fe, stream);
+    case 32: return launch_fold<32>(ma, mb, M, N, kb_total, err, fe, stream);
+    default: return launch_fold<16>(ma, mb, M, N, kb_total, err, fe, stream);
+  }
 }
 
 int tma_map_bf16(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_rows) {

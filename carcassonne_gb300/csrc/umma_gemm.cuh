@@ -63,6 +63,13 @@ int64_t round_up(int64_t a, int64_t b);
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
                  cudaStream_t stream, int m_live = 0);
 int gemm_effective_ksplit(int K, int ksplit);
+// N tile of gemm_bf16_tn: N in ceil(N / 256) equal tiles when those are
+// multiples of 16 (each N tile streams the whole A operand once), else the
+// largest of 256/128/64/32/16 dividing N.
+int gemm_tile_n(int N);
+// Rows to pad a B operand of n rows to so that gemm_bf16_tn tiles it in
+// ceil(n / 256) equal tiles of a multiple of 16 (the least padding).
+int64_t gemm_pad_n(int64_t n);
 // 2D tensor map of a BF16 K-major matrix (inner = K columns, rows), box of
 // 64 columns x box_rows rows, 128-byte swizzle (the GEMM operand layout).
 int tma_map_bf16(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_rows);

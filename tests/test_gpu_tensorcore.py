@@ -28,7 +28,9 @@ def lib():
 
 
 @pytest.mark.parametrize("M,N,K,ksplit", [(128, 16, 64, 1), (256, 64, 256, 1), (128, 256, 512, 3),
-                                          (384, 48, 192, 2), (128, 128, 1024, 4)])
+                                          (384, 48, 192, 2), (128, 128, 1024, 4),
+                                          # N tiles that are not powers of two: 2 x 208, 3 x 192, 1 x 144
+                                          (128, 416, 256, 2), (256, 576, 128, 1), (128, 144, 192, 1)])
 def test_raw_bf16_gemm(lib, M, N, K, ksplit):
     L = lib.load()
     g = torch.Generator().manual_seed(M + N + K)
@@ -142,3 +144,52 @@ def test_fused_matvec_matches_unfused_and_fp64(lib, D, c_ket, c_bra, nvec):
     assert np.abs(y_fused - y64).max() / scale < 5e-5
     assert np.abs(y_two - y64).max() / scale < 5e-5
     assert np.abs(y_fused - y_two).max() / scale < 2e-5
+
+
+def _random_site_operators(d, seed):
+    """The transverse-Ising tag set with random Hermitian d x d site matrices
+    (the identity tag keeps the identity)."""
+    from carcassonne_gb300 import workloads
+    rng = np.random.default_rng(seed)
+    out = []
+    for tag, _ in workloads.ti_operator_arrays():
+        if type(tag).__name__ == "Identity":
+            out.append((tag, np.eye(d, dtype=np.complex128)))
+            continue
+        a = rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))
+        out.append((tag, (a + a.conj().T) / 2))
+    return out
+
+
+# D = 5, 6: W has 400 / 576 rows, tiled 2 x 208 / 3 x 192 by step B; d = 1,
+# 3, 4, 8: the folding epilogue's staged column order (p-major for 2, 4, 8,
+# column order otherwise)
+@pytest.mark.parametrize("D,c_ket,c_bra,nvec,d", [(5, 2, 2, 8, 2), (6, 2, 1, 8, 2), (3, 2, 2, 2, 4),
+                                                  (3, 2, 2, 3, 1), (3, 2, 1, 2, 3), (2, 2, 2, 4, 8)])
+def test_two_kernel_matvec_shapes(lib, D, c_ket, c_bra, nvec, d):
+    """The two-kernel tensor-core path (step A with the folding epilogue, W
+    through HBM, split-K step B), forced through the autotune cache, against
+    the FP64 path."""
+    from carcassonne_gb300 import workloads
+    from carcassonne_gb300.tensors._2d import sparse as tsp
+    L = lib.load()
+    ops = _random_site_operators(d, seed=D + d)
+    corners_a, sides_a, op_a = workloads.matvec_problem_arrays(D=D, c_ket=c_ket, c_bra=c_bra, seed=11,
+                                                               op_arrays=ops)
+    corners, sides, op = workloads.to_device(corners_a, sides_a, op_a)
+    H, _ = tsp.formExpectationAndNormalizationMultipliers(corners, sides, op)
+    opr = H.operator
+    assert opr.d == d
+    rng = np.random.default_rng(5)
+    shape = (nvec,) + opr.in_shape
+    x = torch.as_tensor(rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).cuda()
+    y64 = opr.apply(x, nvec=nvec).cpu().numpy()
+    try:
+        for g in opr._groups:
+            groups = len({t[1] for t in g["terms"]})
+            lib.check(L.carc_tc_autotune_set(g["s0"], g["s1"], opr.d, nvec, groups, 152))
+        y_two = opr.apply_tc(x, nvec=nvec).cpu().numpy()
+        opr.check_status()
+    finally:
+        lib.check(L.carc_tc_autotune_clear())
+    assert np.abs(y_two - y64).max() / np.abs(y64).max() < 5e-5
