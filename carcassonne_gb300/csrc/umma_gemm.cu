@@ -314,13 +314,13 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
 //   warp 0        TMA producer: A and B K-blocks through FG_STAGES stages,
 //                 running ahead into the next tiles
 //   warp 1        MMA issuer: tile i into TMEM accumulator i % 2
-//   warps 2..9    epilogue: accumulator -> staged FP32 block (two warps per
-//                 TMEM lane quadrant) -> fold -> W; they release the
+//   warps 2..17   epilogue: accumulator -> staged FP32 block (four warps
+//                 per TMEM lane quadrant) -> fold -> W; they release the
 //                 accumulator as soon as its last columns are staged, so
 //                 the MMAs of tile i + 2 overlap the fold of tile i.
 // Every wait is bounded; on expiry the CTA raises its abort flag, stops,
 // lets its copies and MMAs land, frees TMEM and reports CARC_NOT_CONVERGED.
-constexpr int FG_EPI_WARPS = 8;
+constexpr int FG_EPI_WARPS = 16;
 constexpr int FG_THREADS = 32 * (2 + FG_EPI_WARPS);
 
 template <int BN>
@@ -465,7 +465,9 @@ __global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_c
         if (mbar_try_wait(done, 0)) break;
     }
   } else {
-    // epilogue warps: e = 0..7, TMEM lane quadrant warp % 4, column half h
+    // epilogue warps: e = 0..15, TMEM lane quadrant warp % 4, column block
+    // phase h (each 32-column block of a quadrant goes to one of its warps)
+    constexpr int PER_QUAD = FG_EPI_WARPS / 4;
     const int e = warp - 2, quad = warp & 3, h = e >> 2;
     const int ds = fold_ds<BN>(fe.d);
     for (int i = 0; i < my_tiles; ++i) {
@@ -481,7 +483,7 @@ __global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_c
         asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
         float* row = sP + (quad * 32 + lane) * FOLD_PITCH<BN>();
 #pragma unroll 1
-        for (int c0 = 32 * h; c0 < HC; c0 += 64) {
+        for (int c0 = 32 * h; c0 < HC; c0 += 32 * PER_QUAD) {
           uint32_t r[32];
           tmem_ld_32x32b_x32(acc + (uint32_t)(h0 + c0), r);
           tmem_ld_wait();
