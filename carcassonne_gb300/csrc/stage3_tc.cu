@@ -166,19 +166,18 @@ ZView view_s2_1_stepB(const S3& s, const void* base) {
   return v;
 }
 
-// zero the padding of the packed W: rows >= rows_valid, and per region the
-// columns [4 kc, reg) (the folding epilogue writes only the valid entries)
-__global__ void clear_w_padding_kernel(__nv_bfloat16* __restrict__ W, int64_t rows_valid, int64_t rows_total,
-                                       int64_t kc4, int64_t reg, int64_t n_reg) {
-  const int64_t kp = reg * n_reg, pad = reg - kc4;
-  const int64_t t1 = rows_valid * n_reg * pad, t2 = (rows_total - rows_valid) * kp;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < t1 + t2; t += (int64_t)gridDim.x * blockDim.x) {
-    if (t < t1) {
-      const int64_t row = t / (n_reg * pad), rem = t % (n_reg * pad);
-      W[row * kp + (rem / pad) * reg + kc4 + rem % pad] = __float2bfloat16_rn(0.f);
-    } else {
-      W[rows_valid * kp + (t - t1)] = __float2bfloat16_rn(0.f);
-    }
+// zero the K padding of the valid rows of the packed W, per region the
+// columns [4 kc, reg) (the folding epilogue writes only the valid entries);
+// W is K-block-major with `rows` rows: column c of row r at
+// (c / 64) rows 64 + r 64 + c % 64
+__global__ void clear_w_padding_kernel(__nv_bfloat16* __restrict__ W, int64_t rows_valid, int64_t rows, int64_t kc4,
+                                       int64_t reg, int64_t n_reg) {
+  const int64_t pad = reg - kc4;
+  const int64_t t1 = rows_valid * n_reg * pad;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < t1; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = t / (n_reg * pad), rem = t % (n_reg * pad);
+    const int64_t c = (rem / pad) * reg + kc4 + rem % pad;
+    W[(c >> 6) * rows * 64 + row * 64 + (c & 63)] = __float2bfloat16_rn(0.f);
   }
 }
 
@@ -1037,7 +1036,7 @@ int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, co
   const int64_t pad_w = rows_valid_w * G * (g.regB - 4 * g.kcB);
   if (pad_w > 0) {
     clear_w_padding_kernel<<<grid_of(pad_w), 256, 0, stream>>>(reinterpret_cast<__nv_bfloat16*>(w.w_pk), rows_valid_w,
-                                                              rows_valid_w, 4 * g.kcB, g.regB, G);
+                                                              g.rowsB_b, 4 * g.kcB, g.regB, G);
     CARC_CHECK_LAUNCH();
   }
   // step A per group: W_g = sum_{t in g} S2_0[i0_t] . Vin_t, folded straight into region g of the step-B operand
@@ -1059,7 +1058,7 @@ int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, co
       fe.N = g.NA;
       fe.kc = g.kcB;
       fe.col_off = (int64_t)q * g.regB;
-      fe.pitch = kpB;
+      fe.rows = g.rowsB_b;
       fe.dst = w.w_pk;
       CARC_RETURN_IF(gemm_bf16_tn_fold(planA, (int)g1.rowsA_a, w.vin + w.vin_off[q], (int)g.rowsA_b, (int)kpA, fe,
                                        status, stream));
@@ -1071,7 +1070,7 @@ int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, co
   {
     PhaseScope ph(PH_TC_STEP_B, stream);
     CARC_RETURN_IF(gemm_bf16_tn(planB, (int)g1.rowsB_a, w.w_pk, (int)g.rowsB_b, (int)kpB, w.pB, g.rowsB_b, w.ksB,
-                                status, stream, (int)(4 * s.l2 * s.l3)));
+                                status, stream, (int)(4 * s.l2 * s.l3), /*b_blocked=*/1));
   }
   return CARC_OK;
 }

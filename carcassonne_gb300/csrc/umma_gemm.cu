@@ -52,9 +52,10 @@ constexpr int smem_bytes() {
 // p-major (slot (n % d) HC/d + n / d), so that consecutive slots walk (vec,
 // k2, k3), i.e. consecutive destination k, and consecutive lanes read
 // consecutive words; otherwise in column order.  After the staged block come
-// two index tables: per complex row m of the tile the destination offset of
-// its (row part, k part) in bf16 pairs, row part x pitch + k part (-1: past
-// M), and per slot {row part, k part} (row part -1: past N).
+// two index tables: per complex row m of the tile {row part, k part} of the
+// destination (row part -1: past M), and per slot {row part, k part} (row
+// part -1: past N).  Destination row = sum of the row parts, complex k = sum
+// of the k parts.
 template <int BN>
 __host__ __device__ constexpr int FOLD_HC() { return BN == 256 ? 128 : (BN == 128 ? 64 : BN); }
 
@@ -100,19 +101,18 @@ template <int BN>
 __device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0, int nb, int ds, int tid,
                                             int nthreads) {
   constexpr int HC = FOLD_HC<BN>();
-  long long* tabM = reinterpret_cast<long long*>(sP + 128 * FOLD_PITCH<BN>());
-  int2* tabN = reinterpret_cast<int2*>(tabM + 32);
+  int2* tabM = reinterpret_cast<int2*>(sP + 128 * FOLD_PITCH<BN>());
+  int2* tabN = tabM + 32;
   const int L0 = (int)fe.l0, L1 = (int)fe.l1, X1 = (int)fe.x1, K2 = (int)fe.k2, K3 = (int)fe.k3, Dp = (int)fe.d;
-  const long long pitch2 = fe.pitch >> 1;
   for (int i = tid; i < 32; i += nthreads) {
     const int64_t m = (int64_t)(m0 >> 2) + i;
-    long long t = -1;
+    int2 t = make_int2(-1, 0);
     if (m < fe.M) {
       int r = (int)m;
       const int ll1 = r % L1; r /= L1;
       const int ll0 = r % L0; r /= L0;
       const int xx1 = r % X1; r /= X1;
-      t = (long long)((ll0 * L1 + ll1) * Dp) * pitch2 + (long long)(r * X1 + xx1) * K2 * K3;
+      t = make_int2((ll0 * L1 + ll1) * Dp, (r * X1 + xx1) * K2 * K3);
     }
     tabM[i] = t;
   }
@@ -135,38 +135,42 @@ __device__ __forceinline__ void fold_tables(float* sP, const FoldEpi& fe, int m0
 // W[m, n] = (P[4m] + P[4m+1]) + i (P[4m+2] + P[4m+3]), split into bf16 hi/lo
 // pairs.  Warp w of nw (nw a multiple of the HC/32 slot groups) takes slot
 // group w % (HC/32) and every (nw / (HC/32))-th complex row: each lane keeps
-// its slot's destination in registers, reads one consecutive staged word per
-// row and stores consecutive k of one destination row with its neighbours.
+// its slot's destination parts in registers, reads one consecutive staged
+// word per row and stores consecutive k of one destination row with its
+// neighbours (one 128-byte run of a K block).
 template <int BN>
 __device__ __forceinline__ void fold_write(const float* sP, const FoldEpi& fe, int warp, int nw) {
   constexpr int HC = FOLD_HC<BN>();
   constexpr int PITCH = FOLD_PITCH<BN>();
   constexpr int JQ = (HC + 31) / 32;  // 32-slot groups per row
-  const long long* tabM = reinterpret_cast<const long long*>(sP + 128 * PITCH);
-  const int2* tabN = reinterpret_cast<const int2*>(tabM + 32);
+  const int2* tabM = reinterpret_cast<const int2*>(sP + 128 * PITCH);
+  const int2* tabN = tabM + 32;
   const int lane = threadIdx.x & 31;
   const int q = (warp % JQ) * 32 + lane;
   const int rstep = nw / JQ;
   if (q >= HC) return;
   const int2 tn = tabN[q];
   if (tn.x < 0) return;
-  // bf16 (re, im) pairs; pitch and col_off are even
-  uint32_t* Wq = static_cast<uint32_t*>(fe.dst) + (fe.col_off >> 1) + (int64_t)tn.x * (fe.pitch >> 1) + tn.y;
+  // bf16 (re, im) pairs in K blocks of 32 pairs x rows (col_off is even)
+  uint32_t* W = static_cast<uint32_t*>(fe.dst);
+  const int rows32 = (int)fe.rows * 32;
+  const int cp_lane = (int)(fe.col_off >> 1) + tn.y;
   const int kc = (int)fe.kc;
   const float* col = sP + q;
 #pragma unroll 4
   for (int ml = warp / JQ; ml < 32; ml += rstep) {
-    const long long off = tabM[ml];
-    if (off < 0) continue;
+    const int2 tm = tabM[ml];
+    if (tm.x < 0) continue;
     const float* c = col + 4 * ml * PITCH;
     const float re = c[0] + c[PITCH];
     const float im = c[2 * PITCH] + c[3 * PITCH];
     const __nv_bfloat162 h2 = __floats2bfloat162_rn(re, im);
     const float2 hf = __bfloat1622float2(h2);
     const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
-    uint32_t* rowp = Wq + off;
-    rowp[0] = *reinterpret_cast<const uint32_t*>(&h2);
-    rowp[kc] = *reinterpret_cast<const uint32_t*>(&l2);
+    const int row32 = (tn.x + tm.x) * 32;
+    const int cp = cp_lane + tm.y, cl = cp + kc;
+    W[(int64_t)(cp >> 5) * rows32 + row32 + (cp & 31)] = *reinterpret_cast<const uint32_t*>(&h2);
+    W[(int64_t)(cl >> 5) * rows32 + row32 + (cl & 31)] = *reinterpret_cast<const uint32_t*>(&l2);
   }
 }
 
@@ -179,7 +183,7 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
                                                                   float* __restrict__ out, int64_t ld_out,
                                                                   int64_t split_stride, int kb_per_split,
                                                                   int kb_total, int a_rows, int* __restrict__ err,
-                                                                  int bn) {
+                                                                  int bn, int b_blk) {
   using namespace umma;
   constexpr int B_STAGE_BYTES = BN * BK * 2;
   constexpr uint32_t TMEM_COLS = tmem_cols_for(BN);
@@ -236,7 +240,10 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
         mbar_arrive_expect_tx(&full[s], (uint32_t)(a_rows * BK * 2 + bn * BK * 2));
         const int kx = (kb0 + i) * BK;
         tma_load_2d(sA + s * A_STAGE_BYTES, &tmA, kx, m0, &full[s]);
-        tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, kx, n0, &full[s]);
+        if (b_blk)
+          tma_load_3d(sB + s * B_STAGE_BYTES, &tmB, 0, n0, kb0 + i, &full[s]);
+        else
+          tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, kx, n0, &full[s]);
         ++issued;
       }
       if (*abort_flag) {
@@ -544,9 +551,29 @@ int make_map(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, 
   return CARC_OK;
 }
 
+// 3D tensor map of a K-block-major BF16 operand ([K / 64][rows][64]): box of
+// 64 columns x box_rows rows of one K block, 128-byte swizzle; the shared
+// memory tile is the same as make_map's.
+int make_map_kblocked(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_rows) {
+  auto fn = encode_fn();
+  if (!fn) return fail(CARC_CUDA_ERROR, "tensor core GEMM: cuTensorMapEncodeTiled is unavailable");
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || inner % BK != 0)
+    return fail(CARC_BAD_ARG, "tensor core GEMM: K-blocked operand not 16-byte aligned or K not a multiple of 64");
+  cuuint64_t dims[3] = {(cuuint64_t)BK, rows, inner / BK};
+  cuuint64_t strides[2] = {(cuuint64_t)BK * 2, rows * BK * 2};
+  cuuint32_t box[3] = {(cuuint32_t)BK, box_rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(CARC_CUDA_ERROR, "tensor core GEMM: cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return CARC_OK;
+}
+
 template <int BN>
 int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_rows, float* out, int64_t ld_out,
-              int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, cudaStream_t stream, int bn) {
+              int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err, cudaStream_t stream, int bn,
+              int b_blk) {
   constexpr int SMEM = smem_bytes<BN>();
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
@@ -556,24 +583,24 @@ int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_
   if (attr_err != cudaSuccess) return fail(CARC_CUDA_ERROR, "tensor core GEMM: %s", cudaGetErrorString(attr_err));
   const dim3 grid(M / BM, N / bn, ksplit);
   gemm_bf16_tn_kernel<BN><<<grid, THREADS, SMEM, stream>>>(ma, mb, out, ld_out, split_stride, kb_per, kb_total, a_rows,
-                                                            err, bn);
+                                                            err, bn, b_blk);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }
 
 int launch_any(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_rows, float* out,
                int64_t ld_out, int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err,
-               cudaStream_t stream) {
+               cudaStream_t stream, int b_blk) {
   switch (bn) {
-    case 256: return launch_bn<256>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
-    case 128: return launch_bn<128>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
-    case 64: return launch_bn<64>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
-    case 32: return launch_bn<32>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
-    case 16: return launch_bn<16>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
+    case 256: return launch_bn<256>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn, b_blk);
+    case 128: return launch_bn<128>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn, b_blk);
+    case 64: return launch_bn<64>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn, b_blk);
+    case 32: return launch_bn<32>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn, b_blk);
+    case 16: return launch_bn<16>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn, b_blk);
     default:
       // other widths (multiples of 16 below 256) run on the 256-wide instance
       if (bn % 16 != 0 || bn < 16 || bn > 256) return fail(CARC_BAD_ARG, "tensor core GEMM: N tile %d", bn);
-      return launch_bn<256>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn);
+      return launch_bn<256>(ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream, bn, b_blk);
   }
 }
 
@@ -591,7 +618,7 @@ int64_t gemm_pad_n(int64_t n) {
 }
 
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
-                 cudaStream_t stream, int m_live) {
+                 cudaStream_t stream, int m_live, int b_blocked) {
   if (M <= 0 || N <= 0 || K <= 0 || M % BM != 0 || K % BK != 0 || N % 16 != 0)
     return fail(CARC_BAD_SHAPE, "tensor core GEMM: shape %d x %d x %d not tileable (M%%128, K%%64, N%%16)", M, N, K);
   if (ld_out < N || ld_out % 4 != 0) return fail(CARC_BAD_ARG, "tensor core GEMM: ld_out %lld", (long long)ld_out);
@@ -604,9 +631,13 @@ int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, 
   const int a_rows = (M == BM && m_live > 0 && m_live <= 64) ? 64 : BM;
   CUtensorMap ma, mb;
   CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, (uint32_t)a_rows));
-  CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
+  if (b_blocked)
+    CARC_RETURN_IF(make_map_kblocked(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
+  else
+    CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
   const int64_t split_stride = (int64_t)M * ld_out;
-  return launch_any(bn, ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream);
+  return launch_any(bn, ma, mb, M, N, a_rows, out, ld_out, split_stride, ksplit, kb_per, kb_total, err, stream,
+                    b_blocked ? 1 : 0);
 }
 
 namespace {
@@ -640,8 +671,8 @@ int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const F
                       cudaStream_t stream) {
   if (M <= 0 || N <= 0 || K <= 0 || M % BM != 0 || K % BK != 0 || N % 16 != 0)
     return fail(CARC_BAD_SHAPE, "tensor core GEMM: shape %d x %d x %d not tileable (M%%128, K%%64, N%%16)", M, N, K);
-  if (fe.M * 4 > M || fe.N > N || (fe.pitch & 1) || (fe.col_off & 1) || fe.pitch >= (int64_t(1) << 31) ||
-      fe.l0 * fe.l1 * fe.d * fe.nvec >= (int64_t(1) << 31))
+  if (fe.M * 4 > M || fe.N > N || (fe.col_off & 1) || fe.rows < fe.l0 * fe.l1 * fe.d * fe.nvec ||
+      fe.rows * 32 >= (int64_t(1) << 31) || fe.col_off / 2 + 2 * fe.kc >= (int64_t(1) << 31))
     return fail(CARC_BAD_ARG, "tensor core GEMM: folding epilogue does not fit the tile grid");
   const int kb_total = K / BK;
   int bn = N % 256 == 0 ? 256 : N % 128 == 0 ? 128 : N % 64 == 0 ? 64 : N % 32 == 0 ? 32 : 16;

@@ -40,15 +40,19 @@ struct ZOut {
 };
 
 // Epilogue that folds the GEMM rows (4m + 2c + s) into complex W[m, n] and
-// writes it split (hi | lo) into a region of a packed K-major operand:
+// writes it split (hi | lo) into a region of a packed operand:
 //   m -> (x0,x1,l0,l1), n -> (vec,k2,k3,p);  row (vec,l0,l1,p), k (x0,x1,k2,k3).
+// The operand is K-block-major: element (row, column c) of a `rows`-row
+// operand sits at (c / 64) rows 64 + row 64 + c % 64, so that one 64-column K
+// block of all its rows is one contiguous run (one TMA box of the step-B GEMM
+// reads whole DRAM pages, not 128 bytes from each of its rows).
 struct FoldEpi {
   int64_t x0, x1, l0, l1;
   int64_t nvec, k2, k3, d;
   int64_t M, N;      // valid complex rows / columns
   int64_t kc;        // complex K of the destination region
-  int64_t col_off;   // first bf16 column of the region
-  int64_t pitch;     // destination row pitch in bf16 elements
+  int64_t col_off;   // first bf16 column of the region (even)
+  int64_t rows;      // rows of the destination operand
   void* dst;
 };
 
@@ -60,8 +64,10 @@ int64_t round_up(int64_t a, int64_t b);
 // (A: M x K, B: N x K, BF16 K-major; M % 128 == 0, K % 64 == 0, N % 16 == 0).
 // m_live (optional): when M == 128 and only rows [0, m_live <= 64) of A can be
 // nonzero, the zero rows are not read from memory.
+// b_blocked: B is K-block-major ([K / 64][N][64], as the folding epilogue
+// writes W) instead of row-major N x K.
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
-                 cudaStream_t stream, int m_live = 0);
+                 cudaStream_t stream, int m_live = 0, int b_blocked = 0);
 int gemm_effective_ksplit(int K, int ksplit);
 // N tile of gemm_bf16_tn: N in ceil(N / 256) equal tiles when those are
 // multiples of 16 (each N tile streams the whole A operand once), else the
