@@ -79,7 +79,9 @@ int64_t gemm_pad_n(int64_t n);
 // 2D tensor map of a BF16 K-major matrix (inner = K columns, rows), box of
 // 64 columns x box_rows rows, 128-byte swizzle (the GEMM operand layout).
 int tma_map_bf16(CUtensorMap* map, const void* base, uint64_t inner, uint64_t rows, uint32_t box_rows);
-// The same GEMM (no K split) with the folding epilogue instead of FP32 planes.
+// The same GEMM (no K split) with the folding epilogue instead of FP32 planes:
+// a persistent warp-specialised kernel (one CTA per SM, two TMEM accumulators)
+// writing W K-block-major (FoldEpi).
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
                       cudaStream_t stream);
 // Deterministic FP64 reduction of split-K planes into a complex output in one
