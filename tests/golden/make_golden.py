@@ -344,11 +344,48 @@ def chain1d():
     np.savez_compressed(os.path.join(HERE, "chain1d.npz"), **out)
 
 
+# operator-term compression followed by absorptions in every direction: the
+# compressed tags (non-unit operator axes) go through the corner, side and
+# stage rules; (corner, direction, contractions before, new dimension)
+OPCOMP_CASES = [(0, 0, 3, 2), (1, 1, 2, 1), (2, 1, 4, 2), (3, 0, 2, 1), (0, 0, 3, 3), (2, 0, 2, 2)]
+
+
+def opcomp():
+    from carcassonne.system._2d import sideFromCorner
+    from carcassonne.utils import L, R, O
+    rng = np.random.default_rng(77)
+    out = {}
+    for case, (corner_id, direction, terms, new_dim) in enumerate(OPCOMP_CASES):
+        side_id = sideFromCorner(corner_id, direction)
+        a, b = cn(rng, 2, 2), cn(rng, 2, 2)
+        ops = np.stack([(a + a.conj().T) / 2, (b + b.conj().T) / 2])
+        kw = "OO_LR" if side_id in (1, 3) else "OO_UD"
+        system = System.newTrivialWithSimpleSparseOperator(**{kw: [D(ops[0]), D(ops[1])]})
+        system.contractTowards(R(side_id) if direction == 0 else L(side_id))
+        for _ in range(terms):
+            system.contractTowards(side_id)
+        e0, n0 = system.computeExpectationAndNormalization()
+        system.compressCornerTwoSiteOperatorTowards(corner_id, direction, new_dim)
+        e1, n1 = system.computeExpectationAndNormalization()
+        seq = [(complex(e0), complex(n0)), (complex(e1), complex(n1))]
+        dirs = [side_id, (side_id + 1) % 4, O(side_id), (side_id + 3) % 4, side_id]
+        for d in dirs:
+            system.contractTowards(d)
+            e, n = system.computeExpectationAndNormalization()
+            seq.append((complex(e), complex(n)))
+        out[f"c{case}_ops"] = ops
+        out[f"c{case}_spec"] = np.array([corner_id, direction, terms, new_dim])
+        out[f"c{case}_dirs"] = np.array(dirs)
+        out[f"c{case}_EN"] = np.array(seq)
+    np.savez_compressed(os.path.join(HERE, "opcomp.npz"), **out)
+
+
 if __name__ == "__main__":
-    sections = dict(dense=dense_cases, tables=tables_and_trajectories, numerics=numerics, chain1d=chain1d)
+    sections = dict(dense=dense_cases, tables=tables_and_trajectories, numerics=numerics, chain1d=chain1d,
+                    opcomp=opcomp)
     chosen = sys.argv[1:] or list(sections)
     for name in chosen:
         sections[name]()
-    for fn in ("dense.npz", "tables.json", "trajectory.npz", "numerics.npz", "chain1d.npz"):
+    for fn in ("dense.npz", "tables.json", "trajectory.npz", "numerics.npz", "chain1d.npz", "opcomp.npz"):
         if os.path.exists(os.path.join(HERE, fn)):
             print(fn, os.path.getsize(os.path.join(HERE, fn)))

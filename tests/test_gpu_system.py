@@ -235,6 +235,38 @@ def test_compress_two_site_operator_new_same_as_old(env, corner_id, direction, t
     assert abs(e2 - e1) < 1e-9
 
 
+@pytest.mark.parametrize("case", range(6))
+def test_operator_compression_then_absorptions_match_reference(env, case):
+    """Operator-term compression (system/_2d.py:229-363), lossless and lossy,
+    followed by absorptions towards every direction: the compressed tags carry
+    non-unit operator axes through the corner, side and stage rules, and the
+    expectation and normalization after each step equal the reference's
+    (golden run of the reference on the same operators)."""
+    TorchData, System, sideFromCorner, sparse = env
+    from carcassonne_gb300.utils import L, R
+    z = np.load(os.path.join(GOLD, "opcomp.npz"))
+    corner_id, direction, terms, new_dim = (int(v) for v in z[f"c{case}_spec"])
+    ops = z[f"c{case}_ops"]
+    side_id = sideFromCorner(corner_id, direction)
+    kw = "OO_LR" if side_id in (1, 3) else "OO_UD"
+    system = System.newTrivialWithSimpleSparseOperator(**{kw: [TorchData(ops[0]), TorchData(ops[1])]})
+    system.contractTowards(R(side_id) if direction == 0 else L(side_id))
+    for _ in range(terms):
+        system.contractTowards(side_id)
+    got = [system.computeExpectationAndNormalization()]
+    system.compressCornerTwoSiteOperatorTowards(corner_id, direction, new_dim)
+    assert sparse.TwoSiteOperatorCompressed(direction) in system.corners[corner_id]
+    got.append(system.computeExpectationAndNormalization())
+    for d in z[f"c{case}_dirs"]:
+        system.contractTowards(int(d))
+        got.append(system.computeExpectationAndNormalization())
+    want = z[f"c{case}_EN"]
+    assert len(got) == len(want)
+    for step, ((e, n), (we, wn)) in enumerate(zip(got, want)):
+        assert abs(complex(e) - we) <= 1e-9 * max(1.0, abs(we)), (step, complex(e), we)
+        assert abs(complex(n) - wn) <= 1e-9 * max(1.0, abs(wn)), (step, complex(n), wn)
+
+
 @pytest.mark.parametrize("which", ["center", "corner", "side"])
 def test_gauge_normalizations_keep_expectations(env, which):
     TorchData, System, _, _ = env
