@@ -3,13 +3,17 @@
 //
 //  matvec  y[v] = sum_t S2_0[i0_t] (x) S2_1[i1_t] (x) O[io_t] . x[v]
 //    terms are grouped by their S2_1 tag g;
-//    step A (one tcgen05 GEMM per group, terms concatenated along K):
+//    step A (one persistent tcgen05 folding GEMM per group, terms
+//    concatenated along K):
 //      W_g[(x0,x1,l0,l1),(v,k2,k3,p)] = sum_{t in g} sum_{k0,k1} S2_0[i0_t] . Vin_t
 //      whose epilogue folds the (hi,lo) and (re,im) rows and writes W_g split
-//      straight into region g of step B's packed operand;
+//      straight into region g of step B's packed, K-block-major operand;
 //    step B (one split-K tcgen05 GEMM over all groups, concatenated along K):
 //      y^T[(l2,l3),(v,l0,l1,p)] = sum_g sum_{x0,x1,k2,k3} S2_1[g] . W_g,
-//      split planes summed in FP64 by a two-level coalesced reduction.
+//      split planes summed by a coalesced reduction (compensated FP32 per
+//      plane sequence, FP64 combination);
+//    or, for eligible shapes, both steps in one fused kernel with W on chip
+//    (below).
 //  matrix  H = sum_o G_o (x) O_o,  G_o = sum_{t in o} S2_0[i0_t] . S2_1[i1_t] over x,
 //          terms of one operator group concatenated along K in one GEMM.
 //
