@@ -181,4 +181,41 @@ def run(count=32, nvec=8, seed=3, mem_budget=24 << 30, reps=3, tune=True):
     return totals
 
 
-__all__ = ["sample_problems", "build_operator", "operator_bytes", "Batch", "autotune", "run", "CHI_FACTORS"]
+def main(argv=None):
+    """Apply one problem's H_eff (transverse Ising, as in the batched
+    workload) to a block of centers a few times: on the path the autotune
+    cache or the eligibility rule picks, or with ``--ksplit K`` on the
+    two-kernel path with step B split K ways.  A small self-contained case for
+    timing or profiling one shape."""
+    import argparse
+    p = argparse.ArgumentParser(prog="python -m carcassonne_gb300.batched")
+    p.add_argument("--D", type=int, default=5)
+    p.add_argument("--chi", type=int, default=56, choices=sorted(CHI_FACTORS))
+    p.add_argument("--h", type=float, default=3.0)
+    p.add_argument("--seed", type=int, default=11)
+    p.add_argument("--nvec", type=int, default=8)
+    p.add_argument("--ksplit", type=int, default=0, help="> 0: pin the two-kernel path with this step-B split")
+    p.add_argument("--reps", type=int, default=3)
+    a = p.parse_args(argv)
+    lib = _lib.load()
+    op = build_operator(a.D, a.chi, a.h, a.seed)
+    x = torch.zeros((a.nvec,) + op.in_shape, dtype=CDT, device="cuda")
+    y = torch.empty((a.nvec,) + op.out_shape, dtype=CDT, device="cuda")
+    if a.ksplit > 0:
+        for g in op._groups:
+            _lib.check(lib.carc_tc_autotune_set(g["s0"], g["s1"], op.d, a.nvec, _groups_of(g), a.ksplit))
+    try:
+        for _ in range(a.reps):
+            op.apply_tc(x, y, a.nvec)
+        torch.cuda.synchronize()
+        op.check_status()
+    finally:
+        if a.ksplit > 0:
+            _lib.check(lib.carc_tc_autotune_clear())
+    print("ok")
+
+
+__all__ = ["sample_problems", "build_operator", "operator_bytes", "Batch", "autotune", "run", "CHI_FACTORS", "main"]
+
+if __name__ == "__main__":
+    main()
