@@ -32,6 +32,13 @@ def _as_cdt(t):
     return t
 
 
+class ARPACKError(Exception):
+    """Declared by the reference's data module (data/__init__.py:12) for
+    ARPACK failures; kept so that code importing or catching it still works.
+    The device eigensolvers report non-convergence through the library's
+    status words instead."""
+
+
 class Data:
     """Base of the Data protocol (data/__init__.py:17-26)."""
 
@@ -404,4 +411,4 @@ for _n in "IXYZ":
     setattr(TorchData, _n, _LazyPauli(_n))
 
 
-__all__ = ["Data", "TorchData", "pauli", "PAULI"]
+__all__ = ["ARPACKError", "Data", "TorchData", "pauli", "PAULI"]

@@ -12,6 +12,8 @@ from __future__ import annotations
 
 from functools import partial
 
+import numpy as np
+
 from .utils import L, R, O
 
 LEFT = 0
@@ -40,6 +42,9 @@ class _Unique:
 
     def __reduce__(self):
         return (type(self), ())
+
+
+Singleton = _Unique
 
 
 class Identity(_Unique):
@@ -338,10 +343,35 @@ def stripAllButIdentityFrom(sparse):
     return {Identity(): sparse[Identity()]}
 
 
+def makeMPO(I, Os=(), OOs=()):
+    """Chain operator sum_i Os[i] + sum_j OOs[j][0] (x) OOs[j][1] as a
+    matrix-product operator (sparse.py:265-287): an (n, n, d, d) tensor with
+    n = 2 + len(OOs) channels, channel 0 the identity still to the right,
+    channel n - 1 the identity after the term, channel j + 1 term j half
+    applied; returns (tensor, right boundary, right tags, left boundary, left
+    tags).  The arguments are not modified (the one-site terms are summed
+    into a new array)."""
+    from .utils import buildTensor
+    I = np.asarray(I)
+    size = 2 + len(OOs)
+    last = size - 1
+    components = {(0, 0): I, (last, last): I}
+    if len(Os):
+        components[(0, last)] = sum(np.asarray(o, dtype=np.complex128) for o in Os)
+    for k, (first, second) in enumerate(OOs):
+        components[(0, k + 1)] = second
+        components[(k + 1, last)] = first
+    d = len(I)
+    two_site = [TwoSiteOperator(k, 2) for k in range(len(OOs))]
+    return (buildTensor((size, size, d, d), components),
+            [1] + [0] * (size - 1), [Identity()] + two_site + [Complete()],
+            [0] * (size - 1) + [1], [Complete()] + list(two_site) + [Identity()])
+
+
 __all__ = [
     "Identity", "Complete", "OneSiteOperator", "TwoSiteOperator", "TwoSiteOperatorCompressed",
     "LEFT", "RIGHT", "CENTER", "Schedule", "compileSparseSchedule",
     "addStandardCompleteAndIdentityTerms", "contractSparseTensors", "formSparseContractor",
     "getInformationFromOperatorCenter", "makeSimpleSparseOperator", "makeSparseOperator", "mapOverSparseData",
-    "stripAllButIdentityFrom",
+    "stripAllButIdentityFrom", "makeMPO", "Singleton",
 ]

@@ -14,6 +14,7 @@ import numpy as np
 
 from .dense import (Stage3Operator, absorbDenseSideIntoCornerFromLeft, absorbDenseSideIntoCornerFromRight,
                     center_pair, formNormalizationStage1, formNormalizationStage2, _absorb_pairs)
+from .dense import *  # noqa: F401,F403  (the dense contractors are reachable from this module too)
 from ...sparse import (Complete, Identity, OneSiteOperator, TwoSiteOperator, TwoSiteOperatorCompressed,
                        addStandardCompleteAndIdentityTerms, compileSparseSchedule, contractSparseTensors,
                        getInformationFromOperatorCenter)

@@ -247,6 +247,11 @@ class Join:
         return new
 
 
+def computeLengthAndCheckForGaps(indices, error_message):
+    """1 + the largest index, after checking that 0..largest all occur (utils.py:322-332)."""
+    return _length_without_gaps(list(indices), error_message)
+
+
 def _length_without_gaps(indices, message):
     if not indices:
         return 0
@@ -255,6 +260,24 @@ def _length_without_gaps(indices, message):
     if missing:
         raise ValueError(message + ": " + str(missing))
     return length
+
+
+def computePostContractionIndexMap(rank, contracted_indices, offset=0):
+    """Old index -> index after the contracted ones are removed (utils.py:407-416)."""
+    return _surviving_index_map(rank, contracted_indices, offset)
+
+
+def invertPermutation(permutation):
+    permutation = list(permutation)
+    return [permutation.index(i) for i in range(len(permutation))]
+
+
+def applyPermutation(permutation, values):
+    return [values[i] for i in permutation]
+
+
+def applyIndexMapTo(index_map, indices):
+    return [index_map[i] for i in indices]
 
 
 def _surviving_index_map(rank, contracted, offset=0):
@@ -387,8 +410,29 @@ def formDataContractor(joins, final_groups, tensor_ranks=None):
     return contract
 
 
+def prependDataContractor(*args, **keywords):
+    """Decorator: the function receives formDataContractor(*args, **keywords)
+    as its first argument (utils.py:221-223)."""
+    return prepend(formDataContractor(*args, **keywords))
+
+
 def maximumNewBandwidth(direction, shape):
     return int(np.prod(dropAt(shape, direction)))
+
+
+def computeAndCheckNewDimension(shape, direction, by=None, to=None, do_as_much_as_possible=False):
+    """(old, new, increment) of a bandwidth increase of axis ``direction``
+    (utils.py:257-267): the new dimension may not exceed the product of the
+    other axes; with do_as_much_as_possible it is clipped to it instead."""
+    old_dimension = shape[direction]
+    new_dimension = computeNewDimension(old_dimension, by=by, to=to)
+    maximum = maximumNewBandwidth(direction, shape)
+    if new_dimension > maximum:
+        if not do_as_much_as_possible:
+            raise ValueError("New dimension {} is greater than the current maximum dimension for direction {}, "
+                             "which is {} (shape = {}).".format(new_dimension, direction, maximum, tuple(shape)))
+        new_dimension = maximum
+    return old_dimension, new_dimension, new_dimension - old_dimension
 
 
 def __getattr__(name):
@@ -403,6 +447,8 @@ __all__ = [
     "DimensionMismatchError", "InvariantViolatedError", "RelaxFailed", "UnexpectedTensorRankError",
     "Multiplier", "prepend", "Pauli", "O", "L", "R", "A", "OA", "LA", "RA", "dropAt", "replaceAt",
     "computeNewDimension", "crand", "randomComplexSample", "checkForNaNsIn", "multiplyBySingleSiteOperator",
-    "buildProductTensor", "buildTensor", "Join", "formDataContractor",
+    "buildProductTensor", "buildTensor", "Join", "formDataContractor", "prependDataContractor",
+    "computeAndCheckNewDimension", "computeLengthAndCheckForGaps", "computePostContractionIndexMap",
+    "invertPermutation", "applyPermutation", "applyIndexMapTo",
     "maximumNewBandwidth", "relaxOver", "unitize", "computeCompressor", "computeCompressorForMatrixTimesItsDagger",
 ]
