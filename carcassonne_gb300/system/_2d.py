@@ -10,6 +10,9 @@ minimizeExpectation(): the reference runs relaxOver (utils.py:805-878) with a
 budget of 100 multiplications.  ``solver="lanczos"`` (default) instead finds
 the lowest generalized eigenpair of (H_eff, N_eff) to ~1e-13 relative with a
 Cholesky-reduced restarted Lanczos started from the current center;
+``solver="mixed"`` runs the mixed-precision solve (H_eff, N_eff formed on the
+tensor cores from split-BF16 operands, complex64 Lanczos, one FP64 Newton
+correction: FP64-level energies, solve.solve_center) from the current center;
 ``solver="relax"`` runs the reference's algorithm on the GPU.
 """
 from __future__ import annotations
@@ -418,6 +421,12 @@ class System(BaseSystem):
         if self.solver == "relax":
             from ..solver import relaxOver
             self.setStateCenter(relaxOver(self.state_center_data, H, N, maximum_number_of_multiplications=100))
+            return
+        if self.solver == "mixed":
+            from ..solve import solve_center
+            out = solve_center(H, N, x0=self.state_center_data, precision="mixed")
+            self.last_solve = dict(eigenvalue=out["energy"], iterations=out["iterations"])
+            self.setStateCenter(TorchData(out["center"]._t.reshape(self.state_center_data.shape)))
             return
         from ..linalg import hegv_lowest
         lam, x, iters = hegv_lowest(H.formMatrix(), N.formMatrix(), x0=self.state_center_data)

@@ -235,6 +235,27 @@ def test_compress_two_site_operator_new_same_as_old(env, corner_id, direction, t
     assert abs(e2 - e1) < 1e-9
 
 
+@pytest.mark.parametrize("name,step", [("ti", 1), ("ti", 3), ("heis", 0), ("heis", 2), ("ising_ud", 2)])
+def test_mixed_solver_in_the_system(env, name, step):
+    """System with solver="mixed": minimizeExpectation runs the
+    mixed-precision center solve (tensor-core pencil, complex64 Lanczos, FP64
+    Newton correction) from the current center and reaches the reference's
+    ground-state energy of the golden step to 1e-8 relative; the next
+    absorption then runs from that center."""
+    with open(os.path.join(GOLD, "tables.json")) as f:
+        tables = json.load(f)
+    traj = np.load(os.path.join(GOLD, "trajectory.npz"))
+    system = _system_at(env, traj, tables[name]["records"][step], name, step)
+    system.solver = "mixed"
+    e_ref = traj[f"{name}_{step}_E"][0].real
+    system.minimizeExpectation()
+    assert abs(system.last_solve["eigenvalue"] - e_ref) <= 1e-8 * max(1.0, abs(e_ref)), (system.last_solve, e_ref)
+    assert abs(system.computeExpectation() - e_ref) <= 1e-8 * max(1.0, abs(e_ref))
+    system.contractTowards(tables[name]["steps"][step])
+    e, n = system.computeExpectationAndNormalization()
+    assert np.isfinite(complex(e)) and abs(complex(n)) > 0
+
+
 @pytest.mark.parametrize("case", range(6))
 def test_operator_compression_then_absorptions_match_reference(env, case):
     """Operator-term compression (system/_2d.py:229-363), lossless and lossy,
