@@ -318,8 +318,9 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
 // persistent warp-specialised kernel: one CTA per SM walks tiles blockIdx.x,
 // blockIdx.x + gridDim.x, ... N-tile-fastest (the N tiles of one M tile run
 // on neighbouring SMs at the same time, so the A tile is read from HBM once).
-//   warp 0        TMA producer: A and B K-blocks through FG_STAGES stages,
-//                 running ahead into the next tiles
+//   warp 0        TMA producer: A and B K-blocks through fg_stages<BN>()
+//                 stages (3 at BN = 256, else 4), running ahead into the
+//                 next tiles
 //   warp 1        MMA issuer: tile i into TMEM accumulator i % 2
 //   warps 2..17   epilogue: accumulator -> staged FP32 block (four warps
 //                 per TMEM lane quadrant) -> fold -> W; they release the
