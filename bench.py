@@ -14,7 +14,10 @@ between timed steps; e2e: the same metric with the block copied from pinned
 host memory and the result copied back inside the timed region.
 ``--impl reference`` times the CPU restatement of the reference's path on
 the host cores (the reference itself is pure Python/NumPy and is not
-available on the GPU host).
+available on the GPU host) for ``--warmup`` untimed and ``--steps`` timed
+steps of the same block, rank 0 only.  Under torchrun (N > 1) every rank runs
+its own replica of the workload with no data-path collective; the slowest
+rank's time sets the whole-job value.
 """
 from __future__ import annotations
 
