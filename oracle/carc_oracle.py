@@ -3,8 +3,8 @@
 This module is the checker, never the product: only the tests, the smoke
 check and the CPU-baseline leg of the benchmark import it.  It restates, in
 plain numpy, the algorithm of gcross/Carcassonne's center-site path so that
-the CUDA implementation can be compared with it on the GPU machine, where the
-reference itself is not available.
+the CUDA implementation can be compared with it on machines where the
+reference itself is not installed.
 
 Parity pin: every function here is checked against golden vectors produced by
 running the reference itself (``tests/golden/make_golden.py`` imports the
