@@ -614,6 +614,7 @@ int gemm_tile_n(int N) {
 }
 
 int64_t gemm_pad_n(int64_t n) {
+  if (n <= 0) return 0;
   const int64_t nt = (n + 255) / 256;
   return nt * round_up((n + nt - 1) / nt, 16);
 }
