@@ -64,3 +64,20 @@ def test_two_gloo_ranks(tmp_path):
     assert all(g["ms"] == [2.0, 20.0] for g in got)           # the slowest rank's times everywhere
     assigned = sorted(i for g in got for i in g["problems"])
     assert assigned == list(range(5))                          # every problem on exactly one rank
+
+
+def test_batched_problem_distribution():
+    """The batched workload's problems (host side): D in {2..6}, chi in
+    {16, 24, ..., 96} split into ket x bra factors whose product is chi, h in
+    [2, 4), distinct seeds, reproducible from the workload seed."""
+    from carcassonne_gb300 import batched
+    specs = batched.sample_problems(256, 3)
+    assert specs == batched.sample_problems(256, 3)
+    assert {D for D, _, _, _ in specs} == {2, 3, 4, 5, 6}
+    assert {chi for _, chi, _, _ in specs} <= set(range(16, 97, 8))
+    assert all(2.0 <= h < 4.0 for _, _, h, _ in specs)
+    assert len({s for _, _, _, s in specs}) == len(specs)
+    for chi, (ck, cb) in batched.CHI_FACTORS.items():
+        assert ck * cb == chi
+    shards = shard_by_cost([problem_cost(D, chi) for D, chi, _, _ in specs], 8)
+    assert sorted(i for s in shards for i in s) == list(range(256))
