@@ -338,7 +338,7 @@ def run_reference_arm(args, rank):
     line = dict(metric=METRIC, value=res["value"], unit=UNIT, n_gpus=args.gpus, steps=args.steps,
                 warmup=args.warmup, ms_per_step=res["ms_per_step"], higher_is_better=True,
                 scaling="weak", vs_baseline=None, dtype="complex128", data="synthetic",
-                config=dict(WORKLOAD, nvec=args.nvec, parallelism="host threads"), impl="reference",
+                config=dict(WORKLOAD, nvec=args.nvec), parallelism="host threads", impl="reference",
                 cpu_baseline=dict(value=res["value"], unit=UNIT, cores=res["cores"], kind=res["kind"],
                                   sample=res["sample"]),
                 e2e=dict(value=res["value"], unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
@@ -553,8 +553,8 @@ def main():
         fp64_path=None if fp64_ms is None else dict(ms_per_step=fp64_ms,
                                                     value=world * flops_per_step / (fp64_ms * 1e-3) / 1e9),
         data="synthetic: i.i.d. N(0,1) seed 1, unit Frobenius norm per tensor",
-        config=dict(WORKLOAD, nvec=nvec, mode=args.mode, l2="flushed between timed steps (512 MB write)",
-                    parallelism="replicas" if world > 1 else "single GPU"),
+        config=dict(WORKLOAD, nvec=nvec), mode=args.mode, l2="flushed between timed steps (512 MB write)",
+        parallelism="replicas" if world > 1 else "single GPU",
         e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=int(xh.numel() * 16),
                  d2h_bytes_per_step=int(yh.numel() * 16)),
         gpu_launches=int(launches_in_steps),

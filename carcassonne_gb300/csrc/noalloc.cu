@@ -11,7 +11,10 @@
 // The array is CARC_NOALLOC_SCRATCH_BYTES (16 MiB) of device memory that every
 // GPU which loads this library holds until the process exits.  Its device
 // address is looked up once per device, on the first call made with that
-// device current; make that first call before any stream capture.  All calls
+// device current; make that first call before any stream capture.  The
+// cached address belongs to the device's primary context: after
+// cudaDeviceReset (or any other destruction of that context) it is stale, and
+// the library has to be unloaded and loaded again.  All calls
 // share the one array, so calls that overlap on the GPU (on different streams,
 // or from different host threads) race on it and must be serialised by the
 // caller.  No byte of the array needs to start at zero: every byte a call

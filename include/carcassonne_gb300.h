@@ -216,9 +216,12 @@ int64_t carc_stage3_form_matrix_tc_workspace_size(const int64_t* s0_shape, const
  * carc_stage3_matvec_f64_workspace_size) are rejected with CARC_TOO_LARGE.
  * The array's address is looked up on the first call made on each device
  * (with that device current); make that first call before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race and
- * must be serialised by the caller.  No counterpart in the reference (which
- * never manages device memory).
+ * capture.  The address is cached for the life of the process: after
+ * cudaDeviceReset, or anything else that destroys the device's primary
+ * context, it is stale, and the library must be unloaded and loaded again
+ * before the next call.  All calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller.  No counterpart in the
+ * reference (which never manages device memory).
  */
 int carc_stage3_matvec_f64_noalloc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
                                    const void* const* s0_ptrs, int32_t n0,

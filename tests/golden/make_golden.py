@@ -1,7 +1,8 @@
 """Generate golden vectors by running the reference implementation itself.
 
-Run in a container that has the reference checked out (default path below, or
-``CARC_REFERENCE``):  ``python tests/golden/make_golden.py``.  It writes
+Run where the reference is checked out, naming its root with
+``CARC_REFERENCE`` (or ``--reference PATH`` as the first arguments):
+``CARC_REFERENCE=/path/to/Carcassonne python tests/golden/make_golden.py [sections]``.  It writes
 ``dense.npz``, ``tables.json``, ``trajectory.npz`` and ``numerics.npz`` next to
 this file.  The reference's randomness comes from numpy's global generator, so
 every case seeds it (``numpy.random.seed``) before calling into it.
@@ -13,7 +14,13 @@ import sys
 
 import numpy as np
 
-REF = os.environ.get("CARC_REFERENCE", "/root/reference")
+if len(sys.argv) > 2 and sys.argv[1] == "--reference":
+    REF = sys.argv[2]
+    del sys.argv[1:3]
+else:
+    REF = os.environ.get("CARC_REFERENCE")
+if not REF:
+    sys.exit("make_golden.py: set CARC_REFERENCE (or pass --reference PATH) to the reference's checkout")
 sys.path.insert(0, REF)
 sys.dont_write_bytecode = True
 
