@@ -227,7 +227,134 @@ int choose_ksplit(int64_t tiles, int64_t kp) {
 // N tile the plain GEMM uses for a B operand of n rows
 int bn_for(int64_t n) { return gemm_tile_n((int)n); }
 
+// ---- compact operands of the fused matvec (F2 kernel, below) -----------------
+// S2_0, step A's A operand: rows (m, c) for the MA complex rows m = (x0,x1,l0,l1)
+// and c = re / im output row of the real embedding [[a_r, -a_i], [a_i, a_r]];
+// per term a 64-column region [hi plane | lo plane] of the row's (k0 k1, c')
+// entries, the lo plane starting at column Wp = round_up(2 k0 k1, 16).
+// S2_1, step B's B operand: rows (j, c) for j = (l2,l3) (padded to NBB, a
+// multiple of 16) and c = re / im of the output, row (j,0) = [s_r, -s_i] and
+// row (j,1) = [s_i, s_r] over the complex K index kB = (x0,x1,k2,k3); per
+// group a region of 4 KcB columns [hi plane (2 KcB) | lo plane (2 KcB)].
+// 8 bytes per complex entry and plane pair in both, against 32 (S2_0) in the
+// first layout.
+constexpr int F2_XT = 64;    // complex step-A rows per x-tile
+constexpr int F2_MAXG = 8;   // S2_1 tags with terms
+
+struct Geo2 {
+  bool ok;
+  int64_t MA, kc, Wp, KcB, NBB, rowsA;
+};
+
+Geo2 geometry2(const S3& s, const TermGroups& tg) {
+  Geo2 g;
+  memset(&g, 0, sizeof(g));
+  const int64_t L = s.l0 * s.l1, K23 = s.k2 * s.k3;
+  g.MA = s.x0 * s.x1 * L;
+  g.kc = s.k0 * s.k1;
+  g.Wp = round_up(2 * g.kc, 16);
+  g.KcB = s.x0 * s.x1 * K23;
+  g.NBB = round_up(2 * s.l2 * s.l3, 16);
+  g.rowsA = 2 * g.MA;
+  g.ok = K23 == L && L % 4 == 0 && F2_XT % L == 0 && g.MA % F2_XT == 0 && 2 * g.Wp <= 64 && g.NBB <= 128 &&
+         !tg.i1.empty() && (int)tg.i1.size() <= F2_MAXG && (s.d == 1 || s.d == 2 || s.d == 4 || s.d == 8);
+  return g;
+}
+
+int64_t plan2_bytes(const Geo2& g, const TermGroups& tg) {
+  if (!g.ok) return 0;
+  int64_t b = 0;
+  for (auto& v : tg.terms) b += a256(g.rowsA * 64 * (int64_t)v.size() * 2);
+  b += a256(g.NBB * 4 * g.KcB * (int64_t)tg.i1.size() * 2);
+  return b;
+}
+
+__device__ __forceinline__ void split_d(double v, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+  hi = __double2bfloat16(v);
+  lo = __double2bfloat16(v - (double)__bfloat162float(hi));
+}
+
+struct Pack2 {
+  int64_t e[6], st[6];  // the S2 tensor's extents and strides in its own axis order
+  int64_t pitch;        // bf16 per packed row
+  int64_t col0;         // first column of the region
+  int64_t lo_off;       // column offset of the lo plane inside the region
+  int64_t n;            // complex rows (S2_0) / K entries (S2_1)
+  int64_t kc;           // complex K entries per row (S2_0) / rows j (S2_1)
+};
+
+// S2_0 (x0,x1,k0,k1,l0,l1): one thread per (m, k), m = (x0,x1,l0,l1), k = (k0,k1)
+__global__ void pack2_s2_0_kernel(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
+                                  const __grid_constant__ Pack2 p) {
+  const int64_t total = p.n * p.kc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t m = t / p.kc, k = t % p.kc;
+    int64_t r = m;
+    const int64_t l1 = r % p.e[5]; r /= p.e[5];
+    const int64_t l0 = r % p.e[4]; r /= p.e[4];
+    const int64_t x1 = r % p.e[1], x0 = r / p.e[1];
+    const int64_t k1 = k % p.e[3], k0 = k / p.e[3];
+    const double2 a = X[x0 * p.st[0] + x1 * p.st[1] + k0 * p.st[2] + k1 * p.st[3] + l0 * p.st[4] + l1 * p.st[5]];
+    const double e[2][2] = {{a.x, -a.y}, {a.y, a.x}};
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      __nv_bfloat16* row = out + (2 * m + c) * p.pitch + p.col0;
+#pragma unroll
+      for (int cp = 0; cp < 2; ++cp) {
+        __nv_bfloat16 hi, lo;
+        split_d(e[c][cp], hi, lo);
+        row[2 * k + cp] = hi;
+        row[p.lo_off + 2 * k + cp] = lo;
+      }
+    }
+  }
+}
+
+// S2_1 (x1,x0,k2,k3,l2,l3): one thread per (j, kB), j = (l2,l3), kB = (x0,x1,k2,k3)
+__global__ void pack2_s2_1_kernel(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
+                                  const __grid_constant__ Pack2 p) {
+  const int64_t total = p.n * p.kc;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = t / p.n, kb = t % p.n;
+    int64_t r = kb;
+    const int64_t k3 = r % p.e[3]; r /= p.e[3];
+    const int64_t k2 = r % p.e[2]; r /= p.e[2];
+    const int64_t x1 = r % p.e[0], x0 = r / p.e[0];
+    const int64_t l3 = j % p.e[5], l2 = j / p.e[5];
+    const double2 a = X[x1 * p.st[0] + x0 * p.st[1] + k2 * p.st[2] + k3 * p.st[3] + l2 * p.st[4] + l3 * p.st[5]];
+    const double e[2][2] = {{a.x, -a.y}, {a.y, a.x}};
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      __nv_bfloat16* row = out + (2 * j + c) * p.pitch + p.col0;
+#pragma unroll
+      for (int cp = 0; cp < 2; ++cp) {
+        __nv_bfloat16 hi, lo;
+        split_d(e[c][cp], hi, lo);
+        row[2 * kb + cp] = hi;
+        row[p.lo_off + 2 * kb + cp] = lo;
+      }
+    }
+  }
+}
+
+Pack2 pack2_params(const S3& s, const int64_t* ext, const int64_t* st, int64_t pitch, int64_t col0, int64_t lo_off,
+                   int64_t n, int64_t kc) {
+  Pack2 p;
+  memset(&p, 0, sizeof(p));
+  for (int i = 0; i < 6; ++i) {
+    p.e[i] = ext[i];
+    p.st[i] = st[i];
+  }
+  p.pitch = pitch;
+  p.col0 = col0;
+  p.lo_off = lo_off;
+  p.n = n;
+  p.kc = kc;
+  return p;
+}
+
 // plan layout: [per group g: S2_0 step-A operand, rowsA_a x (regA * |T_g|)] [S2_1 step-B operand, rowsB_a x (regB * G)]
+// then, for shapes the F2 kernel takes, [per group g: compact S2_0, rowsA x 64 |T_g|] [compact S2_1, NBB x 4 KcB G]
 int64_t plan_bytes_for(const Geo& g1, const TermGroups& tg) {
   int64_t b = 0;
   for (auto& v : tg.terms) b += a256(g1.rowsA_a * g1.regA * (int64_t)v.size() * 2);
@@ -238,7 +365,7 @@ int64_t plan_bytes_for(const Geo& g1, const TermGroups& tg) {
 }  // namespace
 
 int tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int nvec, int groups, int ksplit) {
-  if (ksplit < 0 || nvec < 1 || groups < 1) return fail(CARC_BAD_ARG, "tc autotune: bad entry");
+  if (ksplit < -2 || nvec < 1 || groups < 1) return fail(CARC_BAD_ARG, "tc autotune: bad entry");
   std::lock_guard<std::mutex> lk(g_tune_mu);
   const TuneKey k = tune_key(s0_shape, s1_shape, d, nvec, groups);
   if (ksplit == 0)
@@ -258,7 +385,8 @@ int64_t stage3_tc_plan_size(const int64_t* s0_shape, const int64_t* s1_shape, co
   S3 s;
   if (s3_shapes(s0_shape, s1_shape, 1, &s) != CARC_OK) return -1;
   if (n_terms < 1) return 256;
-  return plan_bytes_for(geometry(s, 1), group_terms(terms, n_terms));
+  const TermGroups tg = group_terms(terms, n_terms);
+  return plan_bytes_for(geometry(s, 1), tg) + plan2_bytes(geometry2(s, tg), tg);
 }
 
 int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const void* const* s0_ptrs, int n0,
@@ -272,7 +400,8 @@ int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const vo
       return fail(CARC_BAD_ARG, "stage3 tc: term %d out of range", t);
   const TermGroups tg = group_terms(terms, n_terms);
   const Geo g = geometry(s, 1);
-  if (plan_bytes < plan_bytes_for(g, tg)) return fail(CARC_BAD_ARG, "stage3 tc: plan too small");
+  if (plan_bytes < plan_bytes_for(g, tg) + plan2_bytes(geometry2(s, tg), tg))
+    return fail(CARC_BAD_ARG, "stage3 tc: plan too small");
   char* p = static_cast<char*>(plan);
   for (size_t q = 0; q < tg.terms.size(); ++q) {
     const int64_t kp = g.regA * (int64_t)tg.terms[q].size();
@@ -285,6 +414,31 @@ int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const vo
   for (size_t q = 0; q < tg.i1.size(); ++q)
     CARC_RETURN_IF(pack_operand_region(view_s2_1_stepB(s, s1_ptrs[tg.i1[q]]), 0, p, g.rowsB_a, kpB,
                                        (int64_t)q * g.regB, g.regB, stream));
+  p += a256(g.rowsB_a * kpB * 2);
+  // the compact operands of the F2 kernel
+  const Geo2 g2 = geometry2(s, tg);
+  if (!g2.ok) return CARC_OK;
+  const int64_t ext0[6] = {s.x0, s.x1, s.k0, s.k1, s.l0, s.l1};
+  const int64_t ext1[6] = {s.x1, s.x0, s.k2, s.k3, s.l2, s.l3};
+  for (size_t q = 0; q < tg.terms.size(); ++q) {
+    const int64_t pitch = 64 * (int64_t)tg.terms[q].size();
+    CARC_CHECK_CUDA(cudaMemsetAsync(p, 0, g2.rowsA * pitch * 2, stream));
+    for (size_t j = 0; j < tg.terms[q].size(); ++j) {
+      const Pack2 pk = pack2_params(s, ext0, s.s0, pitch, 64 * (int64_t)j, g2.Wp, g2.MA, g2.kc);
+      pack2_s2_0_kernel<<<grid_of(g2.MA * g2.kc), 256, 0, stream>>>(
+          static_cast<const double2*>(s0_ptrs[terms[3 * tg.terms[q][j]]]), reinterpret_cast<__nv_bfloat16*>(p), pk);
+      CARC_CHECK_LAUNCH();
+    }
+    p += a256(g2.rowsA * pitch * 2);
+  }
+  const int64_t pitchB = 4 * g2.KcB * (int64_t)tg.i1.size();
+  CARC_CHECK_CUDA(cudaMemsetAsync(p, 0, g2.NBB * pitchB * 2, stream));
+  for (size_t q = 0; q < tg.i1.size(); ++q) {
+    const Pack2 pk = pack2_params(s, ext1, s.s1, pitchB, 4 * g2.KcB * (int64_t)q, 2 * g2.KcB, g2.KcB, s.l2 * s.l3);
+    pack2_s2_1_kernel<<<grid_of(g2.KcB * s.l2 * s.l3), 256, 0, stream>>>(
+        static_cast<const double2*>(s1_ptrs[tg.i1[q]]), reinterpret_cast<__nv_bfloat16*>(p), pk);
+    CARC_CHECK_LAUNCH();
+  }
   return CARC_OK;
 }
 
@@ -1016,6 +1170,724 @@ bool fused_eligible(const S3& s, int nvec, const TermGroups& tg) {
          L % 4 == 0 && 8 % s.d == 0;
 }
 
+// ---------------------------------------------------------------------------
+// Fused matvec on compact operands (F2): step A and step B in one persistent
+// cooperative kernel, W kept on chip, hi and lo parts of the split summed in
+// the accumulator and the lo x lo product left out.
+//
+// A pair is (x-tile t of 64 complex step-A rows = XP x values x all L rows,
+// S2_1 tag g); a unit is one vector part of a pair (VH parts of NAh complex
+// columns).  Per unit:
+//   MMA-A  TMEM_A[u % 2][(m, re/im) x NAh] = S2_0 tile . Vin part, per term
+//          and K step three products hi.hi + hi.lo + lo.hi (TMA-fed, up to
+//          4 stages of one term each)
+//   fold   TMEM_A -> W^T[u % 2] as step B's A operand in shared memory: row
+//          n_B = (vec, l0, l1, p) of the part, K = the pair's 64 complex
+//          (x, k2, k3), [hi plane | lo plane] of (re, im), 128-byte swizzled
+//   MMA-B  TMEM_B[part][n_B x (j, re/im)] += W^T . S2_1 slice (TMA), three
+//          products per K step, accumulated over all units of the CTA
+// TMEM_B becomes one split-K plane per CTA; after a grid barrier the grid sums
+// the planes into y (compensated FP32 per warp in plane order, FP64 across
+// warps in warp order).  Vin is packed by the whole grid before a first grid
+// barrier.  Roles: warp 0 step-A TMA, warp 1 MMA-A, warps 2..17 fold, warp 18
+// S2_1 TMA, warp 19 MMA-B.  Every wait is bounded; on expiry the CTA aborts,
+// lets its copies land, frees TMEM and flags the caller's status word.
+// Shapes (geometry2 and f2_eligible): k2 k3 == l0 l1 = L, L % 4 == 0, L
+// divides 64, x0 x1 L a multiple of 64, 2 round_up(2 k0 k1, 16) <= 64,
+// 2 l2 l3 <= 128, d in {1, 2, 4, 8}, NAh = nvec L d / VH a multiple of 16
+// up to 128, at most 8 S2_1 tags with terms.
+// ---------------------------------------------------------------------------
+constexpr int F2_THREADS = 640;
+constexpr int F2_STAGES = 4;
+constexpr int F2_STAGE_A = 128 * 128;   // A tile: 128 rows x 64 bf16
+constexpr int F2_AB_ATOM = 128 * 128;   // W^T: 128 rows x 64 bf16 per atom
+constexpr int F2_AB = 4 * F2_AB_ATOM;   // W^T: [hi 128 | lo 128] columns
+constexpr int F2_SMEM_MAX = 227 * 1024;
+constexpr int F2_PF_PAIRS = 2;          // L2 prefetch distance, in pairs
+
+struct Vin2 {
+  int n;
+  int64_t rows, kc, k23, d, wp2;          // wp2: u32 column of the lo plane
+  const double2* op[kVinTermsPerLaunch];
+  int64_t dst[kVinTermsPerLaunch];        // u32 offset of the term's region in row 0
+  int64_t pitch[kVinTermsPerLaunch];      // u32 per row
+};
+
+// one u32 (bf16 pair) of a packed Vin region: row n = (vec, k2, k3, p),
+// column col in [0, 32): hi (re, im) of k = col below wp2, lo of k = col - wp2
+// in [wp2, 2 wp2), zero elsewhere and for k >= kc
+__device__ __forceinline__ void pack_vin2_slot(const double2* __restrict__ x, uint32_t* __restrict__ out,
+                                               const Vin2& p, int term, int t) {
+  const int n = t >> 5, col = t & 31;
+  const int kc = (int)p.kc, k23 = (int)p.k23, d = (int)p.d, wp2 = (int)p.wp2;
+  int k = col;
+  bool lo = false;
+  if (col >= wp2) {
+    k = col - wp2;
+    lo = true;
+  }
+  uint32_t word = 0u;
+  if (k < kc && col < 2 * wp2) {
+    const double2* O = p.op[term];
+    const int q = n / d, pp = n - q * d;
+    const int vec = q / k23, kk = q - vec * k23;
+    const double2* xv = x + (((int64_t)vec * kc + k) * k23 + kk) * d;
+    float fr, fi;
+    if (O == nullptr) {
+      const double2 v = xv[pp];
+      fr = (float)v.x;
+      fi = (float)v.y;
+    } else {
+      fr = 0.f;
+      fi = 0.f;
+      for (int qq = 0; qq < d; ++qq) {
+        const double2 o = O[pp * d + qq], v = xv[qq];
+        const float orr = (float)o.x, oi = (float)o.y, vr = (float)v.x, vi = (float)v.y;
+        fr = fmaf(orr, vr, fmaf(-oi, vi, fr));
+        fi = fmaf(orr, vi, fmaf(oi, vr, fi));
+      }
+    }
+    const __nv_bfloat16 hr = __float2bfloat16_rn(fr), hm = __float2bfloat16_rn(fi);
+    __nv_bfloat162 w2;
+    if (lo)
+      w2 = __halves2bfloat162(__float2bfloat16_rn(fr - __bfloat162float(hr)),
+                              __float2bfloat16_rn(fi - __bfloat162float(hm)));
+    else
+      w2 = __halves2bfloat162(hr, hm);
+    word = *reinterpret_cast<const uint32_t*>(&w2);
+  }
+  out[p.dst[term] + (int64_t)n * p.pitch[term] + col] = word;
+}
+
+struct F2Maps {
+  CUtensorMap a[F2_MAXG];    // compact S2_0 of group g: rows (m, re/im), one 64-column region per term
+  CUtensorMap vin[F2_MAXG];  // Vin of group g: rows (vec, k2, k3, p), box NAh rows
+  CUtensorMap b;             // compact S2_1: rows (j, re/im), regions of 4 KcB per group
+};
+
+struct F2Params {
+  int n_pairs, x_tiles, G;
+  int nterm[F2_MAXG];
+  int VH, NAh, NBh, NBB, nksA;
+  int stages, stage_bytes;
+  int L, K23, XP;
+  int64_t kcB4, kcB2;
+  float* planes;  // [grid][VH][NBB][128] (column-major per part)
+  int* err;
+  Vin2 vt;
+  const double2* x;
+  uint32_t* vin;
+  double2* y;
+  int accumulate;
+  int nvec, l0, l1, l2, l3;
+  int64_t yv, yl0, yl1, yl2, yl3;
+  unsigned int* sync;
+  int* abort_word;  // raised by a CTA whose grid barrier timed out
+};
+
+__device__ bool f2_grid_barrier(unsigned int* ctr, int* abort_word, volatile int* abort) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(ctr, 1u);
+    uint32_t i = 0;
+    for (; i < (1u << 22); ++i) {
+      unsigned int v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
+      if (v >= gridDim.x) break;
+      if ((i & 255u) == 255u && *reinterpret_cast<volatile int*>(abort_word)) break;
+      __nanosleep(64);
+    }
+    if (i == (1u << 22)) atomicExch(abort_word, 1);
+    if (*reinterpret_cast<volatile int*>(abort_word)) *abort = 1;
+  }
+  __syncthreads();
+  return *abort == 0;
+}
+
+template <int DD>
+__global__ __launch_bounds__(F2_THREADS, 1) void stage3_fused2_kernel(const __grid_constant__ F2Maps maps,
+                                                                      const __grid_constant__ F2Params p) {
+  using namespace umma;
+  extern __shared__ uint8_t f2sm_raw[];
+  uint8_t* sm = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(f2sm_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* stage = sm;                                      // stages x (A tile, Vin part)
+  uint8_t* aB = sm + p.stages * p.stage_bytes;              // W^T: 2 buffers x 4 atoms of 128 rows
+  const int bb_atom = p.NBB * 128;
+  uint8_t* bB = aB + 2 * F2_AB;                             // 2 buffers x 4 atoms of NBB rows
+  uint64_t* bars = reinterpret_cast<uint64_t*>(bB + 8 * bb_atom);
+  uint64_t* full = bars;           // [4]
+  uint64_t* empty = bars + 4;      // [4]
+  uint64_t* accA_full = bars + 8;  // [2] MMA-A of the unit committed into TMEM_A[u % 2]
+  uint64_t* fold_done = bars + 10; // [2] fold of unit u finished (TMEM_A[u % 2] read, W^T[u % 2] written)
+  uint64_t* aB_free = bars + 12;   // [2] MMA-B of unit u done reading W^T[u % 2]
+  uint64_t* bB_full = bars + 14;   // [2] per pair parity
+  uint64_t* bB_empty = bars + 16;  // [2]
+  uint64_t* doneB = bars + 18;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 19);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < F2_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&accA_full[b], 1);
+      mbar_init(&fold_done[b], 16);
+      mbar_init(&aB_free[b], 1);
+      mbar_init(&bB_full[b], 1);
+      mbar_init(&bB_empty[b], 1);
+    }
+    mbar_init(doneB, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  // rows [NBh, 128) of W^T feed only discarded output rows; zero them once
+  if (p.NBh < 128) {
+    for (int a = 0; a < 8; ++a) {
+      uint4* z = reinterpret_cast<uint4*>(aB + a * F2_AB_ATOM + p.NBh * 128);
+      for (int i = threadIdx.x; i < (128 - p.NBh) * 8; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+    }
+    fence_proxy_async();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, 512);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tB = tmem + 256;
+  const uint32_t stepA_bytes = (uint32_t)(F2_STAGE_A + p.NAh * 128);
+
+  // S2_0 tiles of the first stages and the first pair's S2_1 slice do not
+  // depend on Vin: requested before the packing phase
+  const int my_pairs0 = blockIdx.x < p.n_pairs ? (p.n_pairs - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  int pre = 0;
+  PairWalk cwB((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+  int pcB0 = 0;
+  auto load_bB = [&](int pc, const PairWalk& w) {
+    const int sb = pc & 1;
+    uint8_t* dst = bB + sb * 4 * bb_atom;
+    mbar_arrive_expect_tx(&bB_full[sb], (uint32_t)(4 * bb_atom));
+    const int x0 = (int)(w.g * p.kcB4 + 2 * (int64_t)w.t * F2_XT);
+    tma_load_2d(dst, &maps.b, x0, 0, &bB_full[sb]);
+    tma_load_2d(dst + bb_atom, &maps.b, x0 + 64, 0, &bB_full[sb]);
+    tma_load_2d(dst + 2 * bb_atom, &maps.b, (int)(x0 + p.kcB2), 0, &bB_full[sb]);
+    tma_load_2d(dst + 3 * bb_atom, &maps.b, (int)(x0 + p.kcB2 + 64), 0, &bB_full[sb]);
+  };
+  // L2 prefetch of a pair's S2_0 tiles / S2_1 slice
+  auto prefetch_a = [&](const PairWalk& w) {
+    for (int j = 0; j < p.nterm[w.g]; ++j) tma_prefetch_2d(&maps.a[w.g], j * 64, w.t * 128);
+  };
+  auto prefetch_b = [&](const PairWalk& w) {
+    const int x0 = (int)(w.g * p.kcB4 + 2 * (int64_t)w.t * F2_XT);
+    tma_prefetch_2d(&maps.b, x0, 0);
+    tma_prefetch_2d(&maps.b, x0 + 64, 0);
+    tma_prefetch_2d(&maps.b, (int)(x0 + p.kcB2), 0);
+    tma_prefetch_2d(&maps.b, (int)(x0 + p.kcB2 + 64), 0);
+  };
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < p.G; ++q) {
+      prefetch_tensormap(&maps.a[q]);
+      prefetch_tensormap(&maps.vin[q]);
+    }
+    prefetch_tensormap(&maps.b);
+    PairWalk w((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+    {  // pairs 0 .. F2_PF_PAIRS into L2 while Vin is packed
+      PairWalk w2 = w;
+      for (int k = 0; k <= F2_PF_PAIRS && k < my_pairs0; ++k, w2.next()) prefetch_a(w2);
+    }
+    for (int uc = 0, part = 0, j = 0; pre < p.stages && uc < my_pairs0 * p.VH; ++pre) {
+      mbar_arrive_expect_tx(&full[pre], stepA_bytes);
+      tma_load_2d(stage + pre * p.stage_bytes, &maps.a[w.g], j * 64, w.t * 128, &full[pre]);
+      if (++j == p.nterm[w.g]) {
+        j = 0;
+        ++uc;
+        if (++part == p.VH) {
+          part = 0;
+          w.next();
+        }
+      }
+    }
+  } else if (threadIdx.x == 18 * 32 && my_pairs0 > 0) {
+    load_bB(0, cwB);
+    cwB.next();
+    pcB0 = 1;
+    PairWalk w2 = cwB;
+    for (int k = 1; k <= F2_PF_PAIRS && k < my_pairs0; ++k, w2.next()) prefetch_b(w2);
+  }
+  // ---- phase 0: Vin of every term packed by the whole grid
+  {
+    const int per_term = (int)(p.vt.rows * 32), total = per_term * p.vt.n;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+      const int term = e / per_term;
+      pack_vin2_slot(p.x, p.vin, p.vt, term, e - term * per_term);
+    }
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    f2_grid_barrier(p.sync, p.abort_word, abort_flag);
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+  }
+  const int my_pairs = (my_pairs0 > 0 && *abort_flag == 0) ? my_pairs0 : 0;
+  const int n_units = my_pairs * p.VH;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // ---- step-A producer: per unit and term, the S2_0 tile and the Vin part
+      int issued = 0, s = 0, part = 0;
+      uint32_t ph = 0;
+      bool ok = true;
+      PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+      PairWalk pw = cw;  // L2 prefetch of the S2_0 tiles F2_PF_PAIRS pairs ahead
+      for (int k = 0; k < F2_PF_PAIRS; ++k) pw.next();
+      for (int uc = 0; ok && uc < n_units; ++uc) {
+        if (part == 0 && uc / p.VH + F2_PF_PAIRS < my_pairs) prefetch_a(pw);
+        const int g = cw.g, t = cw.t;
+        for (int j = 0; j < p.nterm[g]; ++j) {
+          uint8_t* st = stage + s * p.stage_bytes;
+          if (issued >= pre) {
+            if (!(ok = mbar_wait_sleep(&empty[s], ph ^ 1u, abort_flag))) break;
+            mbar_arrive_expect_tx(&full[s], stepA_bytes);
+            tma_load_2d(st, &maps.a[g], j * 64, t * 128, &full[s]);
+          }
+          tma_load_2d(st + F2_STAGE_A, &maps.vin[g], j * 64, part * p.NAh, &full[s]);
+          ++issued;
+          if (++s == p.stages) {
+            s = 0;
+            ph ^= 1u;
+          }
+        }
+        if (++part == p.VH) {
+          part = 0;
+          cw.next();
+          pw.next();
+        }
+      }
+      if (*abort_flag) {
+        // stages whose S2_0 tile was requested but not their Vin part get an
+        // in-bounds Vin box, then every copy in flight is let land (bounded)
+        for (; issued < pre; ++issued)
+          tma_load_2d(stage + issued * p.stage_bytes + F2_STAGE_A, &maps.vin[0], 0, 0, &full[issued]);
+        for (int i = max(0, issued - p.stages); i < issued; ++i)
+          for (uint32_t q = 0; q < (1u << 20); ++q)
+            if (mbar_try_wait(&full[i % p.stages], (uint32_t)((i / p.stages) & 1))) break;
+      }
+    }
+  } else if (warp == 18) {
+    if (lane == 0) {
+      // ---- step-B producer: the pair's S2_1 slice (4 atoms), double-buffered
+      int issued = pcB0;
+      PairWalk cw = cwB;
+      for (int pc = pcB0; pc < my_pairs; ++pc) {
+        if (pc >= 2 && !mbar_wait_sleep(&bB_empty[pc & 1], (uint32_t)(((pc >> 1) & 1) ^ 1), abort_flag)) break;
+        load_bB(pc, cw);
+        ++issued;
+        cw.next();
+        if (pc + F2_PF_PAIRS < my_pairs) {
+          PairWalk w2 = cw;
+          for (int k = 1; k < F2_PF_PAIRS; ++k) w2.next();
+          prefetch_b(w2);
+        }
+      }
+      if (*abort_flag)
+        for (int i = max(0, issued - 2); i < issued; ++i)
+          for (uint32_t q = 0; q < (1u << 20); ++q)
+            if (mbar_try_wait(&bB_full[i & 1], (uint32_t)((i >> 1) & 1))) break;
+    }
+  } else if (warp == 1) {
+    // ---- MMA-A issuer (converged warp, one elected lane issues)
+    const bool leader = elect_one();
+    const uint32_t idA = idesc_bf16_f32(128, p.NAh);
+    const uint64_t dStage = smem_desc_sw128(smem_u32(stage));
+    const uint32_t dStageStep = (uint32_t)p.stage_bytes >> 4;
+    constexpr uint32_t dV = F2_STAGE_A >> 4;
+    const int nks = p.nksA;
+    int s = 0, part = 0;
+    uint32_t ph = 0;
+    bool ok = true;
+    PairWalk cw((int)blockIdx.x, (int)gridDim.x, p.x_tiles);
+    for (int uc = 0; ok && uc < n_units; ++uc) {
+      const int b = uc & 1;
+      // TMEM_A[b] was last read by the fold of unit uc - 2
+      if (uc >= 2 && !(ok = mbar_wait_sleep(&fold_done[b], (uint32_t)(((uc >> 1) & 1) ^ 1), abort_flag))) break;
+      const uint32_t tA = tmem + (uint32_t)(b * 128);
+      const int nt = p.nterm[cw.g];
+      for (int j = 0; j < nt; ++j) {
+        if (!(ok = mbar_wait_sleep(&full[s], ph, abort_flag))) break;
+        tc_fence_after();
+        if (leader) {
+          const uint64_t da = dStage + s * dStageStep, dv = da + dV;
+          for (int kk = 0; kk < nks; ++kk) {
+            mma_bf16(tA, da + kk * 2, dv + kk * 2, idA, (j > 0 || kk > 0) ? 1u : 0u);  // hi . hi
+            mma_bf16(tA, da + kk * 2, dv + (nks + kk) * 2, idA, 1u);                     // hi . lo
+            mma_bf16(tA, da + (nks + kk) * 2, dv + kk * 2, idA, 1u);                     // lo . hi
+          }
+          mma_commit(&empty[s]);
+        }
+        __syncwarp();
+        if (++s == p.stages) {
+          s = 0;
+          ph ^= 1u;
+        }
+      }
+      if (!ok) break;
+      if (leader) mma_commit(&accA_full[b]);
+      __syncwarp();
+      if (++part == p.VH) {
+        part = 0;
+        cw.next();
+      }
+    }
+  } else if (warp == 19) {
+    // ---- MMA-B issuer
+    const bool leader = elect_one();
+    const uint32_t idB = idesc_bf16_f32(128, p.NBB);
+    const uint64_t dAB = smem_desc_sw128(smem_u32(aB)), dBB = smem_desc_sw128(smem_u32(bB));
+    constexpr uint32_t dAtomA = F2_AB_ATOM >> 4;
+    const uint32_t dAtomB = (uint32_t)bb_atom >> 4;
+    bool ok = true;
+    int part = 0, pc = 0;
+    for (int uc = 0; ok && uc < n_units; ++uc) {
+      if (!(ok = mbar_wait_sleep(&fold_done[uc & 1], (uint32_t)((uc >> 1) & 1), abort_flag))) break;
+      if (part == 0 && !(ok = mbar_wait_sleep(&bB_full[pc & 1], (uint32_t)((pc >> 1) & 1), abort_flag))) break;
+      tc_fence_after();
+      if (leader) {
+        const uint32_t d = tB + (uint32_t)(part * p.NBB);
+        const uint64_t bb = dBB + (uint32_t)((pc & 1) * 4) * dAtomB;
+        const uint64_t da = dAB + (uint32_t)((uc & 1) * 4) * dAtomA;
+#pragma unroll
+        for (int kk = 0; kk < 8; ++kk) {
+          const uint32_t oa = (uint32_t)(kk >> 2) * dAtomA + (uint32_t)(kk & 3) * 2;
+          const uint32_t ob = (uint32_t)(kk >> 2) * dAtomB + (uint32_t)(kk & 3) * 2;
+          mma_bf16(d, da + oa, bb + ob, idB, (pc > 0 || kk > 0) ? 1u : 0u);  // hi . hi
+          mma_bf16(d, da + oa, bb + 2 * dAtomB + ob, idB, 1u);                // hi . lo
+          mma_bf16(d, da + 2 * dAtomA + oa, bb + ob, idB, 1u);                // lo . hi
+        }
+        mma_commit(&aB_free[uc & 1]);
+        if (part == p.VH - 1) mma_commit(&bB_empty[pc & 1]);
+      }
+      __syncwarp();
+      if (++part == p.VH) {
+        part = 0;
+        ++pc;
+      }
+    }
+    if (leader) mma_commit(doneB);
+    __syncwarp();
+  } else if (warp >= 2 && warp <= 17) {
+    // ---- fold: TMEM_A (lanes (m, re/im), columns n of the part) -> W^T.
+    // The quadrant's 4 warps take the 32-column chunks ci = 0..3 (NAh / 32
+    // of them carry columns).  Lane pair (m, re), (m, im) exchanges halves
+    // so that each lane ends with 4 sets of 4 complex values, a set being 4
+    // consecutive k2 k3 of one (vec, p): 16 contiguous bytes of a W^T row
+    // per plane.  Set S holds chunk columns (S / d) 4d + e d + S % d.
+    const int quad = warp & 3, ci = (warp - 2) >> 2;
+    const int csel = lane & 1;
+    const int m = quad * 16 + (lane >> 1);  // complex step-A row within the x-tile
+    const int xp = m / p.L, l = m - xp * p.L;
+    const bool has_chunk = ci * 32 < p.NAh;
+    uint32_t offs[4];
+#pragma unroll
+    for (int s2 = 0; s2 < 4; ++s2) {
+      const int S = 2 * s2 + csel;
+      const int n = ci * 32 + (S / DD) * 4 * DD + S % DD;  // part column of element 0 of set S
+      const int pp = n % DD, q = n / DD;
+      const int k23 = q % p.K23, vec = q / p.K23;
+      const int row = (vec * p.L + l) * DD + pp;            // W^T row n_B
+      const int kb = xp * p.K23 + k23;                      // complex K column (multiple of 4)
+      offs[s2] = (uint32_t)((kb >> 5) * F2_AB_ATOM + (row >> 3) * 1024 + (row & 7) * 128 +
+                            ((((kb & 31) >> 2) ^ (row & 7)) << 4));
+    }
+    auto setcol = [](int S, int e) { return (S / DD) * 4 * DD + e * DD + S % DD; };
+    const uint32_t sh0 = smem_u32(aB);
+    bool ok = true;
+    for (int uc = 0; uc < n_units; ++uc) {
+      const int b = uc & 1;
+      if (!(ok = mbar_wait_sleep(&accA_full[b], (uint32_t)((uc >> 1) & 1), abort_flag))) break;
+      // W^T[b] was last read by the MMA-B of unit uc - 2
+      if (uc >= 2 && !(ok = mbar_wait_sleep(&aB_free[b], (uint32_t)(((uc >> 1) & 1) ^ 1), abort_flag))) break;
+      tc_fence_after();
+      if (has_chunk) {
+        const uint32_t sh = sh0 + (uint32_t)(b * F2_AB);
+        uint32_t r[32];
+        tmem_ld_32x32b_x32(tmem + (uint32_t)(b * 128) + ((uint32_t)(quad * 32) << 16) + (uint32_t)(ci * 32), r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int s2 = 0; s2 < 4; ++s2) {
+          uint32_t hi[4], lo[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            // this lane keeps set 2 s2 + csel, the partner set 2 s2 + (1 - csel)
+            const float a = __uint_as_float(r[setcol(2 * s2, e)]);
+            const float z = __uint_as_float(r[setcol(2 * s2 + 1, e)]);
+            const float keep = csel ? z : a, send = csel ? a : z;
+            const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+            const float re = csel ? recv : keep, im = csel ? keep : recv;
+            const __nv_bfloat162 h2 = __floats2bfloat162_rn(re, im);
+            const float2 hf = __bfloat1622float2(h2);
+            const __nv_bfloat162 l2 = __floats2bfloat162_rn(re - hf.x, im - hf.y);
+            hi[e] = *reinterpret_cast<const uint32_t*>(&h2);
+            lo[e] = *reinterpret_cast<const uint32_t*>(&l2);
+          }
+          const uint32_t off = offs[s2];
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(sh + off), "r"(hi[0]), "r"(hi[1]),
+                       "r"(hi[2]), "r"(hi[3])
+                       : "memory");
+          asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(sh + 2 * F2_AB_ATOM + off), "r"(lo[0]),
+                       "r"(lo[1]), "r"(lo[2]), "r"(lo[3])
+                       : "memory");
+        }
+      }
+      fence_proxy_async();
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&fold_done[b]);
+    }
+    // ---- TMEM_B -> this CTA's planes [VH][NBB][128]
+    const bool done = ok && mbar_wait_sleep(doneB, 0, abort_flag);
+    tc_fence_after();
+    const int nchunk = (p.VH * p.NBB + 31) / 32;
+    if (done && ci < nchunk) {
+      float* plane = p.planes + (int64_t)blockIdx.x * p.VH * p.NBB * 128;
+      const int row = quad * 32 + lane;
+      for (int c0 = ci * 32; c0 < p.VH * p.NBB; c0 += 4 * 32) {
+        uint32_t r[32];
+        tmem_ld_32x32b_x32(tB + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int j = 0; j < 32; ++j)
+          if (c0 + j < p.VH * p.NBB) plane[(int64_t)(c0 + j) * 128 + row] = n_units > 0 ? __uint_as_float(r[j]) : 0.f;
+      }
+    } else if (!done && ci < nchunk) {
+      // an aborted CTA leaves zeros (the status word reports the abort)
+      float* plane = p.planes + (int64_t)blockIdx.x * p.VH * p.NBB * 128;
+      const int row = quad * 32 + lane;
+      for (int c0 = ci * 32; c0 < p.VH * p.NBB; c0 += 4 * 32)
+        for (int j = 0; j < 32 && c0 + j < p.VH * p.NBB; ++j) plane[(int64_t)(c0 + j) * 128 + row] = 0.f;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 512);
+  }
+  if (f2_grid_barrier(p.sync + 1, p.abort_word, abort_flag) && warp >= 2 && warp <= 17) {
+    // ---- phase 2: planes of all CTAs summed into y.  Item = (part, j, 32
+    // rows n_B), one per CTA at a time; its 16 warps take planes w, w + 16,
+    // ... (compensated FP32, re and im, one batch of loads for up to 160
+    // planes), the partials are added in FP64 in warp order.
+    const int wq = warp - 2;
+    double* part_sum = reinterpret_cast<double*>(stage);
+    const int l23 = p.l2 * p.l3, rgs = (p.NBh + 31) / 32;
+    const int n_items = p.VH * l23 * rgs;
+    const int64_t pstride = (int64_t)p.VH * p.NBB * 128;
+    for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+      const int rg = it % rgs, rest = it / rgs;
+      const int j = rest % l23, pt = rest / l23;
+      const int r = rg * 32 + lane;
+      const float* src = p.planes + (int64_t)(pt * p.NBB + 2 * j) * 128 + r;
+      Kahan are, aim;
+      for (int z0 = wq; z0 < (int)gridDim.x; z0 += 10 * 16) {
+        float vr[10], vi[10];
+#pragma unroll
+        for (int u = 0; u < 10; ++u) {
+          const int z = z0 + u * 16;
+          vr[u] = z < (int)gridDim.x ? __ldcg(src + z * pstride) : 0.f;
+          vi[u] = z < (int)gridDim.x ? __ldcg(src + z * pstride + 128) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 10; ++u) {
+          are.add(vr[u]);
+          aim.add(vi[u]);
+        }
+      }
+      part_sum[wq * 64 + lane] = are.value();
+      part_sum[wq * 64 + 32 + lane] = aim.value();
+      asm volatile("bar.sync 2, 512;" ::: "memory");
+      if (wq == 0 && r < p.NBh) {
+        double vre = part_sum[lane], vim = part_sum[32 + lane];
+        for (int q = 1; q < 16; ++q) {
+          vre += part_sum[q * 64 + lane];
+          vim += part_sum[q * 64 + 32 + lane];
+        }
+        // n_B = (vec_local, l0, l1, p) of part pt; j = (l2, l3)
+        int nn = r;
+        const int pi = nn % DD;
+        nn /= DD;
+        const int l1i = nn % p.l1;
+        nn /= p.l1;
+        const int l0i = nn % p.l0, vec = pt * (p.nvec / p.VH) + nn / p.l0;
+        const int64_t off = (j / p.l3) * p.yl2 + (j % p.l3) * p.yl3 + vec * p.yv + l0i * p.yl0 + l1i * p.yl1 + pi;
+        double2 val = make_double2(vre, vim);
+        if (p.accumulate) val = cadd(val, p.y[off]);
+        p.y[off] = val;
+      }
+      asm volatile("bar.sync 2, 512;" ::: "memory");
+    }
+  }
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(p.err, CARC_NOT_CONVERGED);
+}
+
+// F2 launch geometry for nvec centers, or VH = 0 when the kernel does not take them
+struct F2Geo {
+  int VH, NAh, NBh;
+};
+
+F2Geo f2_geo(const S3& s, const Geo2& g2, int nvec) {
+  F2Geo f{0, 0, 0};
+  if (!g2.ok) return f;
+  const int64_t NA = (int64_t)nvec * s.k2 * s.k3 * s.d;
+  int VH = NA <= 128 ? 1 : 2;
+  if (VH == 2 && nvec % 2 != 0) return f;
+  const int64_t NAh = NA / VH;
+  if (NAh % 16 != 0 || NAh > 128 || NAh < 16) return f;
+  f.VH = VH;
+  f.NAh = (int)NAh;
+  f.NBh = (int)NAh;  // k2 k3 == l0 l1
+  return f;
+}
+
+int f2_grid(const S3& s, const Geo2& g2, const TermGroups& tg) {
+  const int64_t pairs = (g2.MA / F2_XT) * (int64_t)tg.i1.size();
+  return (int)std::max<int64_t>(1, std::min<int64_t>(152, pairs));
+}
+
+int64_t f2_ws_bytes(const S3& s, const Geo2& g2, const TermGroups& tg, int nvec) {
+  const F2Geo f = f2_geo(s, g2, nvec);
+  if (!f.VH) return 0;
+  int64_t vin = 0;
+  for (auto& v : tg.terms) vin += a256((int64_t)f.NAh * f.VH * 64 * (int64_t)v.size() * 2);
+  const int64_t planes = (int64_t)f2_grid(s, g2, tg) * f.VH * g2.NBB * 128 * 4;
+  return vin + a256(planes) + 256;
+}
+
+// Enqueues the cooperative F2 launch; *done tells whether it was accepted (a
+// grid that cannot be co-resident is refused before anything runs).
+int launch_fused2(const S3& s, int nvec, const TermGroups& tg, const Geo2& g2, const void* plan2, void* ws,
+                  const double2* x, double2* y, const void* const* op_ptrs, const int32_t* terms, int accumulate,
+                  bool* done, int* status, cudaStream_t stream) {
+  *done = false;
+  const F2Geo f = f2_geo(s, g2, nvec);
+  if (!f.VH) return CARC_OK;
+  const int G = (int)tg.i1.size();
+  int n_terms_all = 0;
+  for (auto& v : tg.terms) n_terms_all += (int)v.size();
+  if (n_terms_all > kVinTermsPerLaunch) return CARC_OK;
+  F2Maps maps;
+  memset(&maps, 0, sizeof(maps));
+  F2Params fp;
+  memset(&fp, 0, sizeof(fp));
+  fp.VH = f.VH;
+  fp.NAh = f.NAh;
+  fp.NBh = f.NBh;
+  fp.NBB = (int)g2.NBB;
+  fp.nksA = (int)(g2.Wp / 16);
+  fp.L = (int)(s.l0 * s.l1);
+  fp.K23 = (int)(s.k2 * s.k3);
+  fp.XP = F2_XT / fp.L;
+  fp.x_tiles = (int)(g2.MA / F2_XT);
+  fp.G = G;
+  fp.n_pairs = fp.x_tiles * G;
+  fp.kcB4 = 4 * g2.KcB;
+  fp.kcB2 = 2 * g2.KcB;
+  // workspace: [Vin per group][planes][sync, abort word]
+  char* w = static_cast<char*>(ws);
+  std::vector<int64_t> vin_off;
+  int64_t vin_bytes = 0;
+  for (auto& v : tg.terms) {
+    vin_off.push_back(vin_bytes);
+    vin_bytes += a256((int64_t)f.NAh * f.VH * 64 * (int64_t)v.size() * 2);
+  }
+  const int grid = f2_grid(s, g2, tg);
+  float* planes = reinterpret_cast<float*>(w + vin_bytes);
+  char* sync = w + vin_bytes + a256((int64_t)grid * f.VH * g2.NBB * 128 * 4);
+  const char* pA = static_cast<const char*>(plan2);
+  const int64_t NA = (int64_t)f.NAh * f.VH;
+  Vin2 vt;
+  memset(&vt, 0, sizeof(vt));
+  vt.rows = NA;
+  vt.kc = s.k0 * s.k1;
+  vt.k23 = s.k2 * s.k3;
+  vt.d = s.d;
+  vt.wp2 = g2.Wp / 2;
+  for (int q = 0; q < G; ++q) {
+    const int nt = (int)tg.terms[q].size();
+    fp.nterm[q] = nt;
+    CARC_RETURN_IF(tma_map_bf16(&maps.a[q], pA, (uint64_t)(64 * nt), (uint64_t)g2.rowsA, 128));
+    CARC_RETURN_IF(tma_map_bf16(&maps.vin[q], w + vin_off[q], (uint64_t)(64 * nt), (uint64_t)NA, (uint32_t)f.NAh));
+    pA += a256(g2.rowsA * 64 * (int64_t)nt * 2);
+    for (int j = 0; j < nt; ++j) {
+      const int io = terms[3 * tg.terms[q][j] + 2];
+      vt.op[vt.n] = io < 0 ? nullptr : static_cast<const double2*>(op_ptrs[io]);
+      vt.dst[vt.n] = vin_off[q] / 4 + (int64_t)j * 32;
+      vt.pitch[vt.n] = 32 * (int64_t)nt;
+      ++vt.n;
+    }
+  }
+  CARC_RETURN_IF(tma_map_bf16(&maps.b, pA, (uint64_t)(4 * g2.KcB * G), (uint64_t)g2.NBB, (uint32_t)g2.NBB));
+  fp.stage_bytes = F2_STAGE_A + f.NAh * 128;
+  const int fixed = 1024 + 2 * F2_AB + 8 * (int)g2.NBB * 128 + 256;
+  fp.stages = std::min(F2_STAGES, (F2_SMEM_MAX - fixed) / fp.stage_bytes);
+  if (fp.stages < 2) return CARC_OK;
+  const int smem = fixed + fp.stages * fp.stage_bytes;
+  fp.planes = planes;
+  fp.err = status;
+  fp.vt = vt;
+  fp.x = x;
+  fp.vin = reinterpret_cast<uint32_t*>(w);
+  fp.y = y;
+  fp.accumulate = accumulate;
+  fp.nvec = nvec;
+  fp.l0 = (int)s.l0;
+  fp.l1 = (int)s.l1;
+  fp.l2 = (int)s.l2;
+  fp.l3 = (int)s.l3;
+  fp.yl3 = s.d;
+  fp.yl2 = s.l3 * fp.yl3;
+  fp.yl1 = s.l2 * fp.yl2;
+  fp.yl0 = s.l1 * fp.yl1;
+  fp.yv = s.l0 * fp.yl0;
+  fp.sync = reinterpret_cast<unsigned int*>(sync);
+  fp.abort_word = reinterpret_cast<int*>(sync + 8);
+  static std::once_flag once;
+  static cudaError_t attr = cudaSuccess;
+  std::call_once(once, [] {
+    for (auto k : {stage3_fused2_kernel<1>, stage3_fused2_kernel<2>, stage3_fused2_kernel<4>, stage3_fused2_kernel<8>}) {
+      const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, F2_SMEM_MAX);
+      if (e != cudaSuccess) attr = e;
+    }
+  });
+  if (attr != cudaSuccess) return fail(CARC_CUDA_ERROR, "fused matvec (compact): %s", cudaGetErrorString(attr));
+  CARC_CHECK_CUDA(cudaMemsetAsync(sync, 0, 16, stream));
+  PhaseScope ph(PH_TC_STEP_A, stream);
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(F2_THREADS);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute la[1];
+  la[0].id = cudaLaunchAttributeCooperative;
+  la[0].val.cooperative = 1;
+  cfg.attrs = la;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaErrorInvalidValue;
+  switch (s.d) {
+    case 1: e = cudaLaunchKernelEx(&cfg, stage3_fused2_kernel<1>, maps, fp); break;
+    case 2: e = cudaLaunchKernelEx(&cfg, stage3_fused2_kernel<2>, maps, fp); break;
+    case 4: e = cudaLaunchKernelEx(&cfg, stage3_fused2_kernel<4>, maps, fp); break;
+    case 8: e = cudaLaunchKernelEx(&cfg, stage3_fused2_kernel<8>, maps, fp); break;
+  }
+  if (e == cudaSuccess) {
+    ::carc::count_launch();
+    *done = true;
+    return CARC_OK;
+  }
+  (void)cudaGetLastError();  // not co-resident: the caller takes another path
+  return CARC_OK;
+}
+
 }  // namespace
 
 int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const int32_t* terms,
@@ -1023,7 +1895,9 @@ int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, in
   S3 s;
   if (s3_shapes(s0_shape, s1_shape, d, &s) != CARC_OK) return -1;
   if (n_terms < 1 || nvec < 1) return 0;
-  return mv_layout(s, s0_shape, s1_shape, nvec, group_terms(terms, n_terms), nullptr, nullptr);
+  const TermGroups tg = group_terms(terms, n_terms);
+  return std::max(mv_layout(s, s0_shape, s1_shape, nvec, tg, nullptr, nullptr),
+                  f2_ws_bytes(s, geometry2(s, tg), tg, nvec));
 }
 
 namespace {
@@ -1212,9 +2086,23 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
       return fail(CARC_BAD_ARG, "stage3 tc matvec: term %d out of range", t);
   }
   const TermGroups tg = group_terms(terms, n_terms);
+  const Geo g1 = geometry(s, 1);
+  // the compact-operand fused kernel (autotune entry -2 or none) where it
+  // takes the shape; -1 selects the first fused kernel, > 0 the two-kernel path
+  {
+    const Geo2 g2 = geometry2(s, tg);
+    const int tuned = tuned_ksplit(s0_shape, s1_shape, s.d, nvec, (int)tg.i1.size());
+    if (g2.ok && (tuned == 0 || tuned == -2) && f2_geo(s, g2, nvec).VH) {
+      if (ws_bytes < f2_ws_bytes(s, g2, tg, nvec)) return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
+      bool done = false;
+      const char* plan2 = static_cast<const char*>(plan) + plan_bytes_for(g1, tg);
+      CARC_RETURN_IF(launch_fused2(s, nvec, tg, g2, plan2, ws, static_cast<const double2*>(x),
+                                   static_cast<double2*>(y), op_ptrs, terms, accumulate, &done, status, stream));
+      if (done) return CARC_OK;
+    }
+  }
   if (ws_bytes < mv_layout(s, s0_shape, s1_shape, nvec, tg, nullptr, nullptr))
     return fail(CARC_BAD_ARG, "stage3 tc matvec: workspace too small");
-  const Geo g1 = geometry(s, 1);
   const Geo g = geometry(s, nvec);
   MvWs w;
   mv_layout(s, s0_shape, s1_shape, nvec, tg, &w, ws);

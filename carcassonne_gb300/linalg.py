@@ -29,16 +29,19 @@ def _status_check(status, what):
         raise _lib.CarcNotConverged(s, what) if s == _lib.CARC_NOT_CONVERGED else _lib.CarcError(s, what)
 
 
-def svd(data, full_matrices=True):
+def svd(data, full_matrices=True, deferred=None):
     """(U, S, Vh) of a matrix; the economic form (full_matrices is accepted
-    for signature compatibility; only the economic factors are produced)."""
+    for signature compatibility; only the economic factors are produced).
+    ``deferred``: a list to which the device status word is appended instead
+    of being read here (the caller checks it later with check_deferred, so a
+    sequence of calls synchronises once)."""
     t = data._t if isinstance(data, TorchData) else TorchData(data)._t
     if t.dim() != 2:
         raise ValueError("svd needs a matrix")
     m, n = t.shape
     if m < n:
         # A^H = V S U^H
-        U2, S2, Vh2 = svd(TorchData(engine.permute(t, [1, 0], conj=True)))
+        U2, S2, Vh2 = svd(TorchData(engine.permute(t, [1, 0], conj=True)), deferred=deferred)
         return (TorchData(engine.permute(Vh2._t, [1, 0], conj=True)), S2,
                 TorchData(engine.permute(U2._t, [1, 0], conj=True)))
     lib = _lib.load()
@@ -51,13 +54,26 @@ def svd(data, full_matrices=True):
     ws = engine.Workspace.get(ws_bytes, a.device)
     _lib.call("carc_zgesvd_jacobi", m, n, 1, _vp(a), _vp(U), _vp(S), _vp(Vh), _vp(status), _vp(ws), ws_bytes,
               current_stream_handle())
-    _status_check(status, "Jacobi SVD did not converge")
+    if deferred is None:
+        _status_check(status, "Jacobi SVD did not converge")
+    else:
+        deferred.append(status)
     return TorchData(U), TorchData(S), TorchData(Vh)
 
 
-def unitize(data):
+def check_deferred(statuses, what="Jacobi SVD did not converge"):
+    """Read the status words collected by ``deferred`` calls (one device sync)."""
+    if statuses:
+        vals = torch.stack([s.reshape(()) for s in statuses]).cpu().numpy()
+        for v in vals:
+            if int(v) != _lib.CARC_OK:
+                raise (_lib.CarcNotConverged(int(v), what) if int(v) == _lib.CARC_NOT_CONVERGED
+                       else _lib.CarcError(int(v), what))
+
+
+def unitize(data, deferred=None):
     """Polar factor U Vh (utils.py:879-882)."""
-    U, _, Vh = svd(data)
+    U, _, Vh = svd(data, deferred=deferred)
     return U.contractWith(Vh, (1,), (0,))
 
 

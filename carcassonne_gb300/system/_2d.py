@@ -249,12 +249,12 @@ class System(BaseSystem):
             g2 = folded.conj().contractWith(folded, (1,), (1,))
         else:
             g2 = None
-        gram = np.zeros((old_dimension, old_dimension), np.complex128)
+        # block-diagonal Gram matrix assembled on the device (no host round trip)
+        gram_d = TorchData.newZeros((old_dimension, old_dimension))
         if g1 is not None:
-            gram[:n1, :n1] = g1.toArray()
+            gram_d._t[:n1, :n1] = g1._t
         if g2 is not None:
-            gram[n1:, n1:] = g2.toArray()
-        gram_d = TorchData(gram)
+            gram_d._t[n1:, n1:] = g2._t
         corner_mult, side_mult_conj = computeCompressor(old_dimension, new_dimension,
                                                         Multiplier((old_dimension,) * 2, None, 0, lambda: gram_d, 0),
                                                         None, normalize)

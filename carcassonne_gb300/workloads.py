@@ -65,17 +65,18 @@ def random_unit(rng, shape, complex_=False):
     return a / np.linalg.norm(a)
 
 
-def matvec_problem_arrays(D=4, c_ket=8, c_bra=4, seed=1, op_arrays=None, rounds=1):
+def matvec_problem_arrays(D=4, c_ket=8, c_bra=4, seed=1, op_arrays=None, rounds=1, complex_=False):
     """Host arrays of the stage-3 microbenchmark: corners (c,c',1,c,c',1) and
-    sides (c,c',1,c,c',1,D,D) per tag, chi = c*c' merged boundary dimension."""
+    sides (c,c',1,c,c',1,D,D) per tag, chi = c*c' merged boundary dimension;
+    real entries, or complex ones (re and im i.i.d. N(0,1)) with ``complex_``."""
     rng = np.random.default_rng(seed)
     op_arrays = ti_operator_arrays() if op_arrays is None else op_arrays
     op_tags = [t for t, _ in op_arrays]
     corners_t, sides_t = simulate_tags(op_tags, list(range(4)) * rounds)
     cshape = (c_ket, c_bra, 1, c_ket, c_bra, 1)
     sshape = cshape + (D, D)
-    corners = [[(t, random_unit(rng, cshape)) for t in ct] for ct in corners_t]
-    sides = [[(t, random_unit(rng, sshape)) for t in st] for st in sides_t]
+    corners = [[(t, random_unit(rng, cshape, complex_)) for t in ct] for ct in corners_t]
+    sides = [[(t, random_unit(rng, sshape, complex_)) for t in st] for st in sides_t]
     return corners, sides, op_arrays
 
 
@@ -107,6 +108,50 @@ def hermitian_problem_arrays(D=4, c=8, seed=2, op_arrays=None, rounds=1, rank=No
     corners = [[(t, _ket_bra(rng, (c, c), rank)) for t in ct] for ct in corners_t]
     sides = [[(t, _ket_bra(rng, (c, c, D), rank * D)) for t in st] for st in sides_t]
     return corners, sides, op_arrays
+
+
+def bond_start_arrays(D, d, seed):
+    """Start of a growth run: unit corners (1,1,1,1,1,1), each side a random
+    Hermitian positive-definite bond matrix a a^H + I/2 (a with re and im
+    i.i.d. N(0,1)) stored as (1,1,1,1,1,1,D,D), and a random real N(0,1)
+    center (D,D,D,D,d) of unit norm, all from ``default_rng(seed)`` in that
+    order."""
+    rng = np.random.default_rng(seed)
+    corners = [np.ones((1,) * 6, np.complex128) for _ in range(4)]
+    sides = []
+    for _ in range(4):
+        a = rng.standard_normal((D, D)) + 1j * rng.standard_normal((D, D))
+        bond = a @ a.conj().T + 0.5 * np.eye(D)
+        sides.append(bond.reshape((1,) * 6 + (D, D)).astype(np.complex128))
+    st = rng.standard_normal((D,) * 4 + (d,)).astype(np.complex128)
+    return corners, sides, st / np.linalg.norm(st)
+
+
+def growth_operator(kind):
+    """Operator centers of the growth runs, as the reference's constructors
+    build them: transverse Ising makeSimpleSparseOperator(O=-3 Z,
+    OO_UD=(X,-X), OO_LR=(X,-X)); Heisenberg XXX (J=1 in Pauli units)
+    makeSparseOperator(OO_UDs=[(X,X),(Y,Y),(Z,Z)], OO_LRs=same)."""
+    from .data import TorchData
+    from .sparse import makeSimpleSparseOperator, makeSparseOperator
+    Xd, Yd, Zd = TorchData.X, TorchData.Y, TorchData.Z
+    if kind == "ti":
+        return makeSimpleSparseOperator(O=-3.0 * Zd, OO_UD=(Xd, -1.0 * Xd), OO_LR=(Xd, -1.0 * Xd))
+    if kind == "heis":
+        return makeSparseOperator(OO_UDs=[(Xd, Xd), (Yd, Yd), (Zd, Zd)], OO_LRs=[(Xd, Xd), (Yd, Yd), (Zd, Zd)])
+    raise ValueError(kind)
+
+
+def bond_start_system(kind, D, seed):
+    """The growth run's System on the device (bond_start_arrays, growth_operator)."""
+    from .data import TorchData
+    from .sparse import Identity
+    from .system import System
+    op = growth_operator(kind)
+    d = next(iter(op.values())).shape[0]
+    c, s, st = bond_start_arrays(D, d, seed)
+    return System(tuple({Identity(): TorchData(a)} for a in c), tuple({Identity(): TorchData(a)} for a in s),
+                  TorchData(st), op)
 
 
 def to_device(corners, sides, op_arrays):

@@ -38,6 +38,7 @@ enum carc_status_code {
 #define CARC_MAX_SLOTS 64    /* tags per sparse boundary in one grouped call */
 #define CARC_MAX_ENTRIES 512 /* tag pairs in one grouped call */
 #define CARC_NOALLOC_SCRATCH_BYTES (16u << 20) /* fixed scratch of carc_stage3_matvec_f64_noalloc */
+#define CARC_CG_MAX_N 2048 /* largest system carc_zcg_hpsd takes (x, r, p, G p in shared memory) */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* carc_last_error_string(void);
@@ -189,9 +190,13 @@ int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int6
                           const int32_t* terms, int32_t n_terms, const void* x, void* y, int32_t nvec,
                           int32_t accumulate, void* workspace, int64_t workspace_bytes, void* status, void* stream);
 /* Autotune cache of the tensor-core matvec (no counterpart in the reference):
- * the step-B split-K count for one problem shape (S2 shapes, d, block size,
- * number of S2_1 tags carrying terms); 0 removes the entry (the one-wave
- * heuristic applies).  Query workspace sizes after setting an entry. */
+ * the kernel choice for one problem shape (S2 shapes, d, block size, number
+ * of S2_1 tags carrying terms): > 0 the two-kernel path with that step-B
+ * split-K count, -1 the fused kernel on the first (re/im x hi/lo row)
+ * operand layout, -2 the fused kernel on compact operands; 0 removes the
+ * entry (the compact fused kernel where it takes the shape, else the first
+ * fused kernel, else the two-kernel path with the one-wave heuristic).
+ * Query workspace sizes after setting an entry. */
 int carc_tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int32_t nvec, int32_t groups,
                          int32_t ksplit);
 int carc_tc_autotune_clear(void);
@@ -335,6 +340,20 @@ int carc_zminres_projected(int32_t n, const void* C, const void* u, double shift
                            int32_t maxit, double rtol, int32_t* iterations, void* workspace, int64_t workspace_bytes,
                            void* stream);
 int64_t carc_zminres_projected_workspace_size(int32_t n);
+
+/*
+ * Conjugate gradients on a Hermitian positive semi-definite G x = c (n x n
+ * row-major complex128, n <= CARC_CG_MAX_N) from x = 0, the whole iteration
+ * in one thread block with no host round trip: stops when
+ * |r| <= tol |c|, when p^H G p <= 0, or after max_iter iterations.  status
+ * (device int32[2]) receives the iteration count and 1 if the iteration
+ * stopped by one of the first two tests (0: out of iterations); residual
+ * (device double[1]) the final |r| / |c|.  Replaces the
+ * GMRES solve of the normal equations in computeProductCompressor
+ * (compression.py:38-43), whose non-convergence is its assert info == 0.
+ */
+int carc_zcg_hpsd(int32_t n, const void* G, const void* c, void* x, double tol, int32_t max_iter, void* status,
+                  void* residual, void* stream);
 
 /*
  * relaxOver (utils.py:805-878): restarted Krylov / Rayleigh-Ritz on
