@@ -53,10 +53,17 @@ PHASE_NAMES = ("pack", "step_a", "step_b", "reduce")
 KERNEL_OF_PHASE = dict(pack="pack_vin_kernel", step_a="gemm_bf16_tn_kernel<256,1> (folding epilogue)",
                        step_b="gemm_bf16_tn_kernel<256,0> (split-K)", reduce="reduce_planes_kernel",
                        fused="stage3_fused_kernel (one cooperative launch: Vin packing, step A + fold + step B "
-                             "with W on chip, plane reduction)")
+                             "with W on chip, plane reduction)",
+                       fused2="stage3_fused2_kernel (one cooperative launch on compact operands: Vin packing, step A "
+                              "with hi+lo summed in TMEM, fold to W^T in shared memory, transposed step B, plane "
+                              "reduction)")
 # DRAM bytes (read + write) per launch from one ncu capture of this workload
 # (profiles/ holds the summary and the command that produced it)
 NCU_TRAFFIC = {
+    ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "fused2"): dict(
+        bytes_per_launch=63.65e6,
+        source="profiles/stage3_fused2_matvec_D4_chi32_nvec8.md: one cooperative launch of the compact-operand "
+               "kernel, dram read 63.08 MB + write 0.56 MB"),
     ("center-site matvec, TI d=2 (9 terms), D=4, chi=32 (8x4)", "fused"): dict(
         bytes_per_launch=129.9e6,
         source="profiles/stage3_fused_matvec_D4_chi32_nvec8.md: one cooperative fused launch (packing, both "
@@ -139,7 +146,54 @@ def tc_bytes_per_step(opr, nvec):
         out["fused"] = out.get("fused", 0) + 2 * (rows_a * reg_a * nt + rows_vin * reg_a * nt + live_rows * kp_b) \
             + 4 * grid * _round_up(live_b, 32) * nvec * l0 * l1 * d
         out["launches"]["fused"] = out["launches"].get("fused", 0) + 1
+        # the compact-operand kernel: S2_0 as (re/im rows) x 64 columns per term,
+        # S2_1 as (j, re/im) rows x [hi | lo] planes per tag, Vin per term, and
+        # one FP32 plane (VH x NBB x 128) per CTA written and read back
+        f2 = _f2_geo(g, nvec, d)
+        if f2:
+            vh, nah, nbb = f2
+            ma = x0 * x1 * l0 * l1
+            kcb = x0 * x1 * k2 * k3
+            grid2 = max(1, min(152, ma // 64 * len(groups)))
+            out["fused2"] = out.get("fused2", 0) + 2 * (2 * ma * 64 * nt + nbb * 4 * kcb * len(groups)
+                                                        + vh * nah * 64 * nt) + 2 * 4 * grid2 * vh * nbb * 128
+            out["launches"]["fused2"] = out["launches"].get("fused2", 0) + 1
     return out
+
+
+def _f2_geo(g, nvec, d):
+    """(VH, NAh, NBB) of the compact-operand fused kernel for one S2 shape
+    group, or None where the library takes another path (its f2_geo)."""
+    x0, x1, k0, k1, l0, l1 = g["shape0"]
+    _, _, k2, k3, l2, l3 = g["shape1"]
+    L, k23, kc = l0 * l1, k2 * k3, k0 * k1
+    wp = _round_up(2 * kc, 16)
+    groups = len({t[1] for t in g["terms"]})
+    ok = (k23 == L and L % 4 == 0 and 64 % L == 0 and (x0 * x1 * L) % 64 == 0 and 2 * wp <= 64
+          and _round_up(2 * l2 * l3, 16) <= 128 and groups <= 8 and d in (1, 2, 4, 8))
+    if not ok:
+        return None
+    na = nvec * k23 * d
+    vh = 1 if na <= 128 else 2
+    if vh == 2 and nvec % 2:
+        return None
+    nah = na // vh
+    if nah % 16 or nah > 128 or nah < 16:
+        return None
+    return vh, nah, _round_up(2 * l2 * l3, 16)
+
+
+def path_bytes_per_step(opr, nvec):
+    """Algorithmic bytes of one operator application at the path's operand
+    type (split-BF16 complex: hi and lo of re and im, 8 bytes per entry):
+    each term's two S2 halves once, the block of centers in and out (complex128)."""
+    import numpy as np
+    out = 0
+    for g in opr._groups:
+        x0, x1, k0, k1, l0, l1 = g["shape0"]
+        _, _, k2, k3, l2, l3 = g["shape1"]
+        out += len(g["terms"]) * 8 * (x0 * x1 * k0 * k1 * l0 * l1 + x0 * x1 * k2 * k3 * l2 * l3)
+    return out + 2 * nvec * 16 * int(np.prod(opr.in_shape))
 
 
 def solve_section():
@@ -180,6 +234,162 @@ def solve_section():
                 speedup_rayleigh=res["plain"]["seconds"] / res["mixed_rayleigh"]["seconds"])
 
 
+# growth runs (time-to-energy per absorption step): operator, D, seed,
+# absorptions, per-layer boundary dimension kept by state compression
+GROWTH = {
+    "ti_h3_D2_c8": dict(workload="growth run, transverse Ising h=3, D=2, chi=64 (c=8), 20 absorptions", kind="ti",
+                        D=2, seed=0, steps=20, new_dimension=8),
+    "heis_D4_c8": dict(workload="growth run, Heisenberg XXX, D=4, chi=64 (c=8), first 12 absorptions", kind="heis",
+                       D=4, seed=2, steps=12, new_dimension=8),
+}
+
+
+def _sync_time(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    out = fn()
+    torch.cuda.synchronize()
+    return out, time.perf_counter() - t0
+
+
+def growth_run(spec, cpu_steps=()):
+    """One growth run: at every absorption step the center problem is solved
+    twice on the same environment, plain (FP64 H_eff / N_eff on the CUDA
+    cores, FP64 Lanczos) and mixed (tensor-core formation, complex64
+    Lanczos, one FP64 Newton correction), both from the current center; the
+    run then absorbs the step's seeded random unit center
+    (workloads.growth_center, as the golden run of the reference does:
+    contractTowards(step % 4)), timed in FP64 and, on a copy, with every tag
+    pair on the tensor cores, and runs compressCornerStateTowards for every
+    corner axis above the kept dimension.  Wall times with the device
+    synchronised on both sides.  ``cpu_steps``: steps whose environment is
+    also solved, absorbed and compressed by the CPU restatement of the
+    reference (numpy/SciPy on the host cores), as the reference's per-step
+    time."""
+    import numpy as np
+    from copy import copy
+    from carcassonne_gb300 import workloads
+    from carcassonne_gb300.data import TorchData
+    from carcassonne_gb300.sparse import Identity
+    from carcassonne_gb300.solve import solve_center
+    from carcassonne_gb300.tensors._2d import dense
+    system = workloads.bond_start_system(spec["kind"], spec["D"], spec["seed"])
+    steps = []
+    for step in range(spec["steps"]):
+        (H, N), t_build = _sync_time(system.formExpectationAndNormalizationMultipliers)
+        x0 = system.state_center_data
+        plain, t_plain = _sync_time(lambda: solve_center(H, N, x0=x0, precision="plain"))
+        mixed, t_mixed = _sync_time(lambda: solve_center(H, N, x0=x0, precision="mixed"))
+        e_p, e_m = plain["energy"], mixed["energy"]
+        hop = getattr(H, "operator", None)  # None when H_eff has no terms (a Heisenberg center's first step)
+        rec = dict(step=step, n=int(np.prod(N.operator.in_shape)), terms=len(hop.terms) if hop is not None else 0,
+                   energy=e_p, rel_err_mixed=abs(e_m - e_p) / abs(e_p) if e_p != 0 else abs(e_m),
+                   build_s=t_build, plain_solve_s=t_plain, mixed_solve_s=t_mixed)
+        if step in cpu_steps:
+            rec["cpu_reference_s"], rec["cpu_energy"] = _cpu_step(system)
+        seed_c = workloads.GROWTH_CENTER_SEED[spec["kind"]] + step
+        system.setStateCenter(TorchData(workloads.growth_center(tuple(x0.shape), seed_c)))
+        if step in cpu_steps:
+            rec["cpu_contract_s"], rec["cpu_compress_s"] = _cpu_contract_compress(system, step % 4,
+                                                                                 spec["new_dimension"])
+        # the same absorption with every tag pair on the tensor cores, on a copy
+        tc_sys = copy(system)
+        with dense.absorption_precision("tc"):
+            _, t_tc = _sync_time(lambda: tc_sys.contractTowards(step % 4))
+        _, t_contract = _sync_time(lambda: system.contractTowards(step % 4))
+        tc_err = max(float((tc[t]._t - ref[t]._t).abs().max() / ref[t]._t.abs().max().clamp_min(1e-300))
+                     for tc, ref in zip(tc_sys.corners + tc_sys.sides, system.corners + system.sides) for t in ref)
+        del tc_sys
+        t_compress = 0.0
+        for corner in range(4):
+            for cdir, axis in ((0, 0), (1, 3)):
+                if system.corners[corner][Identity()].shape[axis] > spec["new_dimension"]:
+                    np.random.seed(1000 * step + 10 * corner + cdir)
+                    _, t = _sync_time(lambda: system.compressCornerStateTowards(corner, cdir, spec["new_dimension"]))
+                    t_compress += t
+        rec.update(contract_s=t_contract, contract_tc_s=t_tc, contract_tc_rel_err=tc_err, compress_s=t_compress)
+        steps.append(rec)
+    tot = lambda k: sum(r[k] for r in steps)
+    out = dict(spec, steps_detail=[{k: (round(v, 6) if isinstance(v, float) and k.endswith("_s") else v)
+                                    for k, v in r.items()} for r in steps])
+    out.update(time_to_energy_plain_s=tot("build_s") + tot("plain_solve_s"),
+               time_to_energy_mixed_s=tot("build_s") + tot("mixed_solve_s"),
+               solve_plain_s=tot("plain_solve_s"), solve_mixed_s=tot("mixed_solve_s"),
+               build_s=tot("build_s"), contract_s=tot("contract_s"), contract_tc_s=tot("contract_tc_s"),
+               compress_s=tot("compress_s"), max_rel_err_mixed=max(r["rel_err_mixed"] for r in steps),
+               max_contract_tc_rel_err=max(r["contract_tc_rel_err"] for r in steps))
+    out["speedup_solve"] = out["solve_plain_s"] / out["solve_mixed_s"]
+    out["speedup_time_to_energy"] = out["time_to_energy_plain_s"] / out["time_to_energy_mixed_s"]
+    cpu = [r for r in steps if "cpu_reference_s" in r]
+    if cpu:
+        out["cpu_reference"] = dict(
+            kind="port", cores=os.cpu_count(), steps=[r["step"] for r in cpu],
+            seconds_per_step=[round(r["cpu_reference_s"], 4) for r in cpu],
+            gpu_plain_seconds_same_steps=[round(r["build_s"] + r["plain_solve_s"], 5) for r in cpu],
+            gpu_mixed_seconds_same_steps=[round(r["build_s"] + r["mixed_solve_s"], 5) for r in cpu],
+            max_rel_energy_diff_vs_gpu_plain=max(abs(r["cpu_energy"] - r["energy"]) / abs(r["energy"]) for r in cpu),
+            contract_seconds=[round(r["cpu_contract_s"], 4) for r in cpu],
+            gpu_contract_seconds_same_steps=[round(r["contract_s"], 5) for r in cpu],
+            gpu_contract_tc_seconds_same_steps=[round(r["contract_tc_s"], 5) for r in cpu],
+            compress_seconds=[round(r["cpu_compress_s"], 4) for r in cpu],
+            gpu_compress_seconds_same_steps=[round(r["compress_s"], 5) for r in cpu],
+            sample="oracle/carc_oracle.py on host copies of the same environments: multipliers, formMatrix, "
+                   "scipy.linalg.eigh; contractTowards; compressCornerStateTowards with a direct least-squares "
+                   "solve (numpy/BLAS, all host threads)")
+    return out
+
+
+def _oracle_system(system):
+    from oracle import carc_oracle as orc
+    from tests.tagrepr import parse_tag
+    oc = [{parse_tag(repr(t)): d.toArray() for t, d in c.items()} for c in system.corners]
+    osd = [{parse_tag(repr(t)): d.toArray() for t, d in s.items()} for s in system.sides]
+    oo = {parse_tag(repr(t)): d.toArray() for t, d in system.operator_center_tensor.items()}
+    return orc.OracleSystem(oc, osd, system.state_center_data.toArray(), oo)
+
+
+def _cpu_step(system):
+    """The CPU restatement of the reference on one environment: build the
+    multipliers, form H_eff and N_eff, dense generalized eigh (the
+    reference's minimizeExpectationUsingFullEigensolver, system/_2d.py:498-502)."""
+    from oracle import carc_oracle as orc
+    osys = _oracle_system(system)
+    t0 = time.perf_counter()
+    H, N, _ = osys.multipliers()
+    w, _ = orc.lowest_generalized(H.formMatrix(), N.formMatrix())
+    return time.perf_counter() - t0, float(w)
+
+
+def _cpu_contract_compress(system, direction, new_dimension):
+    """The CPU restatement of the reference on one environment: contractTowards
+    (system/_2d.py:435-439) of the step's center, then compressCornerStateTowards
+    (system/_2d.py:191-228, the compressor of compression.py:26-46 with a
+    direct least-squares solve) for every corner axis above new_dimension."""
+    import numpy as np
+    from oracle import carc_oracle as orc
+    osys = _oracle_system(system)
+    t0 = time.perf_counter()
+    osys.contract_towards(direction)
+    t1 = time.perf_counter()
+    rng = np.random.default_rng(direction)
+    for corner in range(4):
+        for cdir, axis in ((0, 0), (1, 3)):
+            old = osys.corners[corner][orc.I_TAG].shape[axis]
+            if old > new_dimension:
+                init = rng.standard_normal((old, new_dimension)) + 1j * rng.standard_normal((old, new_dimension))
+                osys.compress_corner_state_towards(corner, cdir, new_dimension, init)
+    return t1 - t0, time.perf_counter() - t1
+
+
+def growth_section(cpu=True):
+    out = {}
+    for name, spec in GROWTH.items():
+        cpu_steps = (spec["steps"] - 1,) if cpu else ()
+        out[name] = growth_run(spec, cpu_steps)
+    return out
+
+
 def parse_args():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -195,6 +405,8 @@ def parse_args():
     p.add_argument("--no-batched", dest="batched", action="store_false",
                    help="skip the batched uneven-problems comparison (graph replay vs launch loop)")
     p.add_argument("--batched-count", type=int, default=32)
+    p.add_argument("--no-growth", dest="growth", action="store_false",
+                   help="skip the growth runs' per-step time-to-energy (plain vs mixed)")
     return p.parse_args()
 
 
@@ -509,7 +721,9 @@ def main():
         fused = phases["step_b"]["intervals_per_step"] == 0
         if fused:
             # the step-A interval brackets the fused kernel, which does both steps
-            phases["fused"] = phases.pop("step_a")
+            # (the compact-operand one wherever it takes the shape)
+            name = "fused2" if all(_f2_geo(g, nvec, opr.d) for g in opr._groups) else "fused"
+            phases[name] = phases.pop("step_a")
             phases.pop("step_b")
         for pname, ph in phases.items():
             ph["share"] = ph["ms_per_step"] / ms
@@ -525,13 +739,18 @@ def main():
                       launches_per_step=launches, traffic_source=None if traffic is None else traffic["source"],
                       whole_operator_tflops=achieved_tflops,
                       whole_operator_frac_of_bf16=achieved_tflops / peaks["bf16_tflops"])
-        if top == "fused":
+        if top in ("fused", "fused2"):
             # algorithmic flops per launch (CostTracker, the whole operator) over the kernel's time;
-            # the split-BF16 tensor work is 4x that, reported beside it
+            # the split-BF16 tensor work is 4x (first kernel) or 3x (compact kernel: no lo x lo) that
             kt = flops_per_step / (ph["ms_per_step"] * 1e-3) / 1e12
+            alg_bytes = path_bytes_per_step(opr, nvec)
+            alg_gbs = alg_bytes / (ph["ms_per_step"] * 1e-3) / 1e9
             roofline = dict(bound="tensor", achieved=kt, peak=peaks["bf16_tflops"], unit="TFLOP/s",
-                            frac=kt / peaks["bf16_tflops"], tensor_executed_tflops=4 * kt,
-                            hbm_achieved_gbs=ph["achieved_gbs"], hbm_frac=ph["achieved_gbs"] / peaks["hbm_gbs"],
+                            frac=kt / peaks["bf16_tflops"],
+                            tensor_executed_tflops=(3 if top == "fused2" else 4) * kt,
+                            path_bytes_per_launch=alg_bytes, hbm_achieved_gbs=alg_gbs,
+                            hbm_frac=alg_gbs / peaks["hbm_gbs"],
+                            packed_operand_gbs=ph["achieved_gbs"],
                             peak_source=peaks["source"] + " bf16 dense", **common)
         else:
             roofline = dict(bound="hbm", achieved=ph["achieved_gbs"], peak=peaks["hbm_gbs"], unit="GB/s",
@@ -539,6 +758,8 @@ def main():
                             **common)
     cpu = cpu_reference(args, args.cpu_seconds) if world == 1 else None
     solve = solve_section() if args.solve else None
+    if solve is not None and args.growth:
+        solve["growth"] = growth_section(cpu=world == 1)
     batched = None
     if args.batched and world == 1:
         from carcassonne_gb300 import batched as batched_mod

@@ -182,6 +182,43 @@ def _launch(desc, a_list, b_list, out_list, entries, alpha=1.0, accumulate=False
               current_stream_handle())
 
 
+def contract_grouped_tc(spec, a_list, b_list, out_list, entries, conj_a=False, conj_b=False, accumulate=False):
+    """``out[c] (+)= sum_{(i,j,c) in entries} A[i] . B[j]`` with every pair on
+    the tensor cores (``carc_zcontract_tc``: operands split into BF16 hi + lo,
+    FP32 accumulation, FP64 reduction; ~1e-5 relative to the result's scale).
+    Same spec and layout rules as ``contract_grouped``.  Returns the device
+    int32 status words, one per entry (each call clears its own word and sets
+    it on a pipeline timeout); the caller checks them."""
+    sp = spec if isinstance(spec, Spec) else Spec(spec)
+    a0, b0, c0 = a_list[0], b_list[0], out_list[0]
+    a_ls = _tensor_letter_strides(sp.a, a0)
+    b_ls = _tensor_letter_strides(sp.b, b0)
+    ext = _extents(sp, a_ls, b_ls)
+    if not c0.is_contiguous():
+        raise ValueError("output must be contiguous")
+    c_str = out_letter_strides(sp.out, ext)
+    desc = build_desc(sp, ext, {c: s for c, (e, s) in a_ls.items()}, {c: s for c, (e, s) in b_ls.items()}, c_str,
+                      conj_a, conj_b)
+    if desc is None:
+        raise ValueError("contraction %r needs more than %d sub-dimensions per group" %
+                         (sp.a + "," + sp.b + "->" + sp.out, _lib.MAX_SUBDIMS))
+    lib = _lib.load()
+    ws_bytes = lib.carc_zcontract_tc_workspace_size(ctypes.byref(desc), 0)
+    if ws_bytes < 0:
+        _lib.check(_lib.CARC_BAD_ARG)
+    ws = Workspace.get(ws_bytes, c0.device)
+    status = torch.zeros(max(1, len(entries)), dtype=torch.int32, device=c0.device)
+    seen = set()
+    for k, (i, j, c) in enumerate(entries):
+        acc = accumulate or c in seen
+        seen.add(c)
+        _lib.call("carc_zcontract_tc", ctypes.byref(desc), ctypes.c_void_p(a_list[i].data_ptr()),
+                  ctypes.c_void_p(b_list[j].data_ptr()), ctypes.c_void_p(out_list[c].data_ptr()), 1.0, 0.0,
+                  int(acc), 0, ctypes.c_void_p(ws.data_ptr()), ws_bytes, ctypes.c_void_p(status[k].data_ptr()),
+                  current_stream_handle())
+    return status
+
+
 def contract(spec, a, b, out_shape, conj_a=False, conj_b=False, alpha=1.0):
     """Single contraction; returns a new C-contiguous tensor of ``out_shape``."""
     out = torch.empty(tuple(int(x) for x in out_shape), dtype=CDT, device=a.device)

@@ -35,16 +35,66 @@ def _check_dims(ln, li, a, rn, ri, b):
         raise DimensionMismatchError(ln, li, int(a.shape[li]), rn, ri, int(b.shape[ri]))
 
 
-class _PairContractor:
-    """A two-operand contractor given by a spec and an output-shape rule."""
+# Precision of the absorptions (corner <- side, side <- center; contractTowards):
+# "fp64" (default: the FP64 grouped GETT, the parity path) or "tc" (every
+# tag pair on the tensor cores with split-BF16 operands, ~1e-5 relative to
+# the absorbed tensor's scale).  The environment built by "tc" absorptions
+# carries that error into every later energy; set it with
+# ``absorption_precision(...)``.
+_ABSORPTION = {"precision": "fp64", "status": []}
 
-    def __init__(self, name, spec, ranks, joins, shape_fn, doc):
+
+class absorption_precision:
+    """Context manager selecting the absorptions' precision ("fp64" or "tc");
+    on exit the tensor-core status words are checked."""
+
+    def __init__(self, precision):
+        if precision not in ("fp64", "tc"):
+            raise ValueError("absorption precision must be 'fp64' or 'tc', not %r" % (precision,))
+        self.precision = precision
+        self.previous = None
+
+    def __enter__(self):
+        self.previous = _ABSORPTION["precision"]
+        _ABSORPTION["precision"] = self.precision
+        return self
+
+    def __exit__(self, *exc):
+        _ABSORPTION["precision"] = self.previous
+        check_absorption_status()
+        return False
+
+
+def check_absorption_status():
+    """Read the status words of the tensor-core absorptions run so far (one
+    device synchronisation) and raise if a pipeline wait timed out."""
+    st, _ABSORPTION["status"] = _ABSORPTION["status"], []
+    if st:
+        vals = torch.cat([t.reshape(-1) for t in st]).cpu()
+        if int(vals.abs().max()) != 0:
+            raise _lib.CarcNotConverged(int(vals.abs().max()), "tensor-core absorption: a pipeline wait timed out")
+
+
+def _contract(spec, a_list, b_list, out_list, entries, accumulate, tc):
+    if tc and _ABSORPTION["precision"] == "tc":
+        _ABSORPTION["status"].append(engine.contract_grouped_tc(spec, a_list, b_list, out_list, entries,
+                                                                accumulate=accumulate))
+    else:
+        engine.contract_grouped(spec, a_list, b_list, out_list, entries, accumulate=accumulate)
+
+
+class _PairContractor:
+    """A two-operand contractor given by a spec and an output-shape rule;
+    ``tc``: an absorption, run on the tensor cores under absorption_precision("tc")."""
+
+    def __init__(self, name, spec, ranks, joins, shape_fn, doc, tc=False):
         self.__name__ = name
         self.spec = engine.Spec(spec)
         self.ranks = ranks
         self.joins = joins          # [(operand, axis, operand, axis)] dimension checks
         self.shape_fn = shape_fn
         self.__doc__ = doc
+        self.tc = tc
 
     def _validate(self, a, b):
         _check_rank(0, a, self.ranks[0])
@@ -57,7 +107,7 @@ class _PairContractor:
         ta, tb = _t(a), _t(b)
         self._validate(ta, tb)
         out = torch.empty(self.shape_fn(ta.shape, tb.shape), dtype=CDT, device=ta.device)
-        engine.contract_grouped(self.spec, [ta], [tb], [out], [(0, 0, 0)])
+        _contract(self.spec, [ta], [tb], [out], [(0, 0, 0)], False, self.tc)
         return TorchData(out)
 
     def grouped(self, list_a, list_b, table, n_out):
@@ -93,9 +143,8 @@ class _PairContractor:
                 mb = {v: i for i, v in enumerate(used_b)}
                 mc = {v: i for i, v in enumerate(used_c)}
                 single = len(classes) == 1 and lo == 0
-                engine.contract_grouped(self.spec, [ta[i] for i in used_a], [tb[i] for i in used_b],
-                                        [outs[i] for i in used_c], [(ma[i], mb[j], mc[k]) for i, j, k in chunk],
-                                        accumulate=not single or any(written))
+                _contract(self.spec, [ta[i] for i in used_a], [tb[i] for i in used_b], [outs[i] for i in used_c],
+                          [(ma[i], mb[j], mc[k]) for i, j, k in chunk], not single or any(written), self.tc)
         return [TorchData(o) for o in outs]
 
 
@@ -103,13 +152,13 @@ absorbDenseSideIntoCornerFromLeft = _PairContractor(
     "absorbDenseSideIntoCornerFromLeft", "xyzdef,abcxyzjk->abcdjekf", (6, 8),
     [(0, 0, 1, 3), (0, 1, 1, 4), (0, 2, 1, 5)],
     lambda c, s: (s[0], s[1], s[2], c[3] * s[6], c[4] * s[7], c[5]),
-    "C'[a,b,c,(d,j),(e,k),f] = sum C[x,y,z,d,e,f] T[a,b,c,x,y,z,j,k]  (tensors/_2d/dense.py:10-15)")
+    "C'[a,b,c,(d,j),(e,k),f] = sum C[x,y,z,d,e,f] T[a,b,c,x,y,z,j,k]  (tensors/_2d/dense.py:10-15)", tc=True)
 
 absorbDenseSideIntoCornerFromRight = _PairContractor(
     "absorbDenseSideIntoCornerFromRight", "abcxyz,xyzghijk->ajbkcghi", (6, 8),
     [(0, 3, 1, 0), (0, 4, 1, 1), (0, 5, 1, 2)],
     lambda c, s: (c[0] * s[6], c[1] * s[7], c[2], s[3], s[4], s[5]),
-    "C'[(a,j),(b,k),c,g,h,i] = sum C[a,b,c,x,y,z] T[x,y,z,g,h,i,j,k]  (tensors/_2d/dense.py:16-21)")
+    "C'[(a,j),(b,k),c,g,h,i] = sum C[a,b,c,x,y,z] T[x,y,z,g,h,i,j,k]  (tensors/_2d/dense.py:16-21)", tc=True)
 
 formNormalizationStage1 = _PairContractor(
     "formNormalizationStage1", "abcxyz,xyzdefkl->abcdefkl", (6, 8),
@@ -200,8 +249,8 @@ def _absorb_pairs(direction, sides, pairs_e, table, n_out):
                     torch.empty(shape, dtype=CDT, device=ts[0].device)
         ms = {v: i for i, v in enumerate(used_s)}
         mc = {v: i for i, v in enumerate(used_c)}
-        engine.contract_grouped(_SIDE_SPEC, [ts[i] for i in used_s], pairs_e, [outs[c] for c in used_c],
-                                [(ms[i], j, mc[k]) for i, j, k in entries], accumulate=len(classes) > 1 or written)
+        _contract(_SIDE_SPEC, [ts[i] for i in used_s], pairs_e, [outs[c] for c in used_c],
+                  [(ms[i], j, mc[k]) for i, j, k in entries], len(classes) > 1 or written, True)
     return [TorchData(o) for o in outs]
 
 
@@ -462,5 +511,5 @@ __all__ = [
     "absorbDenseCenterSOSIntoSide", "formDenseStage3", "formDenseStage3_formMatrix_and_cost",
     "formDenseStage3_multiply_and_cost", "formNormalizationMultiplier", "formNormalizationStage1",
     "formNormalizationStage2", "formNormalizationStage3", "formNormalizationSubmatrix", "Stage3Operator",
-    "center_pair",
+    "center_pair", "absorption_precision", "check_absorption_status",
 ]

@@ -142,6 +142,21 @@ def growth_operator(kind):
     raise ValueError(kind)
 
 
+# seed of the first absorbed center of each growth run (step k uses base + k)
+GROWTH_CENTER_SEED = {"ti": 500, "heis": 900}
+
+
+def growth_center(shape, seed):
+    """The unit center absorbed at one step of a growth run: re and im i.i.d.
+    N(0,1) from ``default_rng(seed)`` (re drawn first), scaled to unit norm.
+    Absorbing the minimized center instead degenerates from the bond start:
+    the transverse-Ising minimizer is the all-up product state at every step,
+    and the Heisenberg center's first effective Hamiltonian is zero."""
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    return a / np.linalg.norm(a)
+
+
 def bond_start_system(kind, D, seed):
     """The growth run's System on the device (bond_start_arrays, growth_operator)."""
     from .data import TorchData

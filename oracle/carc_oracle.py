@@ -681,15 +681,17 @@ class OracleSystem:
         self.state = v.reshape(self.state.shape)
         return w
 
-    def compress_corner_state_towards(self, corner_id, direction, new_dimension, initial):
-        """compressCornerStateTowardsLeft/Right (system/_2d.py:191-228)."""
+    def compress_corner_state_towards(self, corner_id, direction, new_dimension, initial, P=None):
+        """compressCornerStateTowardsLeft/Right (system/_2d.py:191-228); a given
+        compressor P (new, old) is applied instead of being computed."""
         mo = lambda f, s: {k: f(v) for k, v in s.items()}
         if direction == 0:
             sd = self.sides[L(corner_id)][I_TAG]
             side_j = np.transpose(sd, (0, 1, 2, 6, 7, 3, 4, 5)).reshape(-1, sd.shape[3], sd.shape[4], sd.shape[5])
             cd = self.corners[corner_id][I_TAG]
             corner_j = cd.reshape(cd.shape[0], cd.shape[1], cd.shape[2], -1)
-            P = product_compressor(side_j, corner_j, new_dimension, initial)
+            if P is None:
+                P = product_compressor(side_j, corner_j, new_dimension, initial)
             self.sides[L(corner_id)] = mo(lambda x: absorb_matrix_at(absorb_matrix_at(x, 3, P), 4, P.conj()), self.sides[L(corner_id)])
             self.corners[corner_id] = mo(lambda x: absorb_matrix_at(absorb_matrix_at(x, 0, P.conj()), 1, P), self.corners[corner_id])
         else:
@@ -697,7 +699,8 @@ class OracleSystem:
             corner_j = cd.reshape(-1, cd.shape[3], cd.shape[4], cd.shape[5])
             sd = self.sides[corner_id][I_TAG]
             side_j = sd.reshape(sd.shape[0], sd.shape[1], sd.shape[2], -1)
-            P = product_compressor(corner_j, side_j, new_dimension, initial)
+            if P is None:
+                P = product_compressor(corner_j, side_j, new_dimension, initial)
             self.corners[corner_id] = mo(lambda x: absorb_matrix_at(absorb_matrix_at(x, 3, P), 4, P.conj()), self.corners[corner_id])
             self.sides[corner_id] = mo(lambda x: absorb_matrix_at(absorb_matrix_at(x, 0, P.conj()), 1, P), self.sides[corner_id])
         return P

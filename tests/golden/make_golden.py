@@ -387,12 +387,178 @@ def opcomp():
     np.savez_compressed(os.path.join(HERE, "opcomp.npz"), **out)
 
 
+# --- config-sized cases --------------------------------------------------------
+# The benchmark's shapes: the matvec microbenchmark (transverse Ising after one
+# absorption round, 9 terms, D=4, chi=32 = 8x4, seed 1), the same shapes with
+# the Heisenberg operator and complex boundaries, the Hermitian solve pencil
+# (Heisenberg after one round, 20 terms, D=4, chi=64 = 8x8, seed 2), and two
+# growth runs: transverse Ising h=3 (D=2, per-layer boundary dimension
+# compressed to 8, i.e. chi=64, 20 absorptions, seed 0) and Heisenberg (D=4,
+# compressed to 8, first 8 absorptions, seed 2).  Inputs come from the
+# package's own seeded generators (carcassonne_gb300.workloads) and are handed
+# to the reference with the same tags; every output is the reference's.
+
+def _ref_tag(t):
+    from tagrepr import parse_tag  # tests/tagrepr.py
+    k = parse_tag(repr(t))
+    if k[0] == "I":
+        return rsparse.Identity()
+    if k[0] == "C":
+        return rsparse.Complete()
+    if k[0] == "O":
+        return rsparse.OneSiteOperator(None)
+    if k[0] == "T":
+        return rsparse.TwoSiteOperator(k[1], k[2], k[3])
+    return rsparse.TwoSiteOperatorCompressed(k[1])
+
+
+def _multiplier_cases(out, key, corners, sides, op, nx, seed):
+    rc = [{_ref_tag(t): D(a) for t, a in lst} for lst in corners]
+    rs = [{_ref_tag(t): D(a) for t, a in lst} for lst in sides]
+    ro = {_ref_tag(t): D(a) for t, a in op}
+    Hm, Nm = rsp2.formExpectationAndNormalizationMultipliers(rc, rs, ro)
+    rng = np.random.default_rng(seed)
+    H = Hm.formMatrix().toArray().copy()
+    N = Nm.formMatrix().toArray().copy()
+    vshape = tuple(int(lst[0][1].shape[6]) for lst in sides) + (int(op[0][1].shape[0]),)
+    x = cn(rng, nx, *vshape)
+    out[key + "_x"] = x
+    out[key + "_Hx"] = np.stack([Hm(D(x[i].copy())).toArray().copy() for i in range(nx)])
+    out[key + "_Nx"] = np.stack([Nm(D(x[i].copy())).toArray().copy() for i in range(nx)])
+    out[key + "_H_cols"], out[key + "_N_cols"] = H[:, :8].copy(), N[:, :8].copy()
+    out[key + "_H_diag"], out[key + "_N_diag"] = np.diag(H).copy(), np.diag(N).copy()
+    out[key + "_H_fro"] = np.array([np.linalg.norm(H), np.linalg.norm(N)])
+    out[key + "_cost"] = np.array([Hm.cost_of_multiply, Hm.cost_of_formMatrix, Nm.cost_of_multiply])
+    return H, N
+
+
+def _grow(name, system, steps, new_dimension, out, seed_base):
+    """Per step: the lowest generalized eigenvalue of the step's (H_eff, N_eff)
+    (dense eigh, as minimizeExpectationUsingFullEigensolver), ARPACK's eigsh
+    and relaxOver from the current center; then a seeded random unit center
+    (re and im N(0,1), default_rng(seed_base + step)) is absorbed by
+    contractTowards(step % 4), and compressCornerStateTowards(corner,
+    direction, new_dimension) runs for every corner axis above new_dimension.
+    Absorbing the minimized center instead degenerates from this start: the
+    transverse-Ising minimizer is the all-up product state at every step (the
+    environment's X halves average to zero), whose rank-one boundaries make
+    the compressor's normal equations singular (GMRES's assert,
+    compression.py:43, failed on every retry), and the Heisenberg center's
+    first effective Hamiltonian is zero.  The compressor matrices the
+    reference computes are recorded in order, with the numpy seed of the
+    attempt that succeeded; a failed attempt is retried with the next seed and
+    logged."""
+    import scipy.linalg as sla
+    from scipy.sparse.linalg import LinearOperator, eigsh
+    import carcassonne.system._2d as rsys
+    orig = rsys.computeProductCompressor
+    recorded = []
+
+    def recording(Ld, Rd, nd):
+        P = orig(Ld, Rd, nd)
+        recorded.append(P.toArray().copy())
+        return P
+    rsys.computeProductCompressor = recording
+    energies, comps, retries = [], [], []
+    try:
+        for step in range(steps):
+            direction = step % 4
+            Hm, Nm = system.formExpectationAndNormalizationMultipliers()
+            H = Hm.formMatrix().toArray()
+            N = Nm.formMatrix().toArray()
+            w, v = sla.eigh(H, N)
+            shape = system.state_center_data.shape
+            n = H.shape[0]
+            ar = np.nan
+            if n > 2 and np.abs(H).max() > 0:  # ARPACK rejects the zero operator (a Heisenberg center's first step)
+                op = LinearOperator((n, n), matvec=lambda u: Hm(D(u.reshape(shape).copy())).toArray().ravel(),
+                                    dtype=np.complex128)
+                ar = float(eigsh(op, k=1, M=N, which="SA", tol=1e-10)[0][0])
+            np.random.seed(seed_base + 7919 * step)
+            relax = np.nan
+            if np.abs(H).max() > 0:
+                x = relaxOver(D(system.state_center_data.toArray().copy()), Hm, Nm,
+                              maximum_number_of_multiplications=100)
+                xr = x.toArray().ravel()
+                relax = float((np.vdot(xr, H @ xr) / np.vdot(xr, N @ xr)).real)
+            rs = np.random.default_rng(seed_base + step)
+            absorbed = cn(rs, *shape)
+            absorbed /= np.linalg.norm(absorbed)
+            system.setStateCenter(NDArrayData(absorbed.copy()))
+            out[f"{name}_{step}_absorbed"] = absorbed
+            system.contractTowards(direction)
+            e, nrm = system.computeExpectationAndNormalization()
+            energies.append([w[0], ar, relax, complex(e).real, complex(nrm).real, n,
+                             sum(len(s) for s in system.sides), len(system.corners[0])])
+            for corner_id in range(4):
+                for cdir, axis in ((0, 0), (1, 3)):
+                    if system.corners[corner_id][rsparse.Identity()].shape[axis] <= new_dimension:
+                        continue
+                    for attempt in range(8):
+                        seed = seed_base + 1000 * step + 10 * corner_id + cdir + 100000 * attempt
+                        np.random.seed(seed)
+                        try:
+                            system.compressCornerStateTowards(corner_id, cdir, new_dimension)
+                        except AssertionError as exc:
+                            retries.append([step, corner_id, cdir, attempt])
+                            print("  %s step %d corner %d dir %d: attempt %d failed (%r), retrying"
+                                  % (name, step, corner_id, cdir, attempt, exc))
+                            recorded.clear()
+                            continue
+                        P = recorded.pop()
+                        recorded.clear()
+                        out[f"{name}_P{len(comps)}"] = P
+                        comps.append([step, corner_id, cdir, seed])
+                        break
+                    else:
+                        raise RuntimeError("%s: compression failed 8 times at step %d" % (name, step))
+            print("  %s step %d: E=%.12f (eigsh %.12f, relaxOver %.12f), n=%d, side tags %d, compressions %d"
+                  % (name, step, w[0], ar, relax, n, energies[-1][6], len(comps)))
+    finally:
+        rsys.computeProductCompressor = orig
+    out[f"{name}_E"] = np.array(energies, dtype=np.float64)
+    out[f"{name}_comps"] = np.array(comps, dtype=np.int64).reshape(-1, 4)
+    out[f"{name}_retries"] = np.array(retries, dtype=np.int64).reshape(-1, 4)
+
+
+def configs():
+    import time
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    sys.path.insert(0, os.path.dirname(HERE))
+    from carcassonne_gb300 import workloads
+    out = {}
+    t0 = time.time()
+    c, s, o = workloads.matvec_problem_arrays(D=4, c_ket=8, c_bra=4, seed=1)
+    _multiplier_cases(out, "mv", c, s, o, nx=8, seed=101)
+    print("matvec operator: %.1f s" % (time.time() - t0))
+    c, s, o = workloads.matvec_problem_arrays(D=4, c_ket=8, c_bra=4, seed=4,
+                                              op_arrays=workloads.heisenberg_operator_arrays(), complex_=True)
+    _multiplier_cases(out, "mvz", c, s, o, nx=4, seed=102)
+    print("complex matvec operator: %.1f s" % (time.time() - t0))
+    import scipy.linalg as sla
+    c, s, o = workloads.hermitian_problem_arrays(D=4, c=8, seed=2)
+    H, N = _multiplier_cases(out, "pencil", c, s, o, nx=2, seed=103)
+    w, v = sla.eigh(H, N)
+    out["pencil_E"] = np.array(w[:4])
+    out["pencil_v"] = v[:, 0].copy()
+    print("solve pencil: %.1f s" % (time.time() - t0))
+    ops = operators()
+    op = {k: NDArrayData(v.toArray().copy()) for k, v in ops["ti"]().items()}
+    _grow("ti20", bond_system(op, 2, 0), 20, 8, out, seed_base=workloads.GROWTH_CENTER_SEED["ti"])
+    print("TI growth: %.1f s" % (time.time() - t0))
+    op = {k: NDArrayData(v.toArray().copy()) for k, v in ops["heis"]().items()}
+    _grow("heis8", bond_system(op, 4, 2), 8, 8, out, seed_base=workloads.GROWTH_CENTER_SEED["heis"])
+    print("Heisenberg growth: %.1f s" % (time.time() - t0))
+    np.savez_compressed(os.path.join(HERE, "configs.npz"), **out)
+
+
 if __name__ == "__main__":
     sections = dict(dense=dense_cases, tables=tables_and_trajectories, numerics=numerics, chain1d=chain1d,
-                    opcomp=opcomp)
+                    opcomp=opcomp, configs=configs)
     chosen = sys.argv[1:] or list(sections)
     for name in chosen:
         sections[name]()
-    for fn in ("dense.npz", "tables.json", "trajectory.npz", "numerics.npz", "chain1d.npz", "opcomp.npz"):
+    for fn in ("dense.npz", "tables.json", "trajectory.npz", "numerics.npz", "chain1d.npz", "opcomp.npz",
+               "configs.npz"):
         if os.path.exists(os.path.join(HERE, fn)):
             print(fn, os.path.getsize(os.path.join(HERE, fn)))
