@@ -18,9 +18,9 @@ The system (Hermitian positive semi-definite and consistent) is solved on
 the GPU by conjugate gradients to a relative residual of 1e-12 in a single
 thread block per round (``carc_zcg_hpsd``, no host round trip per
 iteration); the four rounds' status words (CG and the polar factors'
-Jacobi SVDs) are read once at the end, and an
-exhausted iteration budget raises AssertionError where GMRES would report
-non-convergence (compression.py:43).  Systems larger than the single-block
+Jacobi SVDs) are read once at the end, and a solve that ends its budget above
+the reference's GMRES tolerance (1e-5) raises AssertionError where GMRES
+would report non-convergence (compression.py:43).  Systems larger than the single-block
 solver takes fall back to a CG driven from the host, one launch per step.
 """
 from __future__ import annotations
@@ -35,6 +35,11 @@ from .data import TorchData
 from .engine import CDT, current_stream_handle
 
 CG_MAX_N = 2048  # CARC_CG_MAX_N
+# CG aims at a relative residual of 1e-12; when it stalls above that within its
+# budget (singular or ill-conditioned normal equations stop near cond(G) u),
+# the solve is accepted below the reference's own GMRES tolerance (scipy's
+# default rtol 1e-5, compression.py:38-43), and is an error above it
+ACCEPT_RESIDUAL = 1e-5
 
 
 def _normal_equations(Lt, Rt, P, b2):
@@ -85,13 +90,15 @@ def _cg_host(G, c, tol=1e-12, max_iter=None):
             return x
         p = TorchData(r)._axpby(1.0, TorchData(r), rr_new / rr, TorchData(p))._t
         rr = rr_new
+    if np.sqrt(rr / c2) <= ACCEPT_RESIDUAL:
+        return x
     raise AssertionError("normal equations of the product compressor did not converge "
                          "(residual %.3e after %d iterations)" % (np.sqrt(rr / c2), max_iter))
 
 
 def _cg_device(G, c, status, residual, tol=1e-12, max_iter=None):
     n = c.numel()
-    max_iter = max_iter or max(4 * n, 50)
+    max_iter = max_iter or max(10 * n, 500)  # one block iterates in microseconds: ill-conditioned systems need more
     x = torch.empty(n, dtype=CDT, device=c.device)
     _lib.call("carc_zcg_hpsd", n, ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(c.data_ptr()),
               ctypes.c_void_p(x.data_ptr()), float(tol), int(max_iter), ctypes.c_void_p(status.data_ptr()),
@@ -128,11 +135,12 @@ def computeProductCompressor(L, R, new_dimension, rounds=4, initial=None):
     linalg.check_deferred(svd_status)
     if on_device:
         st = status.cpu().numpy()
-        if not st[:, 1].all():
-            k = int(np.argmin(st[:, 1]))
+        res = residual.cpu().numpy()
+        bad = (st[:, 1] == 0) & (res > ACCEPT_RESIDUAL)
+        if bad.any():
+            k = int(np.argmax(bad))
             raise AssertionError("normal equations of the product compressor did not converge "
-                                 "(round %d: residual %.3e after %d iterations)"
-                                 % (k, float(residual[k].item()), int(st[k, 0])))
+                                 "(round %d: residual %.3e after %d iterations)" % (k, float(res[k]), int(st[k, 0])))
     return P.transpose()
 
 

@@ -76,7 +76,11 @@ __global__ __launch_bounds__(SVD_THREADS) void svd_jacobi_kernel(int m, int n, i
         beta = warp_sum(beta);
         gamma = warp_sum2(gamma);
         double g = sqrt(cabs2(gamma));
-        if (g == 0.0 || g <= tol * sqrt(alpha * beta)) continue;
+        // converged pair: orthogonal to tol, or the smaller column negligible
+        // (norm below 1e-14 of the larger: rounding noise of a rank-deficient
+        // input, which no rotation makes orthogonal; its U column is replaced by
+        // the orthonormal completion of svd_complete_kernel)
+        if (g == 0.0 || g <= tol * sqrt(alpha * beta) || fmin(alpha, beta) <= 1e-28 * fmax(alpha, beta)) continue;
         if (lane == 0) rotated = 1;
         double zeta = (beta - alpha) / (2.0 * g);
         double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
@@ -284,7 +288,11 @@ __global__ __launch_bounds__(HEEV_THREADS) void heev_jacobi_kernel(int n, int n_
         double2 apq = A[p * n + q];
         double g = sqrt(cabs2(apq));
         double app = A[p * n + p].x, aqq = A[q * n + q].x;
-        if (g <= 1e-300 || g <= 1e-17 * sqrt(fabs(app * aqq))) continue;
+        // converged pair: negligible against its diagonal, or against the
+        // matrix (1e-16 of the Frobenius norm: the rounding level of a nearly
+        // singular matrix, whose small diagonal entries alone would keep
+        // noise-level pairs rotating forever)
+        if (g <= 1e-300 || g <= 1e-17 * sqrt(fabs(app * aqq)) || g <= 1e-16 * sqrt(off_norm + diag_norm)) continue;
         rotated = 1;
         // phase-rotate so the off-diagonal is real, then a real Jacobi rotation
         double zeta = (aqq - app) / (2.0 * g);

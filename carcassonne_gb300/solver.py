@@ -38,8 +38,12 @@ def relaxOver(initial, expectation_multiplier, normalization_multiplier=None, ma
 
     The operators are formed densely (the reference does the same whenever it
     is cheaper, which covers the center-site sizes).  The normalization
-    matrix is factored by Cholesky (it is Hermitian positive definite on this
-    path) where the reference uses LU; both solve the same systems.  Raises
+    matrix is factored by Cholesky where the reference uses LU; both solve the
+    same systems.  N enters the reference's iteration only through the
+    product N^{-1} (H v), so where Cholesky rejects N (nearly singular, with
+    rounding-level negative eigenvalues, as right after a bandwidth increase)
+    the iteration runs on the formed N^{-1} H instead, N^{-1} taken from N's
+    Hermitian eigendecomposition: the exact inverse LU also computes.  Raises
     RelaxFailed like the reference when the Rayleigh value rises."""
     shape = initial.shape
     x0 = (initial._t if isinstance(initial, TorchData) else TorchData(initial)._t).reshape(-1).contiguous()
@@ -58,6 +62,14 @@ def relaxOver(initial, expectation_multiplier, normalization_multiplier=None, ma
     mm = -1 if maximum_number_of_multiplications is None else int(maximum_number_of_multiplications)
     st = lib.carc_relax_over(n, _vp(H), _vp(N) if N is not None else None, _vp(x0), _vp(x), k, mm, float(tolerance),
                              lam, ctypes.byref(mults), vals, _vp(ws), ws_bytes, current_stream_handle())
+    if st == _lib.CARC_NOT_POSDEF and N is not None:
+        W, V = linalg.eigh_small(TorchData(N))
+        Vt = V._t
+        VinvW = engine.contract("ij,jk->ik", Vt, torch.diag((1.0 / W).to(CDT)), (n, n))  # V diag(1/w)
+        Ninv = engine.contract("ij,kj->ik", VinvW, Vt, (n, n), conj_b=True)
+        M = engine.contract("ij,jk->ik", Ninv, H, (n, n))
+        st = lib.carc_relax_over(n, _vp(M), None, _vp(x0), _vp(x), k, mm, float(tolerance), lam,
+                                 ctypes.byref(mults), vals, _vp(ws), ws_bytes, current_stream_handle())
     if st == _lib.CARC_RELAX_FAILED:
         raise RelaxFailed(complex(vals[0], vals[1]), complex(vals[2], vals[3]))
     if st == _lib.CARC_NOT_POSDEF:

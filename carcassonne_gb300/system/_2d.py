@@ -6,14 +6,17 @@ numerical step runs in libcarcgb300: grouped stage-1/2 contractions, the
 stage-3 operator, the absorption kernels, the Jacobi SVD gauge, the product
 compressor and the generalized eigensolver.
 
-minimizeExpectation(): the reference runs relaxOver (utils.py:805-878) with a
-budget of 100 multiplications.  ``solver="lanczos"`` (default) instead finds
-the lowest generalized eigenpair of (H_eff, N_eff) to ~1e-13 relative with a
-Cholesky-reduced restarted Lanczos started from the current center;
+minimizeExpectation(): as the reference, relaxOver (utils.py:805-878) with a
+budget of 100 multiplications, on the GPU (``solver="relax"``, the default).
+``solver="lanczos"`` instead finds the lowest generalized eigenpair of
+(H_eff, N_eff) to ~1e-13 relative with a Cholesky-reduced restarted Lanczos
+started from the current center (for well-conditioned N_eff: right after a
+bandwidth increase N_eff is nearly singular, and the exact pencil's lowest
+pair can lie in its near-null space, where relaxOver, started from the
+previous center, does not go);
 ``solver="mixed"`` runs the mixed-precision solve (H_eff, N_eff formed on the
 tensor cores from split-BF16 operands, complex64 Lanczos, one FP64 Newton
-correction: FP64-level energies, solve.solve_center) from the current center;
-``solver="relax"`` runs the reference's algorithm on the GPU.
+correction: FP64-level energies, solve.solve_center) from the current center.
 """
 from __future__ import annotations
 
@@ -40,7 +43,7 @@ def sideFromCorner(corner_id, direction):
 
 
 class System(BaseSystem):
-    solver = "lanczos"
+    solver = "relax"
 
     # -- construction ----------------------------------------------------
     def __init__(self, corners, sides, state_center_data, operator_center_tensor, state_center_data_conj=None):

@@ -10,6 +10,18 @@ from tests.test_gpu_system import env  # noqa: F401  (fixture)
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(params=[0, 1, 2], autouse=True)
+def seeded(request):
+    """The runs draw their bandwidth enlargeners and compressor starts from
+    numpy's and Python's global generators, as the reference's do: each test
+    runs for three fixed seeds, independent of the tests before it."""
+    import random
+    import numpy as np
+    np.random.seed(request.param)
+    random.seed(request.param)
+    return request.param
+
+
 def _run(system, bandwidth_policy):
     from carcassonne_gb300 import policies as P
     count = [0]

@@ -120,6 +120,7 @@ def test_trajectory_energies_and_absorption(env, name):
         assert abs(e - expect_ref) <= 1e-10 * max(1, abs(expect_ref))
         assert abs(n - norm_ref) <= 1e-10 * max(1, abs(norm_ref))
         # ground-state energy: 1e-8 relative is the target; FP64 reaches ~1e-12
+        system.solver = "lanczos"
         system.minimizeExpectation()
         lam = system.last_solve["eigenvalue"]
         assert abs(lam - e_ref.real) <= 1e-10 * max(1.0, abs(e_ref.real)), (step, lam, e_ref)
