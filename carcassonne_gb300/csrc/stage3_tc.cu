@@ -662,8 +662,11 @@ struct PairWalk {
 
 // Grid-wide barrier of a cooperative launch: every CTA adds one arrival, then
 // thread 0 polls (bounded) until all gridDim.x have arrived.  Release/acquire
-// at GPU scope order the phases' global-memory writes before the reads.
-__device__ bool grid_barrier(unsigned int* ctr, volatile int* abort) {
+// at GPU scope order the phases' global-memory writes before the reads.  A
+// CTA whose wait runs out raises the launch's global abort word; every other
+// CTA polls it (every 256 polls) and stops waiting too, raising its own
+// abort flag, so the launch ends early instead of each CTA using up its bound.
+__device__ bool grid_barrier(unsigned int* ctr, int* abort_word, volatile int* abort) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -673,9 +676,11 @@ __device__ bool grid_barrier(unsigned int* ctr, volatile int* abort) {
       unsigned int v;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(ctr) : "memory");
       if (v >= gridDim.x) break;
+      if ((i & 255u) == 255u && *reinterpret_cast<volatile int*>(abort_word)) break;
       __nanosleep(64);
     }
-    if (i == (1u << 22)) *abort = 1;
+    if (i == (1u << 22)) atomicExch(abort_word, 1);
+    if (*reinterpret_cast<volatile int*>(abort_word)) *abort = 1;
   }
   __syncthreads();
   return *abort == 0;
@@ -791,7 +796,7 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
       pack_vin_slot(p.x, p.vin, p.vt, term, e - term * per_term);
     }
     asm volatile("fence.proxy.async.global;" ::: "memory");
-    grid_barrier(p.sync, abort_flag);
+    grid_barrier(p.sync, reinterpret_cast<int*>(p.sync + 2), abort_flag);
     asm volatile("fence.proxy.async.global;" ::: "memory");
   }
   // a CTA whose phase 0 failed takes no units (the status word reports it)
@@ -1107,7 +1112,8 @@ __global__ __launch_bounds__(FU_THREADS, 1) void stage3_fused_kernel(const __gri
     tc_fence_after();
     tmem_dealloc(tmem, 512);
   }
-  if (p.coop && grid_barrier(p.sync + 1, abort_flag) && warp >= 2 && warp <= 17) {
+  if (p.coop && grid_barrier(p.sync + 1, reinterpret_cast<int*>(p.sync + 2), abort_flag) && warp >= 2 &&
+      warp <= 17) {
     // ---- phase 2: the planes of all CTAs summed into y, the same arithmetic
     // as reduce_planes_cm_kernel: a unit is (column n, 32 rows); two groups
     // of 8 warps, warp w of a group takes planes w, w + 8, ... (compensated
@@ -2029,7 +2035,7 @@ int launch_fused(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, con
     fp.yl1 = s.l2 * fp.yl2;
     fp.yl0 = s.l1 * fp.yl1;
     fp.yv = s.l0 * fp.yl0;
-    fp.sync = reinterpret_cast<unsigned int*>(w.red);
+    fp.sync = reinterpret_cast<unsigned int*>(w.red);  // [arrivals phase 0, arrivals phase 2, abort word]
     CARC_CHECK_CUDA(cudaMemsetAsync(w.red, 0, 16, stream));
     cudaLaunchConfig_t cfg;
     memset(&cfg, 0, sizeof(cfg));

@@ -81,3 +81,27 @@ def test_batched_problem_distribution():
         assert ck * cb == chi
     shards = shard_by_cost([problem_cost(D, chi) for D, chi, _, _ in specs], 8)
     assert sorted(i for s in shards for i in s) == list(range(256))
+
+
+def test_problem_cost_ranks_like_costtracker():
+    """problem_cost (the sharding key) against the CostTracker count of the
+    actual operators (the oracle's, data/cost_tracker.py:17-22) for problems
+    of the batched workload's structure: the same order, within 0.1 %."""
+    import numpy as np
+    from carcassonne_gb300 import batched, workloads
+    from oracle import carc_oracle as orc
+    from tests.tagrepr import parse_tag
+    cases = [(2, 16), (3, 16), (2, 24), (4, 16), (3, 24), (2, 32)]
+    exact, est = [], []
+    for D, chi in cases:
+        ck, cb = batched.CHI_FACTORS[chi]
+        c, s, o = workloads.matvec_problem_arrays(D=D, c_ket=ck, c_bra=cb, seed=1,
+                                                  op_arrays=workloads.ti_operator_arrays(h=3.0))
+        oc = [{parse_tag(repr(t)): a for t, a in lst} for lst in c]
+        osd = [{parse_tag(repr(t)): a for t, a in lst} for lst in s]
+        oo = {parse_tag(repr(t)): a for t, a in o}
+        H, _, _ = orc.expectation_and_normalization_multipliers(oc, osd, oo)
+        exact.append(H.cost_of_multiply * 8)
+        est.append(problem_cost(D, chi, nvec=8))
+    assert list(np.argsort(exact)) == list(np.argsort(est))
+    assert all(abs(a - b) <= 1e-3 * a for a, b in zip(exact, est))
