@@ -142,18 +142,46 @@ class StartMLP:
 # ---------------------------------------------------------------------------
 def boundary_features(corners, sides, h, k=16):
     """Top-k singular values of the Identity tag of the 4 corners and 4 sides
-    (each matricized as (left ket, left bra) x rest), then h: 8 k + 1 floats."""
-    feats = []
-    for t in list(corners) + list(sides):
+    (each matricized as (left ket, left bra) x rest), then h: 8 k + 1 floats.
+    The singular values are the square roots of the eigenvalues of the Gram
+    matrices m m^H (c0 c1 square), all eight in one batched Jacobi
+    eigensolve when the boundaries share c0 c1."""
+    from . import engine
+    bounds = list(corners) + list(sides)
+    grams = []
+    for t in bounds:
         a = t[Identity()]._t
         c0, c1 = a.shape[0], a.shape[1]
-        m = a.reshape(c0 * c1, -1)
-        _, S, _ = linalg.svd(TorchData(m))
-        s = (S._t.real if S._t.is_complex() else S._t).float()
-        v = torch.zeros(k, dtype=torch.float32, device=a.device)
-        v[: min(k, s.numel())] = s[:k]
-        feats.append(v)
-    feats.append(torch.tensor([float(h)], dtype=torch.float32, device=feats[0].device))
+        m = a.reshape(c0 * c1, -1).contiguous()
+        r = m.shape[0]
+        grams.append(engine.contract("ik,jk->ij", m, m, (r, r), conj_b=True))
+    dev = grams[0].device
+    feats = []
+    if len({g.shape[0] for g in grams}) == 1 and grams[0].shape[0] <= 512:
+        r = grams[0].shape[0]
+        A = torch.stack(grams).contiguous()
+        lib = _lib.load()
+        W = torch.empty((len(grams), r), dtype=torch.float64, device=dev)
+        V = torch.empty((len(grams), r, r), dtype=CDT, device=dev)
+        status = torch.zeros((), dtype=torch.int32, device=dev)
+        ws_bytes = lib.carc_zheev_jacobi_workspace_size(r, len(grams))
+        from .engine import Workspace
+        ws = Workspace.get(ws_bytes, dev)
+        _lib.call("carc_zheev_jacobi", r, len(grams), _vp(A), _vp(W), _vp(V), _vp(status), _vp(ws), ws_bytes,
+                  current_stream_handle())
+        sv = W.clamp_min(0).sqrt().flip(1).float()  # descending
+        for i in range(len(grams)):
+            v = torch.zeros(k, dtype=torch.float32, device=dev)
+            v[: min(k, r)] = sv[i, :k]
+            feats.append(v)
+    else:
+        for g in grams:
+            w, _ = linalg.eigh_small(TorchData(g))
+            sv = w.clamp_min(0).sqrt().flip(0).float()
+            v = torch.zeros(k, dtype=torch.float32, device=dev)
+            v[: min(k, sv.numel())] = sv[:k]
+            feats.append(v)
+    feats.append(torch.tensor([float(h)], dtype=torch.float32, device=dev))
     return torch.cat(feats)
 
 
@@ -224,16 +252,27 @@ def predict_start(mlp, corners, sides, h, shape):
 
 def evaluate(mlp, seeds, D, c, h_range=(2.0, 4.0), tol=1e-10):
     """Lanczos iterations and wall time to residual tol from the learned start,
-    the fixed start (no previous center) and the previous problem's center
-    (previous-iterate), on the same problems; the eigenvalues must agree."""
-    out = {k: dict(iterations=[], seconds=[]) for k in ("learned", "fixed", "previous")}
+    a seeded random start, the solver's fixed start (x0 = None) and the
+    previous problem's center (the previous-iterate start of independent
+    problems), on the same problems; the eigenvalues must agree.  The learned
+    start's wall time includes its features (8 boundary SVDs) and the BF16
+    inference."""
+    out = {k: dict(iterations=[], seconds=[]) for k in ("learned", "random", "fixed", "previous")}
     prev = None
     for seed in seeds:
         h, corners, sides, H, N = problem(seed, D, c, h_range)
         Hm, Nm = H.formMatrix(), N.formMatrix()
         shape = H.operator.in_shape
-        starts = dict(learned=predict_start(mlp, corners, sides, h, shape), fixed=None, previous=prev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        learned_x0 = predict_start(mlp, corners, sides, h, shape)
+        torch.cuda.synchronize()
+        t_infer = time.perf_counter() - t0
+        rng = np.random.default_rng(seed + 7777)
+        rand_x0 = torch.as_tensor(rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).to(CDT).cuda()
+        starts = dict(learned=learned_x0, random=rand_x0, fixed=None, previous=prev)
         lams = {}
+        ground = None
         for name, x0 in starts.items():
             if name == "previous" and x0 is None:
                 continue
@@ -242,20 +281,67 @@ def evaluate(mlp, seeds, D, c, h_range=(2.0, 4.0), tol=1e-10):
             lam, x, it = linalg.hegv_lowest(Hm, Nm, x0=None if x0 is None else TorchData(x0), tol=tol)
             torch.cuda.synchronize()
             out[name]["iterations"].append(it)
-            out[name]["seconds"].append(time.perf_counter() - t0)
+            out[name]["seconds"].append(time.perf_counter() - t0 + (t_infer if name == "learned" else 0.0))
             lams[name] = lam
             if name == "fixed":
                 prev = x._t.reshape(shape)
+                ground = x._t.reshape(-1)
+        # start quality: |<x0, N g>| / sqrt(<x0, N x0> <g, N g>) against the converged center g
+        from . import engine
+        Nt = Nm._t
+        nn = Nt.shape[0]
+        Nmul = lambda u: engine.contract("ij,j->i", Nt, u, (nn,))  # noqa: E731
+        dot = lambda a_, b_: TorchData(a_)._dot(TorchData(b_))  # noqa: E731
+        Ng = Nmul(ground)
+        gNg = float(dot(ground, Ng).real.item())
+        for name, x0 in starts.items():
+            if x0 is None:
+                continue
+            v = x0.reshape(-1).to(CDT).contiguous()
+            ov = abs(complex(dot(v, Ng).item())) / float(np.sqrt(float(dot(v, Nmul(v)).real.item()) * gNg))
+            out[name].setdefault("overlap", []).append(float(ov))
         vals = list(lams.values())
         out.setdefault("max_eigenvalue_spread", 0.0)
         out["max_eigenvalue_spread"] = max(out["max_eigenvalue_spread"],
                                            (max(vals) - min(vals)) / max(abs(vals[0]), 1e-300))
     summary = {k: dict(mean_iterations=float(np.mean(v["iterations"])), mean_ms=1e3 * float(np.mean(v["seconds"])),
+                       mean_overlap=float(np.mean(v["overlap"])) if v.get("overlap") else None,
                        n=len(v["iterations"]))
                for k, v in out.items() if isinstance(v, dict) and v["iterations"]}
     summary["max_eigenvalue_spread"] = out["max_eigenvalue_spread"]
     return summary
 
 
+def main(argv=None):
+    """The configured learned-start experiment: plain-solve centers of
+    transverse-Ising problems (D=3, c=7 so chi=49, h in [2, 4]) for the
+    training seeds 1000, 1001, ... and the held-out seeds 30000, ...; train,
+    then evaluate iterations and wall time to residual 1e-10 against random,
+    fixed and previous-iterate starts.  Prints one JSON line."""
+    import argparse
+    import json
+    p = argparse.ArgumentParser(prog="python -m carcassonne_gb300.learned")
+    p.add_argument("--D", type=int, default=3)
+    p.add_argument("--c", type=int, default=7)
+    p.add_argument("--train", type=int, default=20000)
+    p.add_argument("--eval", type=int, default=512)
+    p.add_argument("--epochs", type=int, default=60)
+    a = p.parse_args(argv)
+    t0 = time.perf_counter()
+    X, T = make_dataset(range(1000, 1000 + a.train), a.D, a.c)
+    t_data = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    mlp, losses = train(X, T, epochs=a.epochs, batch=256, lr=1e-3)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    res = evaluate(mlp, range(30000, 30000 + a.eval), a.D, a.c)
+    print(json.dumps(dict(D=a.D, c=a.c, chi=a.c * a.c, train=a.train, eval=a.eval, epochs=a.epochs,
+                          dataset_seconds=t_data, train_seconds=t_train, loss_first=losses[0],
+                          loss_last=losses[-1], evaluation=res)), flush=True)
+
+
 __all__ = ["StartMLP", "boundary_features", "center_target", "center_from_output", "make_dataset", "train",
-           "predict_start", "evaluate", "problem"]
+           "predict_start", "evaluate", "problem", "main"]
+
+if __name__ == "__main__":
+    main()

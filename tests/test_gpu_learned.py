@@ -1,6 +1,7 @@
 """The learned start vector: the MLP kernels against the CPU oracle
-(forward, loss, every gradient, Adam), BF16 inference against FP32, and what
-the trained network gains over the fixed start on held-out problems."""
+(forward, loss, every gradient, Adam), BF16 inference against FP32, and the
+trained network's start against random, fixed and previous-iterate starts on
+held-out problems."""
 import numpy as np
 import pytest
 import torch
@@ -49,17 +50,24 @@ def test_bf16_inference_matches_fp32(learned):
     assert err < 3e-2, err
 
 
-def test_learned_start_gain(learned):
+def test_learned_start_evaluation(learned):
     """Train on plain-solve centers of transverse-Ising problems (D=3, c=2,
-    h in [2, 4]) and compare Lanczos iterations on held-out seeds: the learned
-    start against the fixed start and the previous problem's center.  All
-    starts must reach the same eigenvalue; the learned start must not cost
-    iterations on average (the measured gain is printed)."""
+    h in [2, 4]) and evaluate on held-out seeds against random, fixed and
+    previous-iterate starts: every start reaches the same eigenvalue, and the
+    evaluation reports Lanczos iterations, wall time (the learned start's
+    feature extraction and BF16 inference included) and each start's overlap
+    with the converged center.  No gain is asserted: on this problem family
+    the network's start is no better than a random one (its features, the
+    boundaries' singular values, do not fix the eigenvector's orientation in
+    the bond basis), which the configured-scale run confirms."""
     D, c = 3, 2
     X, T = learned.make_dataset(range(1000, 1384), D, c)
     mlp, losses = learned.train(X, T, epochs=120, batch=128, lr=2e-3)
-    assert losses[-1] < losses[0]
+    assert losses[-1] < 0.5 * losses[0]
     res = learned.evaluate(mlp, range(20000, 20040), D, c)
     print("learned-start evaluation:", res)
     assert res["max_eigenvalue_spread"] < 1e-9
-    assert res["learned"]["mean_iterations"] <= res["fixed"]["mean_iterations"] + 1e-9
+    for name in ("learned", "random", "fixed", "previous"):
+        assert res[name]["n"] >= 39 and res[name]["mean_iterations"] > 0
+    for name in ("learned", "random", "previous"):
+        assert 0.0 < res[name]["mean_overlap"] <= 1.0 + 1e-12
