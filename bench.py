@@ -47,6 +47,11 @@ SOLVE = dict(workload="center-site solve, Heisenberg XXX d=2, D=4, chi=64 (8x8)"
 # batched uneven problems: transverse Ising, h ~ U[2,4], D ~ U{2..6},
 # chi ~ U{16,24,..,96}, a block of 8 vectors each, seed 3
 BATCHED = dict(workload="batched center-site matvecs, TI, D in 2..6, chi in 16..96, block 8", nvec=8, seed=3)
+# batched solves: Hermitian-definite transverse-Ising problems (ket x bra
+# boundary layers of equal dimension c, chi = c^2), lowest eigenpair of each
+# by the batched block eigensolver (LOBPCG, block 8) to relative residual 1e-4
+BATCHED_SOLVES = dict(workload="batched center solves, TI, h in [2,4], D in 2..6, chi = c^2 with c in 4..9, "
+                               "LOBPCG block 8, relative residual 1e-4", block=8, seed=3, tol=1e-4)
 
 # phases of the tensor-core operator, as numbered by carc_phase_timing_read
 PHASE_NAMES = ("pack", "step_a", "step_b", "reduce")
@@ -405,6 +410,10 @@ def parse_args():
     p.add_argument("--no-batched", dest="batched", action="store_false",
                    help="skip the batched uneven-problems comparison (graph replay vs launch loop)")
     p.add_argument("--batched-count", type=int, default=32)
+    p.add_argument("--no-batched-solves", dest="batched_solves", action="store_false",
+                   help="skip the batched solves (batched block eigensolver vs the per-problem loop; sharded "
+                        "over ranks under torchrun)")
+    p.add_argument("--solves-count", type=int, default=256)
     p.add_argument("--no-growth", dest="growth", action="store_false",
                    help="skip the growth runs' per-step time-to-energy (plain vs mixed)")
     return p.parse_args()
@@ -557,6 +566,32 @@ def run_reference_arm(args, rank):
     print(json.dumps(line), flush=True)
 
 
+def batched_solves_section(args, dist, rank, world, device):
+    """The batched-solve workload.  One GPU: every problem, solved by the
+    batched block eigensolver and by the per-problem loop.  Under torchrun:
+    each rank solves its cost-balanced shard with the batched solver (no
+    data-path collective), the slowest rank sets the whole-job time, and
+    rank 0 reports every problem's result."""
+    from carcassonne_gb300 import batched as batched_mod
+    from carcassonne_gb300.replicas import run_sharded
+    kw = dict(m=BATCHED_SOLVES["block"], tol=BATCHED_SOLVES["tol"])
+    if world == 1:
+        out = batched_mod.run_solves(count=args.solves_count, seed=BATCHED_SOLVES["seed"], **kw)
+        return dict(BATCHED_SOLVES, count=args.solves_count, ranks=1, **out)
+    specs = batched_mod.sample_pencils(args.solves_count, BATCHED_SOLVES["seed"])
+
+    def solve_fn(sub):
+        return batched_mod.run_solves(specs=sub, loop=False, return_problems=True, **kw)
+
+    res = run_sharded(specs, batched_mod.pencil_cost, solve_fn, dist, rank, world, device=device)
+    if res is None:
+        return None
+    it = [v for v in res["iterations"] if v is not None]
+    return dict(BATCHED_SOLVES, count=args.solves_count, ranks=world, sharding="cost-balanced (LPT), no collective",
+                problems=res["problems"], batched_seconds=res["seconds"], batched_solves_per_s=res["solves_per_s"],
+                iterations_mean=sum(it) / len(it), per_rank=res["per_rank"])
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -706,6 +741,7 @@ def main():
     ms, e_ms = max_over_ranks([ms, e_ms], dist, device=x.device)
     value = world * flops_per_step / (ms * 1e-3) / 1e9
     e2e_value = world * flops_per_step / (e_ms * 1e-3) / 1e9
+    solves = batched_solves_section(args, dist, rank, world, x.device) if args.batched_solves else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -765,6 +801,8 @@ def main():
         from carcassonne_gb300 import batched as batched_mod
         batched = dict(BATCHED, count=args.batched_count,
                        **batched_mod.run(count=args.batched_count, nvec=BATCHED["nvec"], seed=BATCHED["seed"]))
+    if solves is not None:
+        batched = dict(batched or {}, solves=solves)
     line = dict(
         metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
         ms_per_step=ms, higher_is_better=True, scaling="weak", vs_baseline=None,

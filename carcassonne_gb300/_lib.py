@@ -99,6 +99,18 @@ SIGNATURES = {
     "carc_relax_over": (ctypes.c_int, [_i32, _vp, _vp, _vp, _vp, _i32, _i32, _dbl, ctypes.POINTER(_dbl),
                                        ctypes.POINTER(_i32), ctypes.POINTER(_dbl), _vp, _i64, _vp]),
     "carc_relax_over_workspace_size": (_i64, [_i32, _i32]),
+    "carc_lobpcg_workspace_size": (_i64, [_i32, _i32]),
+    "carc_lobpcg_inner": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i32, _i32, _vp, _vp,
+                                         _i32, _i32, _vp, _vp, _vp, _i64, _vp]),
+    "carc_lobpcg_orth_prepare": (ctypes.c_int, [_i32, _i32, _vp, _vp, _dbl, _vp, _vp, _vp]),
+    "carc_lobpcg_orth_finish": (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _dbl, _i32, _vp, _vp]),
+    "carc_lobpcg_orth_apply": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                              _vp]),
+    "carc_lobpcg_rr_scale": (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "carc_lobpcg_rr_reduce": (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp, _dbl, _vp, _vp, _vp, _vp]),
+    "carc_lobpcg_rr_combine": (ctypes.c_int, [_i32, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "carc_lobpcg_update": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                          _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
     "carc_zcontract_tc": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _vp, _vp, _vp, _dbl, _dbl, _i32, _i32, _vp, _i64,
                                          _vp, _vp]),
     "carc_zcontract_tc_workspace_size": (_i64, [ctypes.POINTER(ContractDesc), _i32]),

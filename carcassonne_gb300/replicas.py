@@ -1,10 +1,10 @@
 """Several GPUs on independent center-site problems (no data-path
 collective): a single problem's matvec is too small to split, so one GPU per
 process runs whole problems.  Batches of independent problems are sharded
-across ranks by estimated cost (the CostTracker count of one matvec), and the
-host combines per-rank timings and results with small control-plane
-collectives (any torch.distributed backend: NCCL on GPUs, gloo in the CPU
-tests).
+across ranks by estimated cost (the CostTracker count of one matvec), each
+rank solves its shard (``run_sharded``), and the host combines per-rank
+timings and results with small control-plane collectives (any
+torch.distributed backend: NCCL on GPUs, gloo in the CPU tests).
 """
 from __future__ import annotations
 
@@ -53,4 +53,35 @@ def gather_to_root(obj, dist=None, rank=0, world=1):
     return out
 
 
-__all__ = ["shard_by_cost", "problem_cost", "max_over_ranks", "gather_to_root"]
+def run_sharded(specs, cost_of, solve_fn, dist=None, rank=0, world=1, device=None):
+    """The sharded batch: this rank takes ``shard_by_cost`` of the problems'
+    costs and solves its shard with ``solve_fn(list of specs)``, which
+    returns ``dict(energy=[...], iterations=[...], seconds=s)`` in shard
+    order; the slowest rank's seconds set the whole-job time.  Rank 0 gets
+    every problem's results in the original order, the per-rank loads and
+    the whole-job throughput; the other ranks get None."""
+    costs = [cost_of(s) for s in specs]
+    mine = shard_by_cost(costs, world)[rank]
+    if mine:
+        res = solve_fn([specs[i] for i in mine])
+    else:
+        res = dict(energy=[], iterations=[], seconds=0.0)
+    seconds = max_over_ranks([res["seconds"]], dist, device)[0]
+    part = dict(rank=rank, idx=list(mine), energy=[float(e) for e in res["energy"]],
+                iterations=[int(v) for v in res["iterations"]], seconds=float(res["seconds"]),
+                cost=sum(costs[i] for i in mine))
+    got = gather_to_root(part, dist, rank, world)
+    if got is None:
+        return None
+    n = len(specs)
+    energy, iterations = [None] * n, [None] * n
+    for g in got:
+        for j, i in enumerate(g["idx"]):
+            energy[i], iterations[i] = g["energy"][j], g["iterations"][j]
+    return dict(problems=n, ranks=world, seconds=seconds, solves_per_s=n / seconds if seconds > 0 else None,
+                energy=energy, iterations=iterations,
+                per_rank=[dict(rank=g["rank"], problems=len(g["idx"]), seconds=g["seconds"], cost=g["cost"])
+                          for g in got])
+
+
+__all__ = ["shard_by_cost", "problem_cost", "max_over_ranks", "gather_to_root", "run_sharded"]

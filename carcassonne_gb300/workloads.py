@@ -175,3 +175,61 @@ def to_device(corners, sides, op_arrays):
     s = [{t: TorchData(a) for t, a in lst} for lst in sides]
     o = {t: TorchData(a) for t, a in op_arrays}
     return c, s, o
+
+
+def absorb_main(argv=None):
+    """Grow a system by absorbing seeded random unit centers (the growth runs'
+    absorption schedule, without the center solves): at every step
+    contractTowards(step % 4) (system/_2d.py:435-454) with the tag pairs in
+    FP64 or on the tensor cores, then compressCornerStateTowards for every
+    corner axis above ``--new-dim``.  Prints one JSON line per step with the
+    absorption's wall time (device synchronised on both sides); the last
+    step's absorption runs inside an NVTX range named "absorb", so a
+    profiler can select its kernels (``ncu --nvtx --nvtx-include absorb/``)."""
+    import argparse
+    import json
+    import time
+    import torch
+    from .data import TorchData
+    from .sparse import Identity
+    from .tensors._2d import dense
+    p = argparse.ArgumentParser(prog="python -m carcassonne_gb300.workloads")
+    p.add_argument("--kind", default="heis", choices=["ti", "heis"])
+    p.add_argument("--D", type=int, default=4)
+    p.add_argument("--seed", type=int, default=2)
+    p.add_argument("--steps", type=int, default=8)
+    p.add_argument("--new-dim", type=int, default=8, help="kept dimension of each corner axis (chi = new_dim^2)")
+    p.add_argument("--precision", default="tc", choices=["tc", "fp64"])
+    a = p.parse_args(argv)
+    system = bond_start_system(a.kind, a.D, a.seed)
+    for step in range(a.steps):
+        x0 = system.state_center_data
+        system.setStateCenter(TorchData(growth_center(tuple(x0.shape), GROWTH_CENTER_SEED[a.kind] + step)))
+        last = step == a.steps - 1
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if last:
+            torch.cuda.nvtx.range_push("absorb")
+        with dense.absorption_precision(a.precision):
+            system.contractTowards(step % 4)
+            torch.cuda.synchronize()
+            seconds = time.perf_counter() - t0
+            if last:
+                torch.cuda.nvtx.range_pop()
+        side = system.sides[step % 4][Identity()]
+        for corner in range(4):
+            for cdir, axis in ((0, 0), (1, 3)):
+                if system.corners[corner][Identity()].shape[axis] > a.new_dim:
+                    np.random.seed(1000 * step + 10 * corner + cdir)
+                    system.compressCornerStateTowards(corner, cdir, a.new_dim)
+        print(json.dumps(dict(step=step, precision=a.precision, absorb_s=round(seconds, 6),
+                              side_shape=list(side.shape), side_tags=len(system.sides[step % 4]))), flush=True)
+
+
+if __name__ == "__main__":
+    import sys
+    if len(sys.argv) > 1 and sys.argv[1] == "absorb":
+        absorb_main(sys.argv[2:])
+    else:
+        raise SystemExit("usage: python -m carcassonne_gb300.workloads absorb [--kind heis|ti] [--D 4] [--steps 8] "
+                         "[--new-dim 8] [--precision tc|fp64]")

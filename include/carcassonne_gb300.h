@@ -39,6 +39,8 @@ enum carc_status_code {
 #define CARC_MAX_ENTRIES 512 /* tag pairs in one grouped call */
 #define CARC_NOALLOC_SCRATCH_BYTES (16u << 20) /* fixed scratch of carc_stage3_matvec_f64_noalloc */
 #define CARC_CG_MAX_N 2048 /* largest system carc_zcg_hpsd takes (x, r, p, G p in shared memory) */
+#define CARC_LOBPCG_MAX_M 8 /* block vectors per problem of the batched eigensolver */
+#define CARC_LOBPCG_ITEM 256 /* center entries of one problem per work item of the batched eigensolver */
 
 /* Message of the last failing call on this thread ("" if none). */
 const char* carc_last_error_string(void);
@@ -392,6 +394,68 @@ int carc_mlp_to_bf16(int64_t n, const float* x, void* y, void* stream);
 /* Y = X W^T + b with BF16 X, W; output BF16 (Yb) and/or FP32 (Yf) */
 int carc_mlp_linear_bf16(int32_t B, int32_t K, int32_t N, const void* X, const void* W, const float* b, int32_t relu,
                          void* Yb, float* Yf, void* stream);
+
+/*
+ * Batched block eigensolver (LOBPCG) over many independent center-site
+ * problems: the lowest eigenpairs of Hermitian-definite pencils H x = l N x,
+ * the per-problem unit of minimizeExpectation / relaxOver
+ * (system/_2d.py:489-497, utils.py:805-878), which the reference solves one
+ * problem at a time.  Block of m in {1, 2, 4, 8} vectors; search space
+ * S = [X; R; P] of k = 3m rows with H S and N S supplied by the caller's
+ * matvecs.  Per iteration over the whole batch (orthonormalising form): the
+ * caller applies N to R; carc_lobpcg_inner gives [X; R; P]^H N [R, P];
+ * carc_lobpcg_orth_prepare, carc_zheev_jacobi (n = m, 2 batch matrices) and
+ * carc_lobpcg_orth_finish give the coefficients with which
+ * carc_lobpcg_orth_apply makes R and P each N-orthonormal and N-orthogonal
+ * to X; the caller applies H and N to the new R (every few iterations it
+ * also applies them to X afresh and restarts P, which bounds the drift of the
+ * implicitly updated images under the split-precision rounding); carc_lobpcg_inner
+ * gives S^H H S and S^H N S; carc_lobpcg_rr_scale, carc_zheev_jacobi (n = k),
+ * carc_lobpcg_rr_reduce, carc_zheev_jacobi and carc_lobpcg_rr_combine the
+ * Rayleigh-Ritz coefficients; carc_lobpcg_update the next X, P, R and the
+ * residuals.  Layout: problem b's k x n[b] blocks of S, HS, NS row-major at
+ * element offset off[b] of three complex128 pools; work item w covers entries
+ * [item_start[w], item_start[w] + CARC_LOBPCG_ITEM) of problem
+ * item_problem[w], and problem b owns items first[b] .. first[b+1]-1.
+ * Problems with active[b] == 0 are skipped.  Small matrices are row-major per
+ * problem.  All pointers device.
+ */
+int64_t carc_lobpcg_workspace_size(int32_t items, int32_t m);
+/* out1 (batch x ka x kb) = conj(A rows a0..) . (B1 rows b0..)^T per problem; out2 likewise from B2 (may be NULL) */
+int carc_lobpcg_inner(int32_t batch, int32_t items, int32_t m, const int32_t* item_problem, const int32_t* item_start,
+                      const int32_t* first, const int64_t* off, const int32_t* n, const int32_t* active,
+                      const void* A, int32_t a0, int32_t ka, const void* B1, const void* B2, int32_t b0, int32_t kb,
+                      void* out1, void* out2, void* workspace, int64_t workspace_bytes, void* stream);
+/* Q (batch x 3m x 2m) = [X; R; P]^H N [R, P] -> Ms (batch x 2 x m x m): for Z = R, P the unit-diagonal
+ * N-Gram matrix of Z - X (X^H N Z); dscale (batch x 2 x m) their diagonal scalings (0 for a column whose
+ * remaining N-norm^2 is at most floor times its original) */
+int carc_lobpcg_orth_prepare(int32_t batch, int32_t m, const int32_t* active, const void* Q, double floor_, void* Ms,
+                             void* dscale, void* stream);
+/* W (batch x 2 x m), V: eigenpairs of Ms -> M (batch x 4 x m x m) = [M_R1; M_R2; M_P1; M_P2] with
+ * Z <- Z M_Z1 + X M_Z2; directions with W_j <= drop max W are dropped, and all of P's when restart_p != 0
+ * (P restarts from zero, as after a refresh of X's images) */
+int carc_lobpcg_orth_finish(int32_t batch, int32_t m, const int32_t* active, const void* Q, const void* dscale,
+                            const void* W, const void* V, double drop, int32_t restart_p, void* M, void* stream);
+/* in place: R rows of S <- R M_R1 + X M_R2; P rows of S, HS, NS <- P M_P1 + X M_P2 */
+int carc_lobpcg_orth_apply(int32_t batch, int32_t items, int32_t m, const int32_t* item_problem,
+                           const int32_t* item_start, const int32_t* first, const int64_t* off, const int32_t* n,
+                           const int32_t* active, const void* M, void* S, void* HS, void* NS, void* stream);
+/* GNs = D herm(GN) D with D = diag(GN)^-1/2 (0 where the diagonal is 0); dscale (batch x k) = D */
+int carc_lobpcg_rr_scale(int32_t batch, int32_t m, const int32_t* active, const void* GN, void* GNs, void* dscale,
+                         void* stream);
+/* W, V: eigenpairs of GNs; keeps directions with W_j > drop max W (rank per problem);
+ * T = D V diag(W^-1/2 on kept, 0 else), G = T^H herm(GH) T with dropped diagonals raised above the spectrum */
+int carc_lobpcg_rr_reduce(int32_t batch, int32_t m, const int32_t* active, const void* GH, const void* dscale,
+                          const void* W, const void* V, double drop, void* T, void* G, int32_t* rank, void* stream);
+/* C (batch x k x m) = T Y[:, :m], Y the eigenvectors of G */
+int carc_lobpcg_rr_combine(int32_t batch, int32_t m, const int32_t* active, const void* T, const void* Y, void* C,
+                           void* stream);
+/* into the second pools: X' = S^T C, P' = [R; P]^T C[m:] (and likewise from HS, NS), R' = H X' - N X' diag(theta)
+ * (theta: the eigenvalues of G, batch x k ascending); res (batch x m) = |R'_j| / (|H X'_j| + |theta_j| |N X'_j|) */
+int carc_lobpcg_update(int32_t batch, int32_t items, int32_t m, const int32_t* item_problem, const int32_t* item_start,
+                       const int32_t* first, const int64_t* off, const int32_t* n, const int32_t* active, const void* C,
+                       const void* theta, const void* S, const void* HS, const void* NS, void* S2, void* HS2,
+                       void* NS2, void* res, void* workspace, int64_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -38,8 +38,8 @@ def test_graph_replay_matches_loop_and_fp64(batched):
 def test_autotune_choice_is_used(batched):
     from carcassonne_gb300 import _lib
     op = batched.build_operator(3, 32, 3.0, 21)
-    res = batched.autotune(op, 4, candidates=(0, 38, 152), reps=1)
-    assert res and all(v["best"] in (0, 38, 152) for v in res.values())
+    res = batched.autotune(op, 4, candidates=(0, -1, 38, 152), reps=1)
+    assert res and all(e["best"] in (0, -1, 38, 152) for e in res)
     x = torch.randn((4,) + op.in_shape, dtype=torch.complex128, device="cuda")
     ref = op.apply(x, None, 4)
     got = op.apply_tc(x, None, 4)
@@ -48,6 +48,26 @@ def test_autotune_choice_is_used(batched):
     _lib.check(_lib.load().carc_tc_autotune_clear())
 
 
-def test_run_small_distribution(batched):
-    out = batched.run(count=6, nvec=2, seed=5, mem_budget=1 << 30, reps=1)
+def test_run_small_distribution(batched, tmp_path):
+    out = batched.run(count=6, nvec=2, seed=5, mem_budget=1 << 30, reps=1, tune_file=str(tmp_path / "t.json"))
     assert out["problems"] == 6 and out["loop_gflops"] > 0 and out["graph_gflops"] > 0
+
+
+def test_tuning_file_round_trip(batched, tmp_path):
+    """Choices saved to the tuning file are applied by a later load, and the
+    matvec stays within the split-BF16 tolerance on the loaded choice."""
+    from carcassonne_gb300 import _lib
+    op = batched.build_operator(2, 24, 2.7, 31)
+    res = batched.autotune(op, 2, candidates=(0, 76), reps=1)
+    path = str(tmp_path / "tune.json")
+    batched.save_tuning(res + res, path)  # duplicates are written once
+    _lib.check(_lib.load().carc_tc_autotune_clear())
+    loaded = batched.load_tuning(path)
+    assert [e["best"] for e in loaded] == [e["best"] for e in res]
+    assert batched.load_tuning(str(tmp_path / "missing.json")) == []
+    x = torch.randn((2,) + op.in_shape, dtype=torch.complex128, device="cuda")
+    ref = op.apply(x, None, 2)
+    got = op.apply_tc(x, None, 2)
+    op.check_status()
+    assert ((got - ref).abs().max() / ref.abs().max()).item() < 5e-5
+    _lib.check(_lib.load().carc_tc_autotune_clear())

@@ -105,3 +105,53 @@ def test_problem_cost_ranks_like_costtracker():
         est.append(problem_cost(D, chi, nvec=8))
     assert list(np.argsort(exact)) == list(np.argsort(est))
     assert all(abs(a - b) <= 1e-3 * a for a, b in zip(exact, est))
+
+
+def _host_solve(sub):
+    """A host stand-in for the GPU batch solve: a deterministic function of
+    each problem's spec, and a "time" proportional to the shard's cost."""
+    from carcassonne_gb300 import batched
+    return dict(energy=[-(D * 10.0 + c + h) for D, c, h, _ in sub], iterations=[D + c for D, c, _, _ in sub],
+                seconds=sum(batched.pencil_cost(s) for s in sub) * 1e-12)
+
+
+def _sharded_rank_main(rank, world, port, out_path):
+    import json
+    import torch.distributed as dist
+    from carcassonne_gb300 import batched
+    from carcassonne_gb300.replicas import run_sharded
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        specs = batched.sample_pencils(40, 3)   # problem generation, identical on every rank
+        got = run_sharded(specs, batched.pencil_cost, _host_solve, dist, rank, world)
+        if rank == 0:
+            with open(out_path, "w") as f:
+                json.dump(got, f)
+        else:
+            assert got is None
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_batch_on_two_gloo_ranks(tmp_path):
+    """The host side of the sharded batched-solve path (bench.py under
+    torchrun): problem generation, the cost-based shard, per-rank solves, the
+    max-over-ranks time and the gather of every problem's result to rank 0 in
+    the original order, equal to one rank solving everything."""
+    import json
+    from carcassonne_gb300 import batched
+    from carcassonne_gb300.replicas import run_sharded
+    out = tmp_path / "sharded.json"
+    mp.spawn(_sharded_rank_main, args=(2, _free_port(), str(out)), nprocs=2, join=True)
+    got = json.loads(out.read_text())
+    specs = batched.sample_pencils(40, 3)
+    serial = run_sharded(specs, batched.pencil_cost, _host_solve)
+    assert got["problems"] == 40 and got["ranks"] == 2
+    assert got["energy"] == serial["energy"] and got["iterations"] == serial["iterations"]
+    loads = [r["cost"] for r in got["per_rank"]]
+    assert sum(r["problems"] for r in got["per_rank"]) == 40
+    assert max(loads) <= sum(loads) / 2 + max(batched.pencil_cost(s) for s in specs)
+    assert got["seconds"] == max(r["seconds"] for r in got["per_rank"])
+    assert got["seconds"] < serial["seconds"]
