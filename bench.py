@@ -274,7 +274,7 @@ def growth_run(spec, cpu_steps=()):
     time."""
     import numpy as np
     from copy import copy
-    from carcassonne_gb300 import workloads
+    from carcassonne_gb300 import compression, workloads
     from carcassonne_gb300.data import TorchData
     from carcassonne_gb300.sparse import Identity
     from carcassonne_gb300.solve import solve_center
@@ -306,6 +306,19 @@ def growth_run(spec, cpu_steps=()):
         tc_err = max(float((tc[t]._t - ref[t]._t).abs().max() / ref[t]._t.abs().max().clamp_min(1e-300))
                      for tc, ref in zip(tc_sys.corners + tc_sys.sides, system.corners + system.sides) for t in ref)
         del tc_sys
+        # the same compressions with the normal equations' big contractions on
+        # the tensor cores, on a copy (same random starts)
+        tc_c = copy(system)
+        t_compress_tc = 0.0
+        with compression.compression_precision("tc"):
+            for corner in range(4):
+                for cdir, axis in ((0, 0), (1, 3)):
+                    if tc_c.corners[corner][Identity()].shape[axis] > spec["new_dimension"]:
+                        np.random.seed(1000 * step + 10 * corner + cdir)
+                        _, t = _sync_time(lambda: tc_c.compressCornerStateTowards(corner, cdir,
+                                                                                  spec["new_dimension"]))
+                        t_compress_tc += t
+        del tc_c
         t_compress = 0.0
         for corner in range(4):
             for cdir, axis in ((0, 0), (1, 3)):
@@ -313,7 +326,8 @@ def growth_run(spec, cpu_steps=()):
                     np.random.seed(1000 * step + 10 * corner + cdir)
                     _, t = _sync_time(lambda: system.compressCornerStateTowards(corner, cdir, spec["new_dimension"]))
                     t_compress += t
-        rec.update(contract_s=t_contract, contract_tc_s=t_tc, contract_tc_rel_err=tc_err, compress_s=t_compress)
+        rec.update(contract_s=t_contract, contract_tc_s=t_tc, contract_tc_rel_err=tc_err, compress_s=t_compress,
+                   compress_tc_s=t_compress_tc)
         steps.append(rec)
     tot = lambda k: sum(r[k] for r in steps)
     out = dict(spec, steps_detail=[{k: (round(v, 6) if isinstance(v, float) and k.endswith("_s") else v)
@@ -322,7 +336,7 @@ def growth_run(spec, cpu_steps=()):
                time_to_energy_mixed_s=tot("build_s") + tot("mixed_solve_s"),
                solve_plain_s=tot("plain_solve_s"), solve_mixed_s=tot("mixed_solve_s"),
                build_s=tot("build_s"), contract_s=tot("contract_s"), contract_tc_s=tot("contract_tc_s"),
-               compress_s=tot("compress_s"), max_rel_err_mixed=max(r["rel_err_mixed"] for r in steps),
+               compress_s=tot("compress_s"), compress_tc_s=tot("compress_tc_s"), max_rel_err_mixed=max(r["rel_err_mixed"] for r in steps),
                max_contract_tc_rel_err=max(r["contract_tc_rel_err"] for r in steps))
     out["speedup_solve"] = out["solve_plain_s"] / out["solve_mixed_s"]
     out["speedup_time_to_energy"] = out["time_to_energy_plain_s"] / out["time_to_energy_mixed_s"]
@@ -339,6 +353,7 @@ def growth_run(spec, cpu_steps=()):
             gpu_contract_tc_seconds_same_steps=[round(r["contract_tc_s"], 5) for r in cpu],
             compress_seconds=[round(r["cpu_compress_s"], 4) for r in cpu],
             gpu_compress_seconds_same_steps=[round(r["compress_s"], 5) for r in cpu],
+            gpu_compress_tc_seconds_same_steps=[round(r["compress_tc_s"], 5) for r in cpu],
             sample="oracle/carc_oracle.py on host copies of the same environments: multipliers, formMatrix, "
                    "scipy.linalg.eigh; contractTowards; compressCornerStateTowards with a direct least-squares "
                    "solve (numpy/BLAS, all host threads)")

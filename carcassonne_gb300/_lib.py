@@ -114,6 +114,9 @@ SIGNATURES = {
     "carc_zcontract_tc": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _vp, _vp, _vp, _dbl, _dbl, _i32, _i32, _vp, _i64,
                                          _vp, _vp]),
     "carc_zcontract_tc_workspace_size": (_i64, [ctypes.POINTER(ContractDesc), _i32]),
+    "carc_zcontract_tc_grouped": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _pvp, _i32, _pvp, _i32, _pvp, _i32,
+                                                 _pi32, _i32, _dbl, _dbl, _i32, _vp, _i64, _vp, _vp]),
+    "carc_zcontract_tc_grouped_workspace_size": (_i64, [ctypes.POINTER(ContractDesc), _i32, _i32, _i32]),
     "carc_stage3_tc_plan_size": (_i64, [_pi64, _pi64, _pi32, _i32]),
     "carc_stage3_tc_prepare": (ctypes.c_int, [_pi64, _pi64, _pvp, _i32, _pvp, _i32, _pi32, _i32, _vp, _i64, _vp]),
     "carc_stage3_matvec_tc": (ctypes.c_int, [_pi64, _pi64, _i64, _vp, _i32, _i32, _pvp, _i32, _pi32, _i32, _vp, _vp,

@@ -42,6 +42,47 @@ CG_MAX_N = 2048  # CARC_CG_MAX_N
 ACCEPT_RESIDUAL = 1e-5
 
 
+# Precision of the normal equations' contractions: "fp64" (the parity path)
+# or "tc" (every contraction on the tensor cores with split-BF16 operands,
+# ~1e-5 relative, the size of the reference's own GMRES tolerance); set it
+# with ``compression_precision(...)``.
+_PRECISION = {"precision": "fp64", "status": []}
+
+
+class compression_precision:
+    """Context manager selecting the compressor's contraction precision
+    ("fp64" or "tc"); on exit the tensor-core status words are checked."""
+
+    def __init__(self, precision):
+        if precision not in ("fp64", "tc"):
+            raise ValueError("compression precision must be 'fp64' or 'tc', not %r" % (precision,))
+        self.precision = precision
+        self.previous = None
+
+    def __enter__(self):
+        self.previous = _PRECISION["precision"]
+        _PRECISION["precision"] = self.precision
+        return self
+
+    def __exit__(self, *exc):
+        _PRECISION["precision"] = self.previous
+        st, _PRECISION["status"] = _PRECISION["status"], []
+        if st and int(torch.cat([t.reshape(-1) for t in st]).abs().max().item()) != 0:
+            raise _lib.CarcNotConverged(_lib.CARC_NOT_CONVERGED, "tensor-core compression: a pipeline wait timed out")
+        return False
+
+
+def _ct(spec, a, b, out_shape, conj_a=False, conj_b=False, big=False):
+    """One contraction of the normal equations; the big ones (``big``) go to
+    the tensor cores in "tc" mode."""
+    if big and _PRECISION["precision"] == "tc":
+        out = torch.empty(tuple(int(x) for x in out_shape), dtype=CDT, device=a.device)
+        _PRECISION["status"].append(engine.contract_grouped_tc(spec, [a], [b], [out], [(0, 0, 0)], conj_a=conj_a,
+                                                               conj_b=conj_b))
+        return out
+    return engine.contract(spec, a, b, out_shape, conj_a=conj_a, conj_b=conj_b)
+
+
 def _normal_equations(Lt, Rt, P, b2):
     """G = A^H A and c = A^H b of A[(l,r),(a,i)] = sum L[l,a,b,o] conj(P[b,j])
     conj(P[c,i]) P[e,j] R[c,e,o,r] (the reference's join list, compression.py:12-25),
@@ -50,14 +91,19 @@ def _normal_equations(Lt, Rt, P, b2):
     r = Rt.shape[3]
     new = P.shape[1]
     n = old * new
-    t1 = engine.contract("labo,bj->laoj", Lt, P, (l, old, op, new), conj_b=True)
-    t2 = engine.contract("ej,ceor->jcor", P, Rt, (new, old, op, r))
-    t3 = engine.contract("ci,jcor->ijor", P, t2, (new, new, op, r), conj_a=True)
-    X = engine.contract("laoj,lbpk->aojbpk", t1, t1, (old, op, new, old, op, new), conj_a=True)
-    Y = engine.contract("ijor,xkpr->ijoxkp", t3, t3, (new, new, op, new, new, op), conj_a=True)
-    G = engine.contract("aojbpk,ijoxkp->aibx", X, Y, (old, new, old, new)).reshape(n, n)
-    u = engine.contract("ijor,lr->lijo", t3, b2, (l, new, new, op), conj_a=True)
-    c = engine.contract("laoj,lijo->ai", t1, u, (old, new), conj_a=True).reshape(n)
+    # the terms with the long boundary index l (t1, X, u, c) carry almost all
+    # of the work; the rest stay in FP64
+    t1 = _ct("labo,bj->laoj", Lt, P, (l, old, op, new), conj_b=True, big=True)
+    t2 = _ct("ej,ceor->jcor", P, Rt, (new, old, op, r))
+    t3 = _ct("ci,jcor->ijor", P, t2, (new, new, op, r), conj_a=True)
+    X = _ct("laoj,lbpk->aojbpk", t1, t1, (old, op, new, old, op, new), conj_a=True, big=True)
+    Y = _ct("ijor,xkpr->ijoxkp", t3, t3, (new, new, op, new, new, op), conj_a=True)
+    G = _ct("aojbpk,ijoxkp->aibx", X, Y, (old, new, old, new)).reshape(n, n)
+    if _PRECISION["precision"] == "tc":
+        # the split-precision X is Hermitian only to its rounding: so is G
+        G = TorchData(G)._axpby(0.5, TorchData(G), 0.5, TorchData(engine.permute(G, (1, 0), conj=True)))._t
+    u = _ct("ijor,lr->lijo", t3, b2, (l, new, new, op), conj_a=True, big=True)
+    c = _ct("laoj,lijo->ai", t1, u, (old, new), conj_a=True, big=True).reshape(n)
     return G, c
 
 
@@ -144,4 +190,4 @@ def computeProductCompressor(L, R, new_dimension, rounds=4, initial=None):
     return P.transpose()
 
 
-__all__ = ["computeProductCompressor"]
+__all__ = ["computeProductCompressor", "compression_precision"]

@@ -246,6 +246,28 @@ int64_t carc_zcontract_tc_workspace_size(const carc_contract_desc* desc, int32_t
   return zgemm_tc_workspace(zview_a(*desc, nullptr), zview_b(*desc, nullptr), ksplit);
 }
 
+int carc_zcontract_tc_grouped(const carc_contract_desc* desc, const void* const* a_ptrs, int32_t n_a,
+                              const void* const* b_ptrs, int32_t n_b, void* const* c_ptrs, int32_t n_c,
+                              const int32_t* entries, int32_t n_entries, double alpha_re, double alpha_im,
+                              int32_t accumulate, void* workspace, int64_t workspace_bytes, void* status,
+                              void* stream) {
+  if (!desc || !a_ptrs || !b_ptrs || !c_ptrs || !entries || !status)
+    return fail(CARC_BAD_ARG, "carc_zcontract_tc_grouped: NULL argument");
+  CARC_RETURN_IF(validate_desc(*desc));
+  ZView a = zview_a(*desc, nullptr), b = zview_b(*desc, nullptr);
+  ZOut c = zout_c(*desc, nullptr);
+  CARC_CHECK_CUDA(cudaMemsetAsync(status, 0, sizeof(int), as_stream(stream)));
+  return zgemm_tc_grouped(a, b, c, a_ptrs, n_a, b_ptrs, n_b, c_ptrs, n_c, entries, n_entries,
+                          cmk(alpha_re, alpha_im), accumulate, workspace, workspace_bytes, static_cast<int*>(status),
+                          as_stream(stream));
+}
+
+int64_t carc_zcontract_tc_grouped_workspace_size(const carc_contract_desc* desc, int32_t n_a, int32_t n_b,
+                                                 int32_t n_entries) {
+  if (!desc || validate_desc(*desc) != CARC_OK || n_a < 1 || n_b < 1 || n_entries < 1) return -1;
+  return zgemm_tc_grouped_workspace(zview_a(*desc, nullptr), zview_b(*desc, nullptr), n_a, n_b, n_entries);
+}
+
 int carc_gemm_bf16_tn(const void* A, int32_t M, const void* B, int32_t N, int32_t K, float* out, int64_t ld_out,
                       int32_t ksplit, void* status, void* stream) {
   if (!A || !B || !out || !status) return fail(CARC_BAD_ARG, "carc_gemm_bf16_tn: NULL argument");

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 namespace carc {
 
@@ -177,13 +178,13 @@ __device__ __forceinline__ void fold_write(const float* sP, const FoldEpi& fe, i
 // Plain GEMM: out[z][m][n] = sum over split z's K blocks of A[m,:] . B[n,:].
 // The N tile is bn: BN, or (on the BN = 256 instance) any multiple of 16 up
 // to 256 chosen at run time; shared-memory stages and TMEM are sized for BN.
+// One tile: A rows [a_y, a_y + 128) and B rows [b_y, b_y + bn) over the K
+// blocks [kb0, kb0 + nkb), accumulated in TMEM and stored as FP32 at
+// out_tile (row pitch ld_out).
 template <int BN>
-__global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
-                                                                  const __grid_constant__ CUtensorMap tmB,
-                                                                  float* __restrict__ out, int64_t ld_out,
-                                                                  int64_t split_stride, int kb_per_split,
-                                                                  int kb_total, int a_rows, int* __restrict__ err,
-                                                                  int bn, int b_blk) {
+__device__ __forceinline__ void gemm_tile(const CUtensorMap* tmA, const CUtensorMap* tmB, float* __restrict__ out_tile,
+                                          int64_t ld_out, int a_y, int b_y, int kb0, int nkb, int a_rows,
+                                          int* __restrict__ err, int bn, int b_blk) {
   using namespace umma;
   constexpr int B_STAGE_BYTES = BN * BK * 2;
   constexpr uint32_t TMEM_COLS = tmem_cols_for(BN);
@@ -198,10 +199,6 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * bn;
-  const int kb0 = blockIdx.z * kb_per_split;
-  const int kb1 = min(kb_total, kb0 + kb_per_split);
-  const int nkb = max(0, kb1 - kb0);
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -230,8 +227,8 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
   if (warp == 0) {
     if (lane == 0) {
       // TMA producer
-      prefetch_tensormap(&tmA);
-      prefetch_tensormap(&tmB);
+      prefetch_tensormap(tmA);
+      prefetch_tensormap(tmB);
       int issued = 0;
       for (int i = 0; i < nkb; ++i) {
         const int s = i % STAGES;
@@ -239,11 +236,11 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
         if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag)) break;
         mbar_arrive_expect_tx(&full[s], (uint32_t)(a_rows * BK * 2 + bn * BK * 2));
         const int kx = (kb0 + i) * BK;
-        tma_load_2d(sA + s * A_STAGE_BYTES, &tmA, kx, m0, &full[s]);
+        tma_load_2d(sA + s * A_STAGE_BYTES, tmA, kx, a_y, &full[s]);
         if (b_blk)
-          tma_load_3d(sB + s * B_STAGE_BYTES, &tmB, 0, n0, kb0 + i, &full[s]);
+          tma_load_3d(sB + s * B_STAGE_BYTES, tmB, 0, b_y, kb0 + i, &full[s]);
         else
-          tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, kx, n0, &full[s]);
+          tma_load_2d(sB + s * B_STAGE_BYTES, tmB, kx, b_y, &full[s]);
         ++issued;
       }
       if (*abort_flag) {
@@ -284,8 +281,7 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
     const bool ok = mbar_wait_sleep(done, 0, abort_flag);
     tc_fence_after();
     if (ok) {
-      const int row = m0 + quad * 32 + lane;
-      float* dst = out + (int64_t)blockIdx.z * split_stride + (int64_t)row * ld_out + n0;
+      float* dst = out_tile + (int64_t)(quad * 32 + lane) * ld_out;
 #pragma unroll 1
       for (int c0 = 0; c0 < bn; c0 += 32) {
         uint32_t r[32];
@@ -300,6 +296,260 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_c
               nkb > 0 ? make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
                                     __uint_as_float(r[j + 3]))
                       : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0 && *abort_flag) atomicExch(err, CARC_NOT_CONVERGED);
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, TMEM_COLS);
+  }
+}
+
+template <int BN>
+__global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                                  const __grid_constant__ CUtensorMap tmB,
+                                                                  float* __restrict__ out, int64_t ld_out,
+                                                                  int64_t split_stride, int kb_per_split,
+                                                                  int kb_total, int a_rows, int* __restrict__ err,
+                                                                  int bn, int b_blk) {
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * bn;
+  const int kb0 = blockIdx.z * kb_per_split;
+  const int nkb = max(0, min(kb_total, kb0 + kb_per_split) - kb0);
+  gemm_tile<BN>(&tmA, &tmB, out + (int64_t)blockIdx.z * split_stride + (int64_t)m0 * ld_out + n0, ld_out, m0, n0,
+                kb0, nkb, a_rows, err, bn, b_blk);
+}
+
+// Grouped GEMM over a table of (A block, B block) pairs of one shape feeding
+// a set of outputs: the A operands are stacked in one buffer (a_rows_per rows
+// each), the B operands in another (b_rows_per rows each), so one tensor map
+// covers each.  CTA (m tile, n tile, o ks + z) chains the K blocks of split z
+// of every entry of output o (entries e_first[o] .. e_first[o+1]-1, in table
+// order) through one TMEM accumulator.  With one split the epilogue writes
+// the complex FP64 result straight into output o; with several it writes an
+// FP32 plane (o ks + z) for the grouped reduction.
+struct GemmGroup {
+  int n_out, ks, a_rows_per, b_rows_per, kb_total, kb_per;
+  int e_first[CARC_MAX_SLOTS + 1];
+  int2 ij[CARC_MAX_ENTRIES];
+};
+
+struct GroupEpi {
+  int nm, nn, accumulate, alpha_one;
+  int64_t m_ext[CARC_MAX_SUBDIMS], m_str[CARC_MAX_SUBDIMS];
+  int64_t n_ext[CARC_MAX_SUBDIMS], n_str[CARC_MAX_SUBDIMS];
+  int64_t Mc, Nc;
+  double2 alpha;
+  double2* dst[CARC_MAX_SLOTS];
+};
+
+// float -> double by its bit fields (IEEE 754: exponent rebased by 1023 - 127,
+// mantissa moved up 29 bits), on the integer pipe: the conversion instruction
+// issues on the FP64 pipe, whose rate is low on this part.  Infinities and
+// NaNs map to their double counterparts; float subnormals (below 1.2e-38,
+// far under the 1e-5 scale of the split-precision result's error) to zero.
+__device__ __forceinline__ double f32_to_f64_int(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t sign = u & 0x80000000u, e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  uint32_t hi, lo;
+  if (e == 0u) {
+    hi = sign;
+    lo = 0u;
+  } else {
+    const uint32_t ed = e == 0xffu ? 0x7ffu : e + (1023u - 127u);
+    hi = sign | (ed << 20) | (m >> 3);
+    lo = m << 29;
+  }
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+__device__ __forceinline__ int64_t epi_decomp(int64_t idx, int n, const int64_t* ext, const int64_t* str) {
+  int64_t off = 0;
+  for (int j = n - 1; j >= 0; --j) {
+    const int64_t q = idx % ext[j];
+    idx /= ext[j];
+    off += q * str[j];
+  }
+  return off;
+}
+
+template <int BN, int NST>
+__global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_grouped_kernel(const __grid_constant__ CUtensorMap tmA,
+                                                                          const __grid_constant__ CUtensorMap tmB,
+                                                                          float* __restrict__ planes, int64_t ld,
+                                                                          int64_t plane_stride, int* __restrict__ err,
+                                                                          int bn, const __grid_constant__ GemmGroup grp,
+                                                                          const __grid_constant__ GroupEpi epi) {
+  using namespace umma;
+  constexpr int B_STAGE_BYTES = BN * BK * 2;
+  constexpr uint32_t TMEM_COLS = tmem_cols_for(BN);
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + NST * A_STAGE_BYTES;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + NST * B_STAGE_BYTES);
+  uint64_t* empty = full + NST;
+  uint64_t* done = empty + NST;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int o = blockIdx.z / grp.ks, z = blockIdx.z - o * grp.ks;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * bn;
+  const int kb0 = z * grp.kb_per;
+  const int nkb = max(0, min(grp.kb_total, kb0 + grp.kb_per) - kb0);
+  const int e0 = grp.e_first[o];
+  const int n_iter = (grp.e_first[o + 1] - e0) * nkb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    *abort_flag = 0;
+    fence_barrier_init();
+  }
+  if (warp == 1) tmem_alloc(tmem_slot, TMEM_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // TMA producer: the K blocks of split z of each entry, entry after entry
+      prefetch_tensormap(&tmA);
+      prefetch_tensormap(&tmB);
+      int issued = 0;
+      for (int i = 0; i < n_iter; ++i) {
+        const int s = i % NST;
+        const uint32_t ph = (uint32_t)((i / NST) & 1);
+        if (!mbar_wait(&empty[s], ph ^ 1u, abort_flag)) break;
+        const int q = i / nkb, e = e0 + q;
+        const int kx = (kb0 + i - q * nkb) * BK;
+        mbar_arrive_expect_tx(&full[s], (uint32_t)(BM * BK * 2 + bn * BK * 2));
+        tma_load_2d(sA + s * A_STAGE_BYTES, &tmA, kx, grp.ij[e].x * grp.a_rows_per + m0, &full[s]);
+        tma_load_2d(sB + s * B_STAGE_BYTES, &tmB, kx, grp.ij[e].y * grp.b_rows_per + n0, &full[s]);
+        ++issued;
+      }
+      if (*abort_flag) {
+        // let copies already in flight land before the CTA exits (bounded)
+        for (int i = max(0, issued - NST); i < issued; ++i) {
+          const int s = i % NST;
+          for (uint32_t t = 0; t < (1u << 20); ++t)
+            if (mbar_try_wait(&full[s], (uint32_t)((i / NST) & 1))) break;
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(BM, bn);
+      for (int i = 0; i < n_iter; ++i) {
+        const int s = i % NST;
+        const uint32_t ph = (uint32_t)((i / NST) & 1);
+        if (!mbar_wait(&full[s], ph, abort_flag)) break;
+        tc_fence_after();
+        const uint32_t a_base = smem_u32(sA + s * A_STAGE_BYTES);
+        const uint32_t b_base = smem_u32(sB + s * B_STAGE_BYTES);
+#pragma unroll
+        for (int kk = 0; kk < BK / 16; ++kk) {
+          const uint64_t ad = smem_desc_sw128(a_base + kk * 32);
+          const uint64_t bd = smem_desc_sw128(b_base + kk * 32);
+          mma_bf16(tmem, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+        }
+        mma_commit(&empty[s]);
+      }
+      mma_commit(done);
+    }
+  } else {
+    // epilogue: warps 2..5 (TMEM lane quadrant warp % 4)
+    const int quad = warp & 3;
+    const int et = threadIdx.x - 64;  // 0..127
+    int64_t* ntab = reinterpret_cast<int64_t*>(reinterpret_cast<uint8_t*>(full) + 256);  // bn column offsets
+    int64_t* mtab = ntab + 256;                                                          // 32 row offsets
+    if (grp.ks == 1) {
+      // output offsets of the tile's columns and complex rows, while the main loop runs
+      for (int q = et; q < bn; q += 128) {
+        const int64_t n = (int64_t)n0 + q;
+        ntab[q] = n < epi.Nc ? epi_decomp(n, epi.nn, epi.n_ext, epi.n_str) : -1;
+      }
+      if (et < 32) {
+        const int64_t m = (int64_t)(m0 >> 2) + et;
+        mtab[et] = m < epi.Mc ? epi_decomp(m, epi.nm, epi.m_ext, epi.m_str) : -1;
+      }
+    }
+    const bool waited = mbar_wait_sleep(done, 0, abort_flag);
+    // one decision for the four epilogue warps (named barrier 1), which also
+    // publishes the offset tables
+    uint32_t all_ok;
+    asm volatile(
+        "{\n"
+        ".reg .pred p, q;\n"
+        "setp.ne.u32 q, %1, 0;\n"
+        "bar.red.and.pred p, 1, 128, q;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(all_ok)
+        : "r"((uint32_t)waited)
+        : "memory");
+    tc_fence_after();
+    if (all_ok) {
+      const int row = m0 + quad * 32 + lane;
+      if (grp.ks > 1) {
+        float* dst = planes + (int64_t)blockIdx.z * plane_stride + (int64_t)row * ld + n0;
+#pragma unroll 1
+        for (int c0 = 0; c0 < bn; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int j = 0; j < 32; j += 4) {
+            if (c0 + j >= bn) break;
+            *reinterpret_cast<float4*>(dst + c0 + j) =
+                n_iter > 0 ? make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
+                                         __uint_as_float(r[j + 3]))
+                           : make_float4(0.f, 0.f, 0.f, 0.f);
+          }
+        }
+      } else {
+        // 32 columns at a time through shared memory (the A stages, free once
+        // every MMA has completed): rows 4m + 2c + s staged with a pitch of 33
+        // floats, then each thread forms C[m, n] = (hi + lo) + i (hi + lo) in
+        // FP64 for one column n of several complex rows m, consecutive n on
+        // consecutive lanes (coalesced stores into the output)
+        float* stage = reinterpret_cast<float*>(sA);
+        double2* C = epi.dst[o];
+        const int nl = et & 31;
+#pragma unroll 1
+        for (int c0 = 0; c0 < bn; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)c0, r);
+          tmem_ld_wait();
+          float* srow = stage + (quad * 32 + lane) * 33;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) srow[j] = n_iter > 0 ? __uint_as_float(r[j]) : 0.f;
+          asm volatile("bar.sync 1, 128;" ::: "memory");
+          const int64_t no = c0 + nl < bn ? ntab[c0 + nl] : -1;
+#pragma unroll 2
+          for (int i = et >> 5; i < 32; i += 4) {
+            const int64_t mo = mtab[i];
+            if (mo >= 0 && no >= 0) {
+              // hi + lo in FP32 (6e-8 relative, far below the split's 1e-5) and
+              // converted on the integer pipe: no FP64 instruction, whose issue
+              // rate is low on this part, unless alpha != 1 or C is added
+              const float* sv = stage + (4 * i) * 33 + nl;
+              double2 val = make_double2(f32_to_f64_int(__fadd_rn(sv[0], sv[33])),
+                                         f32_to_f64_int(__fadd_rn(sv[66], sv[99])));
+              if (!epi.alpha_one) val = cmul(epi.alpha, val);
+              if (epi.accumulate) val = cadd(val, C[mo + no]);
+              C[mo + no] = val;
+            }
+          }
+          asm volatile("bar.sync 1, 128;" ::: "memory");
         }
       }
     }
@@ -589,6 +839,58 @@ int launch_bn(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_
   return CARC_OK;
 }
 
+// shared memory of the grouped GEMM: NST pipeline stages, the barriers and
+// the epilogue's offset tables (the staged block reuses the A stages)
+template <int BN, int NST>
+constexpr int grouped_smem_bytes() {
+  return 1024 + NST * (A_STAGE_BYTES + BN * BK * 2) + 256 + (256 + 32) * 8;
+}
+
+template <int BN, int NST>
+int launch_grouped_bn(const CUtensorMap& ma, const CUtensorMap& mb, int mt, int nt, float* planes, int64_t ld,
+                      int64_t plane_stride, int* err, int bn, const GemmGroup& grp, const GroupEpi& epi,
+                      cudaStream_t stream) {
+  constexpr int SMEM = grouped_smem_bytes<BN, NST>();
+  static_assert(SMEM <= 227 * 1024, "grouped GEMM shared memory");
+  static_assert(NST * A_STAGE_BYTES >= 128 * 33 * 4, "the staged epilogue block fits in the A stages");
+  static std::once_flag once;
+  static cudaError_t attr_err = cudaSuccess;
+  std::call_once(once, [] {
+    attr_err = cudaFuncSetAttribute(gemm_bf16_tn_grouped_kernel<BN, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    SMEM);
+  });
+  if (attr_err != cudaSuccess) return fail(CARC_CUDA_ERROR, "grouped tensor core GEMM: %s", cudaGetErrorString(attr_err));
+  const dim3 grid(mt, nt, grp.n_out * grp.ks);
+  gemm_bf16_tn_grouped_kernel<BN, NST><<<grid, THREADS, SMEM, stream>>>(ma, mb, planes, ld, plane_stride, err, bn, grp,
+                                                                         epi);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
+}
+
+// two pipeline stages (two CTAs per SM) when every output's chain of K
+// blocks is short, so the epilogue of one CTA overlaps the other's work
+template <int BN>
+int launch_grouped_st(bool short_k, const CUtensorMap& ma, const CUtensorMap& mb, int mt, int nt, float* planes,
+                      int64_t ld, int64_t plane_stride, int* err, int bn, const GemmGroup& grp, const GroupEpi& epi,
+                      cudaStream_t stream) {
+  if (short_k) return launch_grouped_bn<BN, 2>(ma, mb, mt, nt, planes, ld, plane_stride, err, bn, grp, epi, stream);
+  return launch_grouped_bn<BN, 4>(ma, mb, mt, nt, planes, ld, plane_stride, err, bn, grp, epi, stream);
+}
+
+int launch_grouped(int bn, bool short_k, const CUtensorMap& ma, const CUtensorMap& mb, int mt, int nt, float* planes,
+                   int64_t ld, int64_t plane_stride, int* err, const GemmGroup& grp, const GroupEpi& epi,
+                   cudaStream_t stream) {
+  switch (bn) {
+    case 128: return launch_grouped_st<128>(short_k, ma, mb, mt, nt, planes, ld, plane_stride, err, bn, grp, epi, stream);
+    case 64: return launch_grouped_st<64>(short_k, ma, mb, mt, nt, planes, ld, plane_stride, err, bn, grp, epi, stream);
+    case 32: return launch_grouped_st<32>(short_k, ma, mb, mt, nt, planes, ld, plane_stride, err, bn, grp, epi, stream);
+    case 16: return launch_grouped_st<16>(short_k, ma, mb, mt, nt, planes, ld, plane_stride, err, bn, grp, epi, stream);
+    default:
+      if (bn % 16 != 0 || bn < 16 || bn > 256) return fail(CARC_BAD_ARG, "grouped tensor core GEMM: N tile %d", bn);
+      return launch_grouped_st<256>(short_k, ma, mb, mt, nt, planes, ld, plane_stride, err, bn, grp, epi, stream);
+  }
+}
+
 int launch_any(int bn, const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int a_rows, float* out,
                int64_t ld_out, int64_t split_stride, int ksplit, int kb_per, int kb_total, int* err,
                cudaStream_t stream, int b_blk) {
@@ -733,8 +1035,8 @@ __device__ __forceinline__ void split_bf16(double v, __nv_bfloat16& hi, __nv_bfl
 }
 
 // A role: out row (m, c, s) (4 per complex row), column (h, k, c') for h in {0,1}
-__global__ void pack_a_kernel(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
-                              const __grid_constant__ PackParams p) {
+__device__ __forceinline__ void pack_a_body(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
+                                            const PackParams& p) {
   const int64_t total = p.rows_out / 4 * p.Kc;  // one thread per (m, k) complex element, padded rows included
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t m = t / p.Kc, k = t % p.Kc;
@@ -763,9 +1065,14 @@ __global__ void pack_a_kernel(const double2* __restrict__ X, __nv_bfloat16* __re
   }
 }
 
-// B role: out row n, column (h, k, c'): part h of [b_r, b_i]
-__global__ void pack_b_kernel(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
+__global__ void pack_a_kernel(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
                               const __grid_constant__ PackParams p) {
+  pack_a_body(X, out, p);
+}
+
+// B role: out row n, column (h, k, c'): part h of [b_r, b_i]
+__device__ __forceinline__ void pack_b_body(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
+                                            const PackParams& p) {
   const int64_t total = p.rows_out * p.Kc;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t n = t / p.Kc, k = t % p.Kc;
@@ -783,6 +1090,26 @@ __global__ void pack_b_kernel(const double2* __restrict__ X, __nv_bfloat16* __re
     row[2 * p.Kc + 2 * k] = lr;
     row[2 * p.Kc + 2 * k + 1] = li_;
   }
+}
+
+__global__ void pack_b_kernel(const double2* __restrict__ X, __nv_bfloat16* __restrict__ out,
+                              const __grid_constant__ PackParams p) {
+  pack_b_body(X, out, p);
+}
+
+// Grouped packing: operand blockIdx.y of the table into block blockIdx.y of
+// the stacked output (block_elems bf16 each).
+struct PtrTable {
+  const double2* p[CARC_MAX_SLOTS];
+};
+
+__global__ void pack_grouped_kernel(const __grid_constant__ PtrTable src, __nv_bfloat16* __restrict__ out,
+                                    int64_t block_elems, int role, const __grid_constant__ PackParams p) {
+  __nv_bfloat16* o = out + (int64_t)blockIdx.y * block_elems;
+  if (role == 0)
+    pack_a_body(src.p[blockIdx.y], o, p);
+  else
+    pack_b_body(src.p[blockIdx.y], o, p);
 }
 
 // zero columns [c0, c1) of every row (row pitch kp)
@@ -833,9 +1160,8 @@ constexpr int RP_WARPS = 8;
 // Row-major planes P[z][r][n] (r = 4m + 2c + s): a block covers 32 columns of
 // one complex row m, its 8 warps take planes z = w, w+8, ...; the warps'
 // compensated partial sums are added in FP64 in warp order.
-__global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const float* __restrict__ P,
-                                                                       double2* __restrict__ C,
-                                                                       const __grid_constant__ ReduceParams p) {
+__device__ __forceinline__ void reduce_planes_body(const float* __restrict__ P, double2* __restrict__ C,
+                                                   const ReduceParams& p, int ksplit) {
   __shared__ double2 part[RP_WARPS][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int64_t m = blockIdx.y;
@@ -844,14 +1170,14 @@ __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const floa
   if (n < p.Nc) {
     // four planes (16 loads) in flight per thread before they are summed (in plane order)
     const float* base = P + (4 * m) * p.ld + n;
-    for (int z0 = w; z0 < p.ksplit; z0 += 4 * RP_WARPS) {
+    for (int z0 = w; z0 < ksplit; z0 += 4 * RP_WARPS) {
       float v[4][4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         const int z = z0 + u * RP_WARPS;
         const float* b = base + z * p.split_stride;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) v[u][q] = z < p.ksplit ? __ldcg(b + q * p.ld) : 0.f;
+        for (int q = 0; q < 4; ++q) v[u][q] = z < ksplit ? __ldcg(b + q * p.ld) : 0.f;
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
@@ -872,6 +1198,26 @@ __global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const floa
     if (p.accumulate) v = cadd(v, C[off]);
     C[off] = v;
   }
+}
+
+__global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_kernel(const float* __restrict__ P,
+                                                                       double2* __restrict__ C,
+                                                                       const __grid_constant__ ReduceParams p) {
+  reduce_planes_body(P, C, p, p.ksplit);
+}
+
+// Grouped reduction: output blockIdx.z sums planes [first, first + count)
+// (its entries' split planes, in entry order) into its own C.
+struct GroupOut {
+  int first[CARC_MAX_SLOTS], count[CARC_MAX_SLOTS];
+  double2* dst[CARC_MAX_SLOTS];
+};
+
+__global__ __launch_bounds__(32 * RP_WARPS) void reduce_planes_grouped_kernel(const float* __restrict__ P,
+                                                                               const __grid_constant__ ReduceParams p,
+                                                                               const __grid_constant__ GroupOut go) {
+  const int c = blockIdx.z;
+  reduce_planes_body(P + (int64_t)go.first[c] * p.split_stride, go.dst[c], p, go.count[c]);
 }
 
 // Column-major planes P[z][n][r] (r = 4m + 2c + s over `rows` rows): a block
@@ -1117,6 +1463,179 @@ int zgemm_tc(const ZView& a, const ZView& b, const ZOut& c, double2 alpha, int a
   const int64_t ld = rows_b;
   CARC_RETURN_IF(gemm_bf16_tn(A_op, (int)rows_a, B_op, (int)rows_b, (int)kp, P, ld, ks, err, stream));
   return reduce_partials(P, ld, (int64_t)rows_a * ld, ks, c, alpha, accumulate, stream);
+}
+
+// ---------------------------------------------------------------------------
+// C[c] = alpha sum over entries (i, j, c) of A[i] B[j]^T (+ C[c]), all entries
+// of one shape in four launches: the distinct A and B operands packed once
+// each into stacked buffers, one grouped GEMM over (entry, tile, split), one
+// grouped reduction per referenced output (entries summed in table order).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct GroupedGeo {
+  int64_t rows_a, rows_b, kp, ld;
+  int bn, ks, mt, nt;
+};
+
+GroupedGeo grouped_geo(const ZView& a, const ZView& b, int n_out) {
+  GroupedGeo g;
+  const int64_t M = zview_rows(a), N = zview_rows(b), Kc = zview_k(a);
+  g.rows_a = round_up(4 * M, BM);
+  g.rows_b = round_up(N, 16);
+  g.kp = round_up(4 * Kc, BK);
+  g.ld = g.rows_b;
+  g.bn = gemm_tile_n((int)g.rows_b);
+  g.mt = (int)(g.rows_a / BM);
+  g.nt = (int)(g.rows_b / g.bn);
+  // K splits only when the outputs' tiles do not fill the 152 SMs
+  const int64_t tiles = (int64_t)std::max(1, n_out) * g.mt * g.nt;
+  const int want = tiles >= 152 ? 1 : (int)((152 + tiles - 1) / tiles);
+  g.ks = gemm_effective_ksplit((int)g.kp, std::max(1, std::min(want, 65535 / std::max(1, n_out))));
+  return g;
+}
+
+int64_t al256(int64_t x) { return (x + 255) / 256 * 256; }
+
+int64_t grouped_plane_bytes(const GroupedGeo& g, int n_out) {
+  return g.ks > 1 ? (int64_t)n_out * g.ks * g.rows_a * g.ld * 4 : 0;
+}
+
+}  // namespace
+
+int64_t zgemm_tc_grouped_workspace(const ZView& a, const ZView& b, int n_a, int n_b, int n_e) {
+  const GroupedGeo g = grouped_geo(a, b, 1);
+  int64_t planes = 0;
+  for (int n = 1; n <= std::min(n_e, CARC_MAX_SLOTS); ++n) planes = std::max(planes, grouped_plane_bytes(grouped_geo(a, b, n), n));
+  return al256((int64_t)n_a * g.rows_a * g.kp * 2) + al256((int64_t)n_b * g.rows_b * g.kp * 2) + al256(planes) + 256;
+}
+
+int zgemm_tc_grouped(const ZView& a, const ZView& b, const ZOut& c, const void* const* a_ptrs, int n_a,
+                     const void* const* b_ptrs, int n_b, void* const* c_ptrs, int n_c, const int32_t* entries,
+                     int n_e, double2 alpha, int accumulate, void* ws, int64_t ws_bytes, int* err,
+                     cudaStream_t stream) {
+  const int64_t M = zview_rows(a), Kc = zview_k(a);
+  if (zview_k(b) != Kc) return fail(CARC_BAD_SHAPE, "grouped tensor core GEMM: K mismatch");
+  if (n_a < 1 || n_b < 1 || n_c < 1 || n_e < 1 || n_a > CARC_MAX_SLOTS || n_b > CARC_MAX_SLOTS ||
+      n_c > CARC_MAX_SLOTS || n_e > CARC_MAX_ENTRIES)
+    return fail(CARC_BAD_ARG, "grouped tensor core GEMM: %d A, %d B, %d C, %d entries (at most %d operands, %d entries)",
+                n_a, n_b, n_c, n_e, CARC_MAX_SLOTS, CARC_MAX_ENTRIES);
+  for (int e = 0; e < n_e; ++e) {
+    const int i = entries[3 * e], j = entries[3 * e + 1], k = entries[3 * e + 2];
+    if (i < 0 || i >= n_a || j < 0 || j >= n_b || k < 0 || k >= n_c || !a_ptrs[i] || !b_ptrs[j] || !c_ptrs[k])
+      return fail(CARC_BAD_ARG, "grouped tensor core GEMM: entry %d (%d, %d, %d) out of range", e, i, j, k);
+  }
+  // entries ordered by output (stable: table order within an output)
+  std::vector<int> order(n_e);
+  for (int e = 0; e < n_e; ++e) order[e] = e;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return entries[3 * x + 2] < entries[3 * y + 2]; });
+  GemmGroup grp;
+  std::memset(&grp, 0, sizeof(grp));
+  GroupEpi epi;
+  std::memset(&epi, 0, sizeof(epi));
+  int n_out = 0;
+  for (int q = 0; q < n_e; ++q) {
+    const int e = order[q], k = entries[3 * e + 2];
+    grp.ij[q] = make_int2(entries[3 * e], entries[3 * e + 1]);
+    if (q == 0 || entries[3 * order[q - 1] + 2] != k) {
+      grp.e_first[n_out] = q;
+      epi.dst[n_out] = static_cast<double2*>(c_ptrs[k]);
+      ++n_out;
+    }
+  }
+  grp.e_first[n_out] = n_e;
+  const GroupedGeo g = grouped_geo(a, b, n_out);
+  if ((int64_t)n_a * g.rows_a > (1ll << 30) || (int64_t)n_b * g.rows_b > (1ll << 30) || g.kp > (1ll << 30))
+    return fail(CARC_TOO_LARGE, "grouped tensor core GEMM: too large");
+  if (g.ks > 1 && M > 65535) return fail(CARC_TOO_LARGE, "grouped tensor core GEMM: %lld output rows", (long long)M);
+  if (ws_bytes < zgemm_tc_grouped_workspace(a, b, n_a, n_b, n_e))
+    return fail(CARC_BAD_ARG, "grouped tensor core GEMM: workspace too small");
+  grp.n_out = n_out;
+  grp.ks = g.ks;
+  grp.a_rows_per = (int)g.rows_a;
+  grp.b_rows_per = (int)g.rows_b;
+  grp.kb_total = (int)(g.kp / BK);
+  grp.kb_per = (grp.kb_total + g.ks - 1) / g.ks;
+  epi.nm = c.nm;
+  epi.nn = c.nn;
+  epi.Mc = 1;
+  epi.Nc = 1;
+  for (int i = 0; i < c.nm; ++i) {
+    epi.m_ext[i] = c.m_ext[i];
+    epi.m_str[i] = c.m_str[i];
+    epi.Mc *= c.m_ext[i];
+  }
+  for (int i = 0; i < c.nn; ++i) {
+    epi.n_ext[i] = c.n_ext[i];
+    epi.n_str[i] = c.n_str[i];
+    epi.Nc *= c.n_ext[i];
+  }
+  epi.alpha = alpha;
+  epi.alpha_one = alpha.x == 1.0 && alpha.y == 0.0;
+  epi.accumulate = accumulate;
+  char* p = static_cast<char*>(ws);
+  auto* A_all = reinterpret_cast<__nv_bfloat16*>(p);
+  auto* B_all = reinterpret_cast<__nv_bfloat16*>(p + al256((int64_t)n_a * g.rows_a * g.kp * 2));
+  float* P = reinterpret_cast<float*>(p + al256((int64_t)n_a * g.rows_a * g.kp * 2) +
+                                      al256((int64_t)n_b * g.rows_b * g.kp * 2));
+  // pack every distinct operand once
+  PtrTable ta, tb;
+  std::memset(&ta, 0, sizeof(ta));
+  std::memset(&tb, 0, sizeof(tb));
+  for (int i = 0; i < n_a; ++i) ta.p[i] = static_cast<const double2*>(a_ptrs[i]);
+  for (int j = 0; j < n_b; ++j) tb.p[j] = static_cast<const double2*>(b_ptrs[j]);
+  const PackParams pa = pack_params(a, g.rows_a, g.kp, 0), pb = pack_params(b, g.rows_b, g.kp, 0);
+  pack_grouped_kernel<<<dim3(grid_of(g.rows_a / 4 * Kc), n_a), 256, 0, stream>>>(ta, A_all, g.rows_a * g.kp, 0, pa);
+  CARC_CHECK_LAUNCH();
+  pack_grouped_kernel<<<dim3(grid_of(g.rows_b * Kc), n_b), 256, 0, stream>>>(tb, B_all, g.rows_b * g.kp, 1, pb);
+  CARC_CHECK_LAUNCH();
+  if (g.kp > 4 * Kc) {
+    pack_pad_kernel<<<grid_of((int64_t)n_a * g.rows_a * (g.kp - 4 * Kc)), 256, 0, stream>>>(
+        A_all, (int64_t)n_a * g.rows_a, 4 * Kc, g.kp, g.kp);
+    CARC_CHECK_LAUNCH();
+    pack_pad_kernel<<<grid_of((int64_t)n_b * g.rows_b * (g.kp - 4 * Kc)), 256, 0, stream>>>(
+        B_all, (int64_t)n_b * g.rows_b, 4 * Kc, g.kp, g.kp);
+    CARC_CHECK_LAUNCH();
+  }
+  // one grouped GEMM (its epilogue writes the outputs when there is one split)
+  CUtensorMap ma, mb;
+  CARC_RETURN_IF(make_map(&ma, A_all, (uint64_t)g.kp, (uint64_t)(n_a * g.rows_a), BM));
+  CARC_RETURN_IF(make_map(&mb, B_all, (uint64_t)g.kp, (uint64_t)(n_b * g.rows_b), (uint32_t)g.bn));
+  const int64_t plane_stride = g.rows_a * g.ld;
+  int max_chain = 0;  // longest chain of K blocks of one output (entries x split K blocks)
+  for (int q = 0; q < n_out; ++q) max_chain = std::max(max_chain, (grp.e_first[q + 1] - grp.e_first[q]) * grp.kb_per);
+  CARC_RETURN_IF(launch_grouped(g.bn, max_chain <= 4, ma, mb, g.mt, g.nt, P, g.ld, plane_stride, err, grp, epi,
+                                stream));
+  if (g.ks == 1) return CARC_OK;
+  // several splits: one grouped reduction of each output's planes
+  ReduceParams rp;
+  std::memset(&rp, 0, sizeof(rp));
+  rp.nm = epi.nm;
+  rp.nn = epi.nn;
+  for (int i = 0; i < CARC_MAX_SUBDIMS; ++i) {
+    rp.m_ext[i] = epi.m_ext[i];
+    rp.m_str[i] = epi.m_str[i];
+    rp.n_ext[i] = epi.n_ext[i];
+    rp.n_str[i] = epi.n_str[i];
+  }
+  rp.Mc = epi.Mc;
+  rp.Nc = epi.Nc;
+  rp.ld = g.ld;
+  rp.split_stride = plane_stride;
+  rp.accumulate = accumulate;
+  rp.alpha = alpha;
+  GroupOut go;
+  std::memset(&go, 0, sizeof(go));
+  for (int q = 0; q < n_out; ++q) {
+    go.first[q] = q * g.ks;
+    go.count[q] = g.ks;
+    go.dst[q] = epi.dst[q];
+  }
+  dim3 grid((unsigned)((rp.Nc + 31) / 32), (unsigned)rp.Mc, (unsigned)n_out);
+  reduce_planes_grouped_kernel<<<grid, 32 * RP_WARPS, 0, stream>>>(P, rp, go);
+  CARC_CHECK_LAUNCH();
+  return CARC_OK;
 }
 
 ZView zview_a(const carc_contract_desc& d, const void* base) {

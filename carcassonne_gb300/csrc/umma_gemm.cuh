@@ -69,6 +69,15 @@ int64_t round_up(int64_t a, int64_t b);
 int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, int64_t ld_out, int ksplit, int* err,
                  cudaStream_t stream, int m_live = 0, int b_blocked = 0);
 int gemm_effective_ksplit(int K, int ksplit);
+// C[c] (+)= alpha sum over entries (i, j, c) of A[i] B[j]^T for operands of one
+// shape (a, b, c give the geometry; their bases are ignored): the distinct
+// operands packed once each, one grouped GEMM launch over (entry, tile,
+// split), one grouped reduction; entries (HOST int32 [n_e][3]).
+int64_t zgemm_tc_grouped_workspace(const ZView& a, const ZView& b, int n_a, int n_b, int n_e);
+int zgemm_tc_grouped(const ZView& a, const ZView& b, const ZOut& c, const void* const* a_ptrs, int n_a,
+                     const void* const* b_ptrs, int n_b, void* const* c_ptrs, int n_c, const int32_t* entries,
+                     int n_e, double2 alpha, int accumulate, void* ws, int64_t ws_bytes, int* err,
+                     cudaStream_t stream);
 // N tile of gemm_bf16_tn: N in ceil(N / 256) equal tiles when those are
 // multiples of 16 (each N tile streams the whole A operand once), else the
 // largest of 256/128/64/32/16 dividing N.

@@ -182,20 +182,30 @@ def _launch(desc, a_list, b_list, out_list, entries, alpha=1.0, accumulate=False
               current_stream_handle())
 
 
-def contract_grouped_tc(spec, a_list, b_list, out_list, entries, conj_a=False, conj_b=False, accumulate=False):
+def contract_grouped_tc(spec, a_list, b_list, out_list, entries, conj_a=False, conj_b=False, accumulate=False,
+                        grouped=True):
     """``out[c] (+)= sum_{(i,j,c) in entries} A[i] . B[j]`` with every pair on
-    the tensor cores (``carc_zcontract_tc``: operands split into BF16 hi + lo,
-    FP32 accumulation, FP64 reduction; ~1e-5 relative to the result's scale).
-    Same spec and layout rules as ``contract_grouped``.  Returns the device
-    int32 status words, one per entry (each call clears its own word and sets
-    it on a pipeline timeout); the caller checks them."""
+    the tensor cores (operands split into BF16 hi + lo, FP32 accumulation,
+    FP64 reduction; ~1e-5 relative to the result's scale).  Same spec and
+    layout rules as ``contract_grouped``.  The whole table is one grouped call
+    (``carc_zcontract_tc_grouped``: each distinct operand packed once, one
+    grouped GEMM over (entry, tile, split), one grouped reduction) when it
+    fits the library's table limits (and ``grouped``), else one
+    ``carc_zcontract_tc`` per entry.  Returns the device int32 status words (one per call; each call
+    clears its own word and sets it on a pipeline timeout); the caller checks
+    them."""
     sp = spec if isinstance(spec, Spec) else Spec(spec)
     a0, b0, c0 = a_list[0], b_list[0], out_list[0]
     a_ls = _tensor_letter_strides(sp.a, a0)
     b_ls = _tensor_letter_strides(sp.b, b0)
     ext = _extents(sp, a_ls, b_ls)
-    if not c0.is_contiguous():
-        raise ValueError("output must be contiguous")
+    for t in out_list:
+        if not t.is_contiguous() or tuple(t.shape) != tuple(c0.shape):
+            raise ValueError("outputs must be contiguous and of one shape")
+    for lst, t0 in ((a_list, a0), (b_list, b0)):
+        for t in lst:
+            if tuple(t.shape) != tuple(t0.shape) or t.stride() != t0.stride():
+                raise ValueError("grouped operands must share shape and strides")
     c_str = out_letter_strides(sp.out, ext)
     desc = build_desc(sp, ext, {c: s for c, (e, s) in a_ls.items()}, {c: s for c, (e, s) in b_ls.items()}, c_str,
                       conj_a, conj_b)
@@ -203,6 +213,22 @@ def contract_grouped_tc(spec, a_list, b_list, out_list, entries, conj_a=False, c
         raise ValueError("contraction %r needs more than %d sub-dimensions per group" %
                          (sp.a + "," + sp.b + "->" + sp.out, _lib.MAX_SUBDIMS))
     lib = _lib.load()
+    if (grouped and entries and len(a_list) <= _lib.MAX_SLOTS and len(b_list) <= _lib.MAX_SLOTS
+            and len(out_list) <= _lib.MAX_SLOTS and len(entries) <= _lib.MAX_ENTRIES):
+        ws_bytes = lib.carc_zcontract_tc_grouped_workspace_size(ctypes.byref(desc), len(a_list), len(b_list),
+                                                                 len(entries))
+        if ws_bytes < 0:
+            _lib.check(_lib.CARC_BAD_ARG)
+        ws = Workspace.get(ws_bytes, c0.device)
+        status = torch.zeros(1, dtype=torch.int32, device=c0.device)
+        pa, _ka = _lib.ptr_array([t.data_ptr() for t in a_list])
+        pb, _kb = _lib.ptr_array([t.data_ptr() for t in b_list])
+        pc, _kc = _lib.ptr_array([t.data_ptr() for t in out_list])
+        pe, _ke = _lib.i32_array([int(x) for e in entries for x in e])
+        _lib.call("carc_zcontract_tc_grouped", ctypes.byref(desc), pa, len(a_list), pb, len(b_list), pc,
+                  len(out_list), pe, len(entries), 1.0, 0.0, int(bool(accumulate)), ctypes.c_void_p(ws.data_ptr()),
+                  ws_bytes, ctypes.c_void_p(status.data_ptr()), current_stream_handle())
+        return status
     ws_bytes = lib.carc_zcontract_tc_workspace_size(ctypes.byref(desc), 0)
     if ws_bytes < 0:
         _lib.check(_lib.CARC_BAD_ARG)

@@ -183,9 +183,11 @@ def absorb_main(argv=None):
     contractTowards(step % 4) (system/_2d.py:435-454) with the tag pairs in
     FP64 or on the tensor cores, then compressCornerStateTowards for every
     corner axis above ``--new-dim``.  Prints one JSON line per step with the
-    absorption's wall time (device synchronised on both sides); the last
-    step's absorption runs inside an NVTX range named "absorb", so a
-    profiler can select its kernels (``ncu --nvtx --nvtx-include absorb/``)."""
+    absorption's and the compressions' wall times (device synchronised on
+    both sides); the last
+    step's absorption runs inside an NVTX range named "absorb" and its
+    compressions inside one named "compress", so a profiler can select their
+    kernels (``ncu --nvtx --nvtx-include absorb/``)."""
     import argparse
     import json
     import time
@@ -217,13 +219,21 @@ def absorb_main(argv=None):
             if last:
                 torch.cuda.nvtx.range_pop()
         side = system.sides[step % 4][Identity()]
+        t0 = time.perf_counter()
+        if last:
+            torch.cuda.nvtx.range_push("compress")
         for corner in range(4):
             for cdir, axis in ((0, 0), (1, 3)):
                 if system.corners[corner][Identity()].shape[axis] > a.new_dim:
                     np.random.seed(1000 * step + 10 * corner + cdir)
                     system.compressCornerStateTowards(corner, cdir, a.new_dim)
+        torch.cuda.synchronize()
+        compress_s = time.perf_counter() - t0
+        if last:
+            torch.cuda.nvtx.range_pop()
         print(json.dumps(dict(step=step, precision=a.precision, absorb_s=round(seconds, 6),
-                              side_shape=list(side.shape), side_tags=len(system.sides[step % 4]))), flush=True)
+                              compress_s=round(compress_s, 6), side_shape=list(side.shape),
+                              side_tags=len(system.sides[step % 4]))), flush=True)
 
 
 if __name__ == "__main__":

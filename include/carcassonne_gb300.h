@@ -163,6 +163,25 @@ int carc_zcontract_tc(const carc_contract_desc* desc, const void* A, const void*
                       double alpha_re, double alpha_im, int32_t accumulate, int32_t ksplit,
                       void* workspace, int64_t workspace_bytes, void* status, void* stream);
 int64_t carc_zcontract_tc_workspace_size(const carc_contract_desc* desc, int32_t ksplit);
+/*
+ * The grouped form of carc_zcontract_tc, with the arguments of
+ * carc_zcontract_grouped: C[c] = alpha * sum over entries (i, j, c), in table
+ * order, of A[i] . B[j] (+ the old C[c] when accumulate != 0), every pair of
+ * one shape on the tensor cores in four launches for the whole table (each
+ * distinct operand packed once into a stacked split-BF16 buffer, one grouped
+ * GEMM over (entry, tile, split) work items, one grouped reduction).  HOST
+ * pointer and entry arrays; at most CARC_MAX_SLOTS operands of each role and
+ * CARC_MAX_ENTRIES entries.  *status (device int32) = CARC_NOT_CONVERGED if a
+ * pipeline wait timed out.  Replaces the tag-pair loop of
+ * contractSparseTensors (sparse.py:223-240) in the absorptions.
+ */
+int carc_zcontract_tc_grouped(const carc_contract_desc* desc, const void* const* a_ptrs, int32_t n_a,
+                              const void* const* b_ptrs, int32_t n_b, void* const* c_ptrs, int32_t n_c,
+                              const int32_t* entries, int32_t n_entries, double alpha_re, double alpha_im,
+                              int32_t accumulate, void* workspace, int64_t workspace_bytes, void* status,
+                              void* stream);
+int64_t carc_zcontract_tc_grouped_workspace_size(const carc_contract_desc* desc, int32_t n_a, int32_t n_b,
+                                                 int32_t n_entries);
 /* The raw tensor-core GEMM: out[z][m][n] = sum over K-split z of A[m,:].B[n,:]
  * (BF16, K-major, M % 128 == 0, K % 64 == 0, N % 16 == 0, FP32 out with row
  * pitch ld_out, ksplit partial planes of M*ld_out floats). */

@@ -27,7 +27,8 @@ solve to 1e-8 relative of the reference's energy), absorbs the same center
 (contractTowards, system/_2d.py:435-439) and applies the reference's
 compressor (compressCornerStateTowards, system/_2d.py:191-228); the GPU's own
 compressor is run on the same inputs from the same random start and must fit
-the boundary product at least as well as the reference's.
+the boundary product at least as well as the reference's, in FP64 and with
+its big contractions on the tensor cores.
 """
 import os
 
@@ -167,8 +168,11 @@ def test_growth_run_replay(gold, name, solver, tol, monkeypatch):
         assert P.shape == (nd, Ld.shape[1])
         np.random.seed(cseed)
         ours = compression.computeProductCompressor(Ld, Rd, nd).toArray()
+        np.random.seed(cseed)
+        with compression.compression_precision("tc"):
+            ours_tc = compression.computeProductCompressor(Ld, Rd, nd).toArray()
         Lt, Rt = Ld.toArray(), Rd.toArray()
-        fits.append((_fit_residual(Lt, Rt, ours), _fit_residual(Lt, Rt, P)))
+        fits.append((_fit_residual(Lt, Rt, ours), _fit_residual(Lt, Rt, P), _fit_residual(Lt, Rt, ours_tc)))
         return TorchData(P)
 
     monkeypatch.setattr(sys2d, "computeProductCompressor", replay_compressor)
@@ -197,7 +201,10 @@ def test_growth_run_replay(gold, name, solver, tol, monkeypatch):
     assert not queue
     # the GPU's compressor fits each boundary product at least as well as the
     # reference's (both start from the same random isometry; the reference
-    # solves the normal equations by GMRES to 1e-5, the GPU by CG to 1e-12)
-    for ours, ref in fits:
+    # solves the normal equations by GMRES to 1e-5, the GPU by CG to 1e-12),
+    # also with the normal equations' big contractions on the tensor cores
+    # (split-BF16, ~1e-5 relative: the size of the reference's GMRES tolerance)
+    for ours, ref, ours_tc in fits:
         assert ours <= ref * 1.05 + 1e-10, fits
+        assert ours_tc <= ref * 1.05 + 1e-8, fits
     print(name, solver, "worst relative energy error %.2e over %d steps, %d compressions" % (worst, steps, len(fits)))
