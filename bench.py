@@ -336,10 +336,19 @@ def growth_run(spec, cpu_steps=()):
                time_to_energy_mixed_s=tot("build_s") + tot("mixed_solve_s"),
                solve_plain_s=tot("plain_solve_s"), solve_mixed_s=tot("mixed_solve_s"),
                build_s=tot("build_s"), contract_s=tot("contract_s"), contract_tc_s=tot("contract_tc_s"),
-               compress_s=tot("compress_s"), compress_tc_s=tot("compress_tc_s"), max_rel_err_mixed=max(r["rel_err_mixed"] for r in steps),
+               compress_s=tot("compress_s"), compress_tc_s=tot("compress_tc_s"),
+               max_rel_err_mixed=max(r["rel_err_mixed"] for r in steps),
                max_contract_tc_rel_err=max(r["contract_tc_rel_err"] for r in steps))
     out["speedup_solve"] = out["solve_plain_s"] / out["solve_mixed_s"]
     out["speedup_time_to_energy"] = out["time_to_energy_plain_s"] / out["time_to_energy_mixed_s"]
+    # whole steps: build, solve, absorb and compress, all FP64 against the
+    # mixed solve with the tensor-core absorption and compression (the latter
+    # two timed on copies of the same environments; the run itself continues
+    # from the FP64 ones)
+    out["step_total_plain_s"] = out["build_s"] + out["solve_plain_s"] + out["contract_s"] + out["compress_s"]
+    out["step_total_mixed_tc_s"] = (out["build_s"] + out["solve_mixed_s"] + out["contract_tc_s"] +
+                                    out["compress_tc_s"])
+    out["speedup_step_total"] = out["step_total_plain_s"] / out["step_total_mixed_tc_s"]
     cpu = [r for r in steps if "cpu_reference_s" in r]
     if cpu:
         out["cpu_reference"] = dict(

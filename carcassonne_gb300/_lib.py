@@ -89,6 +89,8 @@ SIGNATURES = {
                                               _i64, _vp]),
     "carc_zminres_projected_workspace_size": (_i64, [_i32]),
     "carc_zcg_hpsd": (ctypes.c_int, [_i32, _vp, _vp, _vp, _dbl, _i32, _vp, _vp, _vp]),
+    "carc_zcg_hpsd_grid": (ctypes.c_int, [_i32, _vp, _vp, _vp, _dbl, _i32, _vp, _vp, _vp, _i64, _vp]),
+    "carc_zcg_hpsd_grid_workspace_size": (_i64, [_i32]),
     "carc_mlp_linear_forward": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _i32, _vp, _vp]),
     "carc_mlp_linear_backward": (ctypes.c_int, [_i32, _i32, _i32, _vp, _vp, _vp, _vp, _i32, _vp, _vp, _vp, _vp, _vp]),
     "carc_mlp_mse": (ctypes.c_int, [_i64, _i32, _vp, _vp, _vp, _vp, _vp]),

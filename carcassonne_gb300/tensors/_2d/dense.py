@@ -214,6 +214,44 @@ def center_pair(direction, state, op=None, state_conj=None):
     return engine.contract(ket_in + "," + bra_in + "->uvwxyzkl", s_in, sc, shape, conj_b=conj)
 
 
+def center_pairs(direction, state, ops, state_conj=None):
+    """``[center_pair(direction, state, op, state_conj) for op in ops]`` in two
+    grouped launches (every S . O, then every pair with conj(S)) instead of one
+    or two per operator; operators whose shape does not keep the center's
+    physical dimension take the single path."""
+    s = _t(state)
+    _check_rank(1, s, 5)
+    conj = state_conj is None
+    sc = s if conj else _t(state_conj)
+    ts = [None if op is None else _t(op) for op in ops]
+    for o in ts:
+        if o is not None:
+            _check_rank(3, o, 2)
+            if o.shape[1] != s.shape[4]:
+                raise DimensionMismatchError(3, 1, int(o.shape[1]), 1, 4, int(s.shape[4]))
+    real = [o for o in ts if o is not None]
+    if any(o.shape[0] != s.shape[4] for o in real) or len({(tuple(o.shape), o.stride()) for o in real}) > 1:
+        return [center_pair(direction, state, op, state_conj) for op in ops]
+    ket = _center_letters(direction, True)
+    bra = _center_letters(direction, False)
+    so = [torch.empty(tuple(s.shape), dtype=CDT, device=s.device) for _ in real]
+    if real:
+        engine.contract_grouped(ket + ",pq->" + ket[:4] + "p", [s], real, so, [(0, i, i) for i in range(len(real))])
+    a_list, entries, k = [s.contiguous()] + so, [], 0  # grouped operands share strides
+    for i, o in enumerate(ts):
+        if o is None:
+            entries.append((0, 0, i))
+        else:
+            k += 1
+            entries.append((k, 0, i))
+    ext = {c: int(s.shape[i]) for i, c in enumerate(ket[:4])}
+    ext.update({c: int(sc.shape[i]) for i, c in enumerate(bra[:4])})
+    shape = tuple(ext[c] for c in "uvwxyzkl")
+    outs = [torch.empty(shape, dtype=CDT, device=s.device) for _ in ts]
+    engine.contract_grouped(ket[:4] + "p," + bra[:4] + "p->uvwxyzkl", a_list, [sc], outs, entries, conj_b=conj)
+    return outs
+
+
 _SIDE_SPEC = engine.Spec("abcdefkl,uvwxyzkl->aubxcdveyfwz")
 
 
@@ -511,5 +549,5 @@ __all__ = [
     "absorbDenseCenterSOSIntoSide", "formDenseStage3", "formDenseStage3_formMatrix_and_cost",
     "formDenseStage3_multiply_and_cost", "formNormalizationMultiplier", "formNormalizationStage1",
     "formNormalizationStage2", "formNormalizationStage3", "formNormalizationSubmatrix", "Stage3Operator",
-    "center_pair", "absorption_precision", "check_absorption_status",
+    "center_pair", "center_pairs", "absorption_precision", "check_absorption_status",
 ]

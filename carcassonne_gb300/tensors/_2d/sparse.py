@@ -13,7 +13,7 @@ import itertools
 import numpy as np
 
 from .dense import (Stage3Operator, absorbDenseSideIntoCornerFromLeft, absorbDenseSideIntoCornerFromRight,
-                    center_pair, formNormalizationStage1, formNormalizationStage2, _absorb_pairs)
+                    center_pair, center_pairs, formNormalizationStage1, formNormalizationStage2, _absorb_pairs)
 from .dense import *  # noqa: F401,F403  (the dense contractors are reachable from this module too)
 from ...sparse import (Complete, Identity, OneSiteOperator, TwoSiteOperator, TwoSiteOperatorCompressed,
                        addStandardCompleteAndIdentityTerms, compileSparseSchedule, contractSparseTensors,
@@ -85,15 +85,15 @@ def absorbSparseCenterSOSIntoSide(direction, side, state_center_data, operator_c
     if not sched.entries:
         return {}
     e_slot = {}
-    e_list = []
+    e_ops = []
     table = []
     for i_side, i_op, slot, kind in sched.entries:
         key = None if kind == _SS else i_op
         if key not in e_slot:
-            e_slot[key] = len(e_list)
-            op = None if key is None else operator_center_data[op_tags[key]]
-            e_list.append(center_pair(direction, state_center_data, op, state_center_data_conj))
+            e_slot[key] = len(e_ops)
+            e_ops.append(None if key is None else operator_center_data[op_tags[key]])
         table.append((i_side, e_slot[key], slot))
+    e_list = center_pairs(direction, state_center_data, e_ops, state_center_data_conj)
     outs = _absorb_pairs(direction, [side[t] for t in side_tags], e_list, table, len(sched.result_tags))
     return dict(zip(sched.result_tags, outs))
 

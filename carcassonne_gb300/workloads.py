@@ -201,8 +201,11 @@ def absorb_main(argv=None):
     p.add_argument("--seed", type=int, default=2)
     p.add_argument("--steps", type=int, default=8)
     p.add_argument("--new-dim", type=int, default=8, help="kept dimension of each corner axis (chi = new_dim^2)")
-    p.add_argument("--precision", default="tc", choices=["tc", "fp64"])
+    p.add_argument("--precision", default="tc", choices=["tc", "fp64"], help="absorption precision")
+    p.add_argument("--compress-precision", default="fp64", choices=["tc", "fp64"],
+                   help="precision of the compressor's large contractions")
     a = p.parse_args(argv)
+    from .compression import compression_precision
     system = bond_start_system(a.kind, a.D, a.seed)
     for step in range(a.steps):
         x0 = system.state_center_data
@@ -222,16 +225,18 @@ def absorb_main(argv=None):
         t0 = time.perf_counter()
         if last:
             torch.cuda.nvtx.range_push("compress")
-        for corner in range(4):
-            for cdir, axis in ((0, 0), (1, 3)):
-                if system.corners[corner][Identity()].shape[axis] > a.new_dim:
-                    np.random.seed(1000 * step + 10 * corner + cdir)
-                    system.compressCornerStateTowards(corner, cdir, a.new_dim)
+        with compression_precision(a.compress_precision):
+            for corner in range(4):
+                for cdir, axis in ((0, 0), (1, 3)):
+                    if system.corners[corner][Identity()].shape[axis] > a.new_dim:
+                        np.random.seed(1000 * step + 10 * corner + cdir)
+                        system.compressCornerStateTowards(corner, cdir, a.new_dim)
         torch.cuda.synchronize()
         compress_s = time.perf_counter() - t0
         if last:
             torch.cuda.nvtx.range_pop()
-        print(json.dumps(dict(step=step, precision=a.precision, absorb_s=round(seconds, 6),
+        print(json.dumps(dict(step=step, precision=a.precision, compress_precision=a.compress_precision,
+                              absorb_s=round(seconds, 6),
                               compress_s=round(compress_s, 6), side_shape=list(side.shape),
                               side_tags=len(system.sides[step % 4]))), flush=True)
 
