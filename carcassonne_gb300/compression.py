@@ -15,8 +15,8 @@ which costs l (old op new)^2 + r (new^2 op)^2 + (old new)^2 (op new)^2
 complex MACs per round instead of the l r (old new)^2 of A^H A (at a
 boundary of l = 1024, r = 64, old = 32, new = 8: 7e7 instead of 4.3e9).
 The system (Hermitian positive semi-definite and consistent) is solved on
-the GPU by conjugate gradients to a relative residual of 1e-12 in a single
-thread block per round (``carc_zcg_hpsd``, no host round trip per
+the GPU by conjugate gradients to a relative residual of 1e-12 in one
+cooperative launch per round (``carc_zcg_hpsd_grid``, no host round trip per
 iteration); the four rounds' status words (CG and the polar factors'
 Jacobi SVDs) are read once at the end, and a solve that ends its budget above
 the reference's GMRES tolerance (1e-5) raises AssertionError where GMRES
@@ -83,6 +83,41 @@ def _ct(spec, a, b, out_shape, conj_a=False, conj_b=False, big=False):
     return engine.contract(spec, a, b, out_shape, conj_a=conj_a, conj_b=conj_b)
 
 
+def absorb_matrices(sparse, ax1, M1, ax2, M2):
+    """``{tag: d.absorbMatrixAt(ax1, M1).absorbMatrixAt(ax2, M2)}`` over a
+    sparse boundary (the compressor's application in
+    compressCornerStateTowards, system/_2d.py:191-228).  In the "tc" mode of
+    ``compression_precision`` every tag of one shape takes one grouped
+    tensor-core call per matrix (the tags are the B operands of M . d over
+    the axis); otherwise each tag its FP64 contractions."""
+    from .data import LETTERS
+    if _PRECISION["precision"] != "tc":
+        return {t: d.absorbMatrixAt(ax1, M1).absorbMatrixAt(ax2, M2) for t, d in sparse.items()}
+    classes = {}
+    for t, d in sparse.items():
+        classes.setdefault((tuple(d.shape), tuple(d._t.stride())), []).append(t)
+    out = {}
+    for (shape, _), tags in classes.items():
+        ts = [sparse[t]._t for t in tags]
+        for axis, M in ((ax1, M1), (ax2, M2)):
+            m = M._t if isinstance(M, TorchData) else torch.as_tensor(M)
+            n = len(ts[0].shape)
+            la = LETTERS[:n]
+            o = list(la)
+            o[axis] = "Z"
+            spec = "Z" + la[axis] + "," + la + "->" + "".join(o)
+            shp = list(ts[0].shape)
+            if m.shape[1] != shp[axis]:
+                raise ValueError("shape-mismatch for sum")
+            shp[axis] = m.shape[0]
+            outs = [torch.empty(shp, dtype=CDT, device=ts[0].device) for _ in ts]
+            _PRECISION["status"].append(engine.contract_grouped_tc(spec, [m.contiguous()], ts, outs,
+                                                                   [(0, i, i) for i in range(len(ts))]))
+            ts = outs
+        out.update({t: TorchData(x) for t, x in zip(tags, ts)})
+    return {t: out[t] for t in sparse}
+
+
 def _normal_equations(Lt, Rt, P, b2):
     """G = A^H A and c = A^H b of A[(l,r),(a,i)] = sum L[l,a,b,o] conj(P[b,j])
     conj(P[c,i]) P[e,j] R[c,e,o,r] (the reference's join list, compression.py:12-25),
@@ -91,8 +126,8 @@ def _normal_equations(Lt, Rt, P, b2):
     r = Rt.shape[3]
     new = P.shape[1]
     n = old * new
-    # the terms with the long boundary index l (t1, X, u, c) carry almost all
-    # of the work; the rest stay in FP64
+    # the terms with the long boundary index l (t1, X, u, c, and b2 above)
+    # carry almost all of the work; the rest stay in FP64
     t1 = _ct("labo,bj->laoj", Lt, P, (l, old, op, new), conj_b=True, big=True)
     t2 = _ct("ej,ceor->jcor", P, Rt, (new, old, op, r))
     t3 = _ct("ci,jcor->ijor", P, t2, (new, new, op, r), conj_a=True)
@@ -143,12 +178,20 @@ def _cg_host(G, c, tol=1e-12, max_iter=None):
 
 
 def _cg_device(G, c, status, residual, tol=1e-12, max_iter=None):
+    """CG on the device with no host round trip: over a cooperative grid
+    (``carc_zcg_hpsd_grid``: G p spread over the SMs, a few microseconds per
+    iteration) -- FP64 issues slowly on this part, and on one SM alone an
+    iteration costs n^2 complex multiply-adds at a sixty-fourth of the GPU's
+    FP64 rate."""
     n = c.numel()
-    max_iter = max_iter or max(10 * n, 500)  # one block iterates in microseconds: ill-conditioned systems need more
+    max_iter = max_iter or max(10 * n, 500)  # iterations are cheap: ill-conditioned systems need more
     x = torch.empty(n, dtype=CDT, device=c.device)
-    _lib.call("carc_zcg_hpsd", n, ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(c.data_ptr()),
+    ws_bytes = _lib.load().carc_zcg_hpsd_grid_workspace_size(n)
+    ws = engine.Workspace.get(ws_bytes, c.device)
+    _lib.call("carc_zcg_hpsd_grid", n, ctypes.c_void_p(G.data_ptr()), ctypes.c_void_p(c.data_ptr()),
               ctypes.c_void_p(x.data_ptr()), float(tol), int(max_iter), ctypes.c_void_p(status.data_ptr()),
-              ctypes.c_void_p(residual.data_ptr()), current_stream_handle())
+              ctypes.c_void_p(residual.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ws_bytes,
+              current_stream_handle())
     return x
 
 
@@ -163,7 +206,7 @@ def computeProductCompressor(L, R, new_dimension, rounds=4, initial=None):
     Lt = L._t.contiguous()
     Rt = R._t.contiguous()
     l, r = Lt.shape[0], Rt.shape[3]
-    b2 = engine.contract("labo,abor->lr", Lt, Rt, (l, r))
+    b2 = _ct("labo,abor->lr", Lt, Rt, (l, r), big=True)
     if initial is None:
         initial = TorchData.newRandom(old, new_dimension)  # numpy's global generator, as the reference
     svd_status = []
@@ -176,7 +219,10 @@ def computeProductCompressor(L, R, new_dimension, rounds=4, initial=None):
         residual = torch.zeros(rounds, dtype=torch.float64, device=Lt.device)
     for k in range(rounds):
         G, c = _normal_equations(Lt, Rt, P._t, b2)
-        x = _cg_device(G, c, status[k], residual[k]) if on_device else _cg_host(G, c)
+        # the split-precision normal equations are exact to ~1e-5: a residual
+        # of 1e-9 (four orders below the reference's GMRES tolerance) is enough
+        tol = 1e-9 if _PRECISION["precision"] == "tc" else 1e-12
+        x = _cg_device(G, c, status[k], residual[k], tol=tol) if on_device else _cg_host(G, c, tol=tol)
         P = linalg.unitize(TorchData(x.reshape(old, new_dimension)), deferred=svd_status)
     linalg.check_deferred(svd_status)
     if on_device:
@@ -190,4 +236,4 @@ def computeProductCompressor(L, R, new_dimension, rounds=4, initial=None):
     return P.transpose()
 
 
-__all__ = ["computeProductCompressor", "compression_precision"]
+__all__ = ["computeProductCompressor", "compression_precision", "absorb_matrices"]

@@ -26,7 +26,7 @@ from random import randint
 
 import numpy as np
 
-from ..compression import computeProductCompressor
+from ..compression import absorb_matrices, computeProductCompressor
 from ..data import TorchData
 from ..sparse import (Identity, OneSiteOperator, TwoSiteOperator, TwoSiteOperatorCompressed, makeSimpleSparseOperator,
                       makeSparseOperator, mapOverSparseData, stripAllButIdentityFrom)
@@ -198,10 +198,8 @@ class System(BaseSystem):
         corner = self.corners[corner_id][Identity()].join(0, 1, 2, (3, 4, 5))
         P = computeProductCompressor(side, corner, new_dimension)
         Pc = P.conj()
-        self.sides[L(corner_id)] = mapOverSparseData(lambda d: d.absorbMatrixAt(3, P).absorbMatrixAt(4, Pc),
-                                                     self.sides[L(corner_id)])
-        self.corners[corner_id] = mapOverSparseData(lambda d: d.absorbMatrixAt(0, Pc).absorbMatrixAt(1, P),
-                                                    self.corners[corner_id])
+        self.sides[L(corner_id)] = absorb_matrices(self.sides[L(corner_id)], 3, P, 4, Pc)
+        self.corners[corner_id] = absorb_matrices(self.corners[corner_id], 0, Pc, 1, P)
         return P
 
     def compressCornerStateTowardsRight(self, corner_id, new_dimension):
@@ -209,10 +207,8 @@ class System(BaseSystem):
         side = self.sides[corner_id][Identity()].join(0, 1, 2, (3, 4, 5, 6, 7))
         P = computeProductCompressor(corner, side, new_dimension)
         Pc = P.conj()
-        self.corners[corner_id] = mapOverSparseData(lambda d: d.absorbMatrixAt(3, P).absorbMatrixAt(4, Pc),
-                                                    self.corners[corner_id])
-        self.sides[corner_id] = mapOverSparseData(lambda d: d.absorbMatrixAt(0, Pc).absorbMatrixAt(1, P),
-                                                  self.sides[corner_id])
+        self.corners[corner_id] = absorb_matrices(self.corners[corner_id], 3, P, 4, Pc)
+        self.sides[corner_id] = absorb_matrices(self.sides[corner_id], 0, Pc, 1, P)
         return P
 
     def compressCornerTwoSiteOperatorTowards(self, corner_id, direction, new_dimension, normalize=False):

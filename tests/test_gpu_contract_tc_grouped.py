@@ -87,3 +87,25 @@ def test_grouped_tc_is_deterministic(engine):
         outs.append(C)
     for x, y in zip(*outs):
         assert torch.equal(x, y)
+
+
+def test_absorb_matrices_tc_matches_fp64(engine):
+    """The compressor's application to every tag of a boundary
+    (compression.absorb_matrices): one grouped tensor-core call per shape
+    class and matrix against the FP64 absorbMatrixAt chain, with tags of two
+    shapes (a compressed operator axis)."""
+    from carcassonne_gb300.compression import absorb_matrices, compression_precision
+    from carcassonne_gb300.data import TorchData
+    g = torch.Generator().manual_seed(8)
+    sparse = {"a": TorchData(_rand((6, 5, 1, 12, 12, 1, 3, 3), g)), "b": TorchData(_rand((6, 5, 1, 12, 12, 1, 3, 3), g)),
+              "c": TorchData(_rand((6, 5, 2, 12, 12, 1, 3, 3), g))}
+    P = TorchData(_rand((4, 12), g))
+    Pc = P.conj()
+    ref = absorb_matrices(sparse, 3, P, 4, Pc)
+    with compression_precision("tc"):
+        got = absorb_matrices(sparse, 3, P, 4, Pc)
+    assert list(got) == list(ref)
+    for t in ref:
+        r, o = ref[t]._t, got[t]._t
+        assert tuple(o.shape) == tuple(r.shape) == tuple(sparse[t].shape[:3]) + (4, 4) + tuple(sparse[t].shape[5:])
+        assert (o - r).abs().max().item() <= TC_TOL * r.abs().max().item()
