@@ -10,8 +10,11 @@ operator H_eff to a block of ``--nvec`` centers of shape (D,D,D,D,d).
 
 value: GFLOP/s of algorithmic work (the reference's CostTracker count of
 complex MACs x 8 real flops) with inputs resident in HBM, L2 flushed
-between timed steps; e2e: the same metric with the block copied from pinned
-host memory and the result copied back inside the timed region.
+between timed steps; e2e: the same metric with the block in pinned host
+memory and the result returned to pinned host memory inside the timed
+region -- the kernel reads and writes host memory mapped into the device's
+address space (NVLink-C2C); the figure with a copy each way
+(cudaMemcpyAsync) is reported beside it.
 ``--impl reference`` times the CPU restatement of the reference's path on
 the host cores (the reference itself is pure Python/NumPy and is not
 available on the GPU host) for ``--warmup`` untimed and ``--steps`` timed
@@ -759,12 +762,44 @@ def main():
         yh.copy_(y, non_blocking=True)
         e_ends[i].record()
     torch.cuda.synchronize()
-    e_ms = sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)) / args.steps
+    e_ms_copies = sum(s.elapsed_time(e) for s, e in zip(e_starts, e_ends)) / args.steps
+    e_ms = e_ms_copies
+    e2e_transfer = "cudaMemcpyAsync each way (pinned host block -> device, result -> pinned host)"
+    if args.mode == "tc":
+        # the block and the result in pinned host memory mapped into the device's
+        # address space: the kernel reads the block and writes the result over the
+        # host link (NVLink-C2C) inside the call, the same bytes each way per step
+        from carcassonne_gb300.hostmem import MappedHostBuffer
+        xm = MappedHostBuffer(tuple(x.shape))
+        ym = MappedHostBuffer(tuple(y.shape))
+        xm.host[...] = xs
+        for _ in range(2):
+            opr.apply_tc_ptr(xm.device_ptr, ym.device_ptr, nvec)
+        torch.cuda.synchronize()
+        opr.check_status()
+        mapped_ok = bool(np.array_equal(ym.host, y_chk.cpu().numpy()))
+        m_starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        m_ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        for i in range(args.steps):
+            flush_l2()
+            m_starts[i].record()
+            opr.apply_tc_ptr(xm.device_ptr, ym.device_ptr, nvec)
+            m_ends[i].record()
+        torch.cuda.synchronize()
+        opr.check_status()
+        if not mapped_ok:
+            raise RuntimeError("the mapped-host matvec differs from the device one")
+        e_ms = sum(s.elapsed_time(e) for s, e in zip(m_starts, m_ends)) / args.steps
+        e2e_transfer = ("pinned host memory mapped into the device's address space: the kernel reads the block "
+                        "and writes the result on the host over NVLink-C2C (result equal to the device path's)")
+        xm.close()
+        ym.close()
 
     from carcassonne_gb300.replicas import max_over_ranks
-    ms, e_ms = max_over_ranks([ms, e_ms], dist, device=x.device)
+    ms, e_ms, e_ms_copies = max_over_ranks([ms, e_ms, e_ms_copies], dist, device=x.device)
     value = world * flops_per_step / (ms * 1e-3) / 1e9
     e2e_value = world * flops_per_step / (e_ms * 1e-3) / 1e9
+    e2e_copies_value = world * flops_per_step / (e_ms_copies * 1e-3) / 1e9
     solves = batched_solves_section(args, dist, rank, world, x.device) if args.batched_solves else None
     if rank != 0:
         if dist:
@@ -839,7 +874,8 @@ def main():
         config=dict(WORKLOAD, nvec=nvec), mode=args.mode, l2="flushed between timed steps (512 MB write)",
         parallelism="replicas" if world > 1 else "single GPU",
         e2e=dict(value=e2e_value, unit=UNIT, h2d_bytes_per_step=int(xh.numel() * 16),
-                 d2h_bytes_per_step=int(yh.numel() * 16)),
+                 d2h_bytes_per_step=int(yh.numel() * 16), ms_per_step=e_ms, transfer=e2e_transfer,
+                 copies_value=e2e_copies_value, copies_ms_per_step=e_ms_copies),
         gpu_launches=int(launches_in_steps),
         roofline=roofline, phases=phases, solve=solve, batched=batched,
         cpu_baseline=None if cpu is None else dict(value=cpu["value"], unit=UNIT, cores=cpu["cores"],

@@ -50,6 +50,8 @@ SIGNATURES = {
     "carc_version": (ctypes.c_int, []),
     "carc_launch_counter": (_i64, []),
     "carc_phase_timing_enable": (_i32, [_i32]),
+    "carc_host_alloc_mapped": (ctypes.c_int, [_i64, ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    "carc_host_free": (ctypes.c_int, [_vp]),
     "carc_phase_timing_read": (_i32, [_i32, ctypes.POINTER(ctypes.c_double), _pi64]),
     "carc_zcontract_grouped": (ctypes.c_int, [ctypes.POINTER(ContractDesc), _pvp, _i32, _pvp, _i32, _pvp, _i32,
                                               _pi32, _i32, _dbl, _dbl, _i32, _vp, _i64, _vp]),

@@ -30,6 +30,29 @@ int carc_version(void) { return 100; }
 
 int64_t carc_launch_counter(void) { return (int64_t)launch_count(); }
 
+int carc_host_alloc_mapped(int64_t bytes, void** host_ptr, void** device_ptr) {
+  if (!host_ptr || !device_ptr || bytes <= 0) return fail(CARC_BAD_ARG, "carc_host_alloc_mapped: bad argument");
+  *host_ptr = nullptr;
+  *device_ptr = nullptr;
+  void* h = nullptr;
+  CARC_CHECK_CUDA(cudaHostAlloc(&h, (size_t)bytes, cudaHostAllocMapped | cudaHostAllocPortable));
+  void* d = nullptr;
+  const cudaError_t e = cudaHostGetDevicePointer(&d, h, 0);
+  if (e != cudaSuccess || !d) {
+    cudaFreeHost(h);
+    return fail(CARC_CUDA_ERROR, "carc_host_alloc_mapped: no device mapping (%s)", cudaGetErrorString(e));
+  }
+  *host_ptr = h;
+  *device_ptr = d;
+  return CARC_OK;
+}
+
+int carc_host_free(void* host_ptr) {
+  if (!host_ptr) return CARC_OK;
+  CARC_CHECK_CUDA(cudaFreeHost(host_ptr));
+  return CARC_OK;
+}
+
 int carc_phase_timing_enable(int32_t on) { return phase_timing_enable(on); }
 
 int carc_phase_timing_read(int32_t phase, double* total_ms, int64_t* count) {

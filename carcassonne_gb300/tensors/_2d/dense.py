@@ -403,14 +403,23 @@ class Stage3Operator:
 
     def apply_tc(self, x, y=None, nvec=1, accumulate=False):
         """y = op . x on the tensor cores (split-BF16 operands, ~1e-5 relative)."""
-        lib = _lib.load()
         x = x.contiguous()
         if y is None:
             y = torch.empty((nvec,) + self.out_shape if nvec > 1 else self.out_shape, dtype=CDT, device=x.device)
+        self.apply_tc_ptr(x.data_ptr(), y.data_ptr(), nvec, accumulate)
+        return y
+
+    def apply_tc_ptr(self, x_ptr, y_ptr, nvec=1, accumulate=False):
+        """``apply_tc`` on raw device addresses of nvec contiguous centers:
+        device memory, or pinned host memory mapped into the device's address
+        space (``carc_host_alloc_mapped``), which the kernels then read and
+        write directly over the host link."""
+        lib = _lib.load()
         if not self._groups:
             if not accumulate:
-                _lib.call("carc_zfill", y.numel(), 0.0, 0.0, ctypes.c_void_p(y.data_ptr()), current_stream_handle())
-            return y
+                n = nvec * int(np.prod(self.out_shape))
+                _lib.call("carc_zfill", n, 0.0, 0.0, ctypes.c_void_p(int(y_ptr)), current_stream_handle())
+            return
         st = self._status()
         for gi, g in enumerate(self._groups):
             plan = self._tc_plan(g)
@@ -418,13 +427,12 @@ class Stage3Operator:
                                                                 nvec)
             if ws_bytes < 0:
                 _lib.check(_lib.CARC_BAD_SHAPE)
-            ws = engine.Workspace.get(ws_bytes, x.device)
+            ws = engine.Workspace.get(ws_bytes, self.device)
             _lib.call("carc_stage3_matvec_tc", g["s0"], g["s1"], self.d, ctypes.c_void_p(plan.data_ptr()), g["n0"],
-                      g["n1"], self._po, len(self.ops), g["pt"], len(g["terms"]), ctypes.c_void_p(x.data_ptr()),
-                      ctypes.c_void_p(y.data_ptr()), nvec, int(bool(accumulate or gi > 0)),
+                      g["n1"], self._po, len(self.ops), g["pt"], len(g["terms"]), ctypes.c_void_p(int(x_ptr)),
+                      ctypes.c_void_p(int(y_ptr)), nvec, int(bool(accumulate or gi > 0)),
                       ctypes.c_void_p(ws.data_ptr()), ws_bytes, ctypes.c_void_p(st.data_ptr()),
                       current_stream_handle())
-        return y
 
     def form_matrix_tc(self, out=None, accumulate=False):
         """H on the tensor cores (split-BF16 operands, ~1e-5 relative)."""

@@ -59,6 +59,15 @@ int64_t carc_launch_counter(void);
  * stream is synchronized, returns the summed milliseconds and the number of
  * bracketed intervals of one phase and drops its records. */
 int carc_phase_timing_enable(int32_t on);
+/* Page-locked host memory mapped into the device's address space
+ * (cudaHostAllocMapped | cudaHostAllocPortable): *host_ptr for the host,
+ * *device_ptr for kernels, which read and write it directly over the
+ * host link (NVLink-C2C on Grace parts).  Passing *device_ptr as x or y of a
+ * matvec entry point moves the block and the result inside that call, with
+ * no separate copy.  Free with carc_host_free.  (No counterpart in the
+ * reference; host plumbing for callers that keep their data on the host.) */
+int carc_host_alloc_mapped(int64_t bytes, void** host_ptr, void** device_ptr);
+int carc_host_free(void* host_ptr);
 int carc_phase_timing_read(int32_t phase, double* total_ms, int64_t* count);
 
 /*
