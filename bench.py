@@ -51,10 +51,12 @@ SOLVE = dict(workload="center-site solve, Heisenberg XXX d=2, D=4, chi=64 (8x8)"
 # chi ~ U{16,24,..,96}, a block of 8 vectors each, seed 3
 BATCHED = dict(workload="batched center-site matvecs, TI, D in 2..6, chi in 16..96, block 8", nvec=8, seed=3)
 # batched solves: Hermitian-definite transverse-Ising problems (ket x bra
-# boundary layers of equal dimension c, chi = c^2), lowest eigenpair of each
-# by the batched block eigensolver (LOBPCG, block 8) to relative residual 1e-4
-BATCHED_SOLVES = dict(workload="batched center solves, TI, h in [2,4], D in 2..6, chi = c^2 with c in 4..9, "
-                               "LOBPCG block 8, relative residual 1e-4", block=8, seed=3, tol=1e-4)
+# boundary layers of equal dimension c: the drawn chi rounded to the nearest
+# square c^2), lowest eigenpair of each by the batched block eigensolver
+# (LOBPCG, block 8) to relative residual 1e-4
+BATCHED_SOLVES = dict(workload="batched center solves, TI, h in [2,4], D in 2..6, chi in 16..96 rounded to the "
+                               "nearest square c^2 (c = 4..10), LOBPCG block 8, relative residual 1e-4", block=8,
+                      seed=3, tol=1e-4)
 
 # phases of the tensor-core operator, as numbered by carc_phase_timing_read
 PHASE_NAMES = ("pack", "step_a", "step_b", "reduce")

@@ -263,13 +263,21 @@ def run(count=32, nvec=8, seed=3, mem_budget=24 << 30, reps=3, tune=True, tune_f
 
 
 # -- the solve workload ----------------------------------------------------------
-def sample_pencils(count, seed=3, D_choices=(2, 3, 4, 5, 6), c_choices=(4, 5, 6, 7, 8, 9), h_range=(2.0, 4.0)):
-    """(D, c, h, seed) of each Hermitian-definite problem: D, c and h drawn
-    uniformly; the boundary dimension is chi = c^2 (ket x bra layers of equal
-    dimension c, as every physical double-layer boundary has)."""
+def pencil_c(chi):
+    """Layer dimension of a Hermitian-definite problem drawn with boundary
+    dimension chi: ket and bra layers of equal dimension c, so chi is rounded
+    to the nearest square c^2 (c = 4..10 for chi = 16..96)."""
+    return int(np.floor(np.sqrt(chi) + 0.5))
+
+
+def sample_pencils(count, seed=3, D_choices=(2, 3, 4, 5, 6), chi_choices=tuple(range(16, 97, 8)), h_range=(2.0, 4.0)):
+    """(D, c, h, seed) of each Hermitian-definite problem: D, chi and h drawn
+    uniformly as in the batched matvec workload, chi then rounded to the
+    nearest square c^2 (every physical double-layer boundary has ket and bra
+    layers of equal dimension c)."""
     rng = np.random.default_rng(seed)
-    return [(int(rng.choice(D_choices)), int(rng.choice(c_choices)), float(rng.uniform(*h_range)), seed * 100003 + i)
-            for i in range(count)]
+    return [(int(rng.choice(D_choices)), pencil_c(int(rng.choice(chi_choices))), float(rng.uniform(*h_range)),
+             seed * 100003 + i) for i in range(count)]
 
 
 def build_pencil(D, c, h, seed):
@@ -409,7 +417,7 @@ def main(argv=None):
 
 __all__ = ["sample_problems", "build_operator", "operator_bytes", "Batch", "autotune", "run", "CHI_FACTORS", "main",
            "TUNE_CANDIDATES", "load_tuning", "save_tuning", "default_tuning_file", "sample_pencils", "build_pencil",
-           "run_solves", "pencil_cost"]
+           "run_solves", "pencil_cost", "pencil_c"]
 
 if __name__ == "__main__":
     main()
