@@ -128,6 +128,7 @@ SIGNATURES = {
     "carc_stage3_matvec_tc_workspace_size": (_i64, [_pi64, _pi64, _i64, _pi32, _i32, _i32]),
     "carc_tc_autotune_set": (ctypes.c_int, [_pi64, _pi64, _i64, _i32, _i32, _i32]),
     "carc_tc_autotune_clear": (ctypes.c_int, []),
+    "carc_tc_autotune_set_fold": (ctypes.c_int, [_pi64, _pi64, _i64, _i32, _i32, _i32]),
     "carc_stage3_form_matrix_tc": (ctypes.c_int, [_pi64, _pi64, _i64, _pvp, _i32, _pvp, _i32, _pvp, _i32, _pi32, _i32,
                                                   _vp, _i32, _vp, _i64, _vp, _vp]),
     "carc_stage3_form_matrix_tc_workspace_size": (_i64, [_pi64, _pi64, _i64, _i32]),

@@ -135,20 +135,23 @@ def _tune_key(op, g, nvec):
                 groups=_groups_of(g))
 
 
-def _set_tuning(key, ks):
+def _set_tuning(key, ks, fold=0):
     lib = _lib.load()
     s0, keep0 = _lib.i64_array(key["s0"])
     s1, keep1 = _lib.i64_array(key["s1"])
     _lib.check(lib.carc_tc_autotune_set(s0, s1, key["d"], key["nvec"], key["groups"], int(ks)))
+    _lib.check(lib.carc_tc_autotune_set_fold(s0, s1, key["d"], key["nvec"], key["groups"], int(fold)))
     del keep0, keep1
 
 
 def autotune(op, nvec, candidates=TUNE_CANDIDATES, reps=3):
-    """Time the tensor-core matvec of one operator for each candidate (0: the
-    default choice, the compact-operand fused kernel where it takes the
-    shape; -1: the first fused kernel where it takes the shape; > 0: the
-    two-kernel path with that step-B split-K count) and keep the fastest in
-    the library's autotune cache; returns one entry per term-group shape."""
+    """Time the tensor-core matvec of one operator for each path candidate
+    (0: the default choice, the compact-operand fused kernel where it takes
+    the shape; -1: the first fused kernel where it takes the shape; > 0: the
+    two-kernel path with that step-B split-K count), then, where the two-kernel
+    path wins, its step-A folding GEMM in the second tile configuration (two
+    CTAs per SM, 128-column tiles, two stages); keep the fastest in the
+    library's autotune cache.  Returns one entry per term-group shape."""
     x = torch.zeros((nvec,) + op.in_shape, dtype=CDT, device="cuda")
     y = torch.empty((nvec,) + op.out_shape, dtype=CDT, device="cuda")
     results = []
@@ -159,8 +162,15 @@ def autotune(op, nvec, candidates=TUNE_CANDIDATES, reps=3):
             _set_tuning(key, ks)
             times[ks] = _time(lambda: op.apply_tc(x, y, nvec), reps)
         best = min(times, key=times.get)
-        _set_tuning(key, best)
-        results.append(dict(key, best=int(best), ms={str(k): round(v, 5) for k, v in times.items()}))
+        fold, fold_ms = 0, None
+        if best >= 0:  # the two-kernel path (best > 0), or possibly the default (a shape no fused kernel takes)
+            _set_tuning(key, best, 1)
+            fold_ms = _time(lambda: op.apply_tc(x, y, nvec), reps)
+            if fold_ms < 0.97 * times[best]:  # a margin above timing noise
+                fold = 1
+        _set_tuning(key, best, fold)
+        results.append(dict(key, best=int(best), fold=fold, ms={str(k): round(v, 5) for k, v in times.items()},
+                            fold_ms=None if fold_ms is None else round(fold_ms, 5)))
     op.check_status()
     return results
 
@@ -181,7 +191,7 @@ def load_tuning(path=None):
     with open(path) as f:
         entries = json.load(f)["entries"]
     for e in entries:
-        _set_tuning(e, e["best"])
+        _set_tuning(e, e["best"], e.get("fold", 0))
     return entries
 
 
@@ -395,6 +405,8 @@ def main(argv=None):
     p.add_argument("--seed", type=int, default=11)
     p.add_argument("--nvec", type=int, default=8)
     p.add_argument("--ksplit", type=int, default=0, help="> 0: pin the two-kernel path with this step-B split")
+    p.add_argument("--fold", type=int, default=0, choices=[0, 1],
+                   help="step A's folding-GEMM configuration on the two-kernel path (1: two CTAs per SM)")
     p.add_argument("--reps", type=int, default=3)
     a = p.parse_args(argv)
     lib = _lib.load()
@@ -404,6 +416,7 @@ def main(argv=None):
     if a.ksplit > 0:
         for g in op._groups:
             _lib.check(lib.carc_tc_autotune_set(g["s0"], g["s1"], op.d, a.nvec, _groups_of(g), a.ksplit))
+            _lib.check(lib.carc_tc_autotune_set_fold(g["s0"], g["s1"], op.d, a.nvec, _groups_of(g), a.fold))
     try:
         for _ in range(a.reps):
             op.apply_tc(x, y, a.nvec)

@@ -329,6 +329,12 @@ int carc_tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64
   return tc_autotune_set(s0_shape, s1_shape, d, nvec, groups, ksplit);
 }
 
+int carc_tc_autotune_set_fold(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int32_t nvec,
+                              int32_t groups, int32_t variant) {
+  if (!s0_shape || !s1_shape) return fail(CARC_BAD_ARG, "carc_tc_autotune_set_fold: NULL shape");
+  return tc_autotune_set_fold(s0_shape, s1_shape, d, nvec, groups, variant);
+}
+
 int carc_tc_autotune_clear(void) { return tc_autotune_clear(); }
 
 int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,

@@ -197,6 +197,7 @@ struct TuneKey {
 };
 std::mutex g_tune_mu;
 std::map<TuneKey, int> g_tune;
+std::map<TuneKey, int> g_tune_fold;  // step A's folding-GEMM configuration (0 or 1)
 
 TuneKey tune_key(const int64_t* s0, const int64_t* s1, int64_t d, int nvec, int groups) {
   TuneKey k;
@@ -214,6 +215,12 @@ int tuned_ksplit(const int64_t* s0, const int64_t* s1, int64_t d, int nvec, int 
   std::lock_guard<std::mutex> lk(g_tune_mu);
   auto it = g_tune.find(tune_key(s0, s1, d, nvec, groups));
   return it == g_tune.end() ? 0 : it->second;
+}
+
+int tuned_fold(const int64_t* s0, const int64_t* s1, int64_t d, int nvec, int groups) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune_fold.find(tune_key(s0, s1, d, nvec, groups));
+  return it == g_tune_fold.end() ? 0 : it->second;
 }
 
 // split-K count that fills the 152 SMs (one CTA each) in a single wave
@@ -375,9 +382,22 @@ int tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
   return CARC_OK;
 }
 
+int tc_autotune_set_fold(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int nvec, int groups,
+                         int variant) {
+  if (variant < 0 || variant > 1 || nvec < 1 || groups < 1) return fail(CARC_BAD_ARG, "tc autotune: bad fold entry");
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  const TuneKey k = tune_key(s0_shape, s1_shape, d, nvec, groups);
+  if (variant == 0)
+    g_tune_fold.erase(k);
+  else
+    g_tune_fold[k] = variant;
+  return CARC_OK;
+}
+
 int tc_autotune_clear() {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune.clear();
+  g_tune_fold.clear();
   return CARC_OK;
 }
 
@@ -1910,7 +1930,7 @@ namespace {
 
 // step A (one folding GEMM per S2_1 tag, W to HBM) and step B (one split-K GEMM)
 int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, const Geo& g, const void* plan,
-                  const MvWs& w, int* status, cudaStream_t stream) {
+                  const MvWs& w, int* status, cudaStream_t stream, int fold_variant) {
   const int G = (int)tg.i1.size();
   const int64_t kpB = g.regB * G;
   const int64_t rows_valid_w = (int64_t)nvec * s.l0 * s.l1 * s.d;
@@ -1945,7 +1965,7 @@ int unfused_steps(const S3& s, int nvec, const TermGroups& tg, const Geo& g1, co
       fe.rows = g.rowsB_b;
       fe.dst = w.w_pk;
       CARC_RETURN_IF(gemm_bf16_tn_fold(planA, (int)g1.rowsA_a, w.vin + w.vin_off[q], (int)g.rowsA_b, (int)kpA, fe,
-                                       status, stream));
+                                       status, stream, fold_variant));
       planA += a256(g1.rowsA_a * kpA * 2);
     }
   }
@@ -2164,7 +2184,8 @@ int stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d
     plane_ld = rows_valid_w;
     plane_stride = round_up(4 * s.l2 * s.l3, 32) * rows_valid_w;
   } else {
-    CARC_RETURN_IF(unfused_steps(s, nvec, tg, g1, g, plan, w, status, stream));
+    CARC_RETURN_IF(unfused_steps(s, nvec, tg, g1, g, plan, w, status, stream,
+                                 tuned_fold(s0_shape, s1_shape, s.d, nvec, (int)tg.i1.size())));
     plane_ld = g.rowsB_b;
     plane_stride = g.rowsB_a * g.rowsB_b;
   }

@@ -8,6 +8,8 @@ int stage3_tc_prepare(const int64_t* s0_shape, const int64_t* s1_shape, const vo
                       const void* const* s1_ptrs, int n1, const int32_t* terms, int n_terms, void* plan,
                       int64_t plan_bytes, cudaStream_t stream);
 int tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int nvec, int groups, int ksplit);
+int tc_autotune_set_fold(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int nvec, int groups,
+                         int variant);
 int tc_autotune_clear();
 int64_t stage3_matvec_tc_ws(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, const int32_t* terms,
                             int n_terms, int nvec);

@@ -580,6 +580,11 @@ __global__ __launch_bounds__(THREADS, 1) void gemm_bf16_tn_grouped_kernel(const 
 // lets its copies and MMAs land, frees TMEM and reports CARC_NOT_CONVERGED.
 constexpr int FG_EPI_WARPS = 16;
 constexpr int FG_THREADS = 32 * (2 + FG_EPI_WARPS);
+// the second configuration: two CTAs per SM, each with 8 fold warps, two
+// stages and 128-column tiles (about 100 KB of shared memory and 256 TMEM
+// columns per CTA), so that one CTA's fold overlaps the other's loads and MMAs
+constexpr int FG2_EPI_WARPS = 8;
+constexpr int FG2_STAGES = 2;
 
 template <int BN>
 __host__ __device__ constexpr int fg_stage_bytes() { return A_STAGE_BYTES + BN * BK * 2; }
@@ -597,8 +602,14 @@ __host__ __device__ constexpr int fg_smem_bytes() {
   return 1024 + fg_stages<BN>() * fg_stage_bytes<BN>() + fold_smem_bytes<BN>() + 256;
 }
 
+template <int BN, int NST>
+__host__ __device__ constexpr int fg_smem_bytes_st() {
+  return 1024 + NST * fg_stage_bytes<BN>() + fold_smem_bytes<BN>() + 256;
+}
+
 // OR of a predicate over the epilogue warps (named barrier 1): every one of
 // them takes the same branch after a wait that may have given up.
+template <int EPIW>
 __device__ __forceinline__ bool fg_epilogue_any(bool v) {
   uint32_t r;
   asm volatile(
@@ -609,25 +620,25 @@ __device__ __forceinline__ bool fg_epilogue_any(bool v) {
       "selp.u32 %0, 1, 0, p;\n"
       "}\n"
       : "=r"(r)
-      : "r"((uint32_t)v), "n"(32 * FG_EPI_WARPS)
+      : "r"((uint32_t)v), "n"(32 * EPIW)
       : "memory");
   return r != 0;
 }
 
-template <int BN>
-__global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
+template <int BN, int EPIW, int NST>
+__global__ __launch_bounds__(32 * (2 + EPIW), EPIW == EPIW ? 1 : 2) void fold_gemm_kernel(const __grid_constant__ CUtensorMap tmA,
                                                                   const __grid_constant__ CUtensorMap tmB,
                                                                   int n_tiles, int tiles, int nkb, int* __restrict__ err,
                                                                   const __grid_constant__ FoldEpi fe) {
   using namespace umma;
-  constexpr int STAGES = fg_stages<BN>();
+  constexpr int STAGES = NST;
   static_assert(STAGES >= 2, "the folding GEMM needs at least two pipeline stages");
-  static_assert(FG_EPI_WARPS % ((FOLD_HC<BN>() + 31) / 32) == 0, "epilogue warps per slot group");
+  static_assert(EPIW % ((FOLD_HC<BN>() + 31) / 32) == 0, "epilogue warps per slot group");
   constexpr int B_STAGE_BYTES = BN * BK * 2;
   constexpr uint32_t ACC_COLS = tmem_cols_for(BN);
   constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
   constexpr int HC = FOLD_HC<BN>();
-  constexpr int EPI_THREADS = 32 * FG_EPI_WARPS;
+  constexpr int EPI_THREADS = 32 * EPIW;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint8_t* sA = smem;
@@ -651,7 +662,7 @@ __global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_c
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], FG_EPI_WARPS);
+      mbar_init(&acc_empty[b], EPIW);
     }
     mbar_init(done, 1);
     *abort_flag = 0;
@@ -725,7 +736,7 @@ __global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_c
   } else {
     // epilogue warps: e = 0..15, TMEM lane quadrant warp % 4, column block
     // phase h (each 32-column block of a quadrant goes to one of its warps)
-    constexpr int PER_QUAD = FG_EPI_WARPS / 4;
+    constexpr int PER_QUAD = EPIW / 4;
     const int e = warp - 2, quad = warp & 3, h = e >> 2;
     const int ds = fold_ds<BN>(fe.d);
     for (int i = 0; i < my_tiles; ++i) {
@@ -733,7 +744,7 @@ __global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_c
       const int t = (int)blockIdx.x + i * (int)gridDim.x;
       const int m0 = (t / n_tiles) * BM, n0 = (t % n_tiles) * BN;
       const bool got = mbar_wait_sleep(&acc_full[b], (uint32_t)((i >> 1) & 1), abort_flag);
-      if (fg_epilogue_any(!got)) break;  // all epilogue warps leave together
+      if (fg_epilogue_any<EPIW>(!got)) break;  // all epilogue warps leave together
       tc_fence_after();
       const uint32_t acc = tmem + (uint32_t)b * ACC_COLS + ((uint32_t)(quad * 32) << 16);
       for (int h0 = 0; h0 < BN; h0 += HC) {
@@ -760,7 +771,7 @@ __global__ __launch_bounds__(FG_THREADS, 1) void fold_gemm_kernel(const __grid_c
         }
         fold_tables<BN>(sP, fe, m0, n0 + h0, ds, threadIdx.x - 64, EPI_THREADS);
         asm volatile("bar.sync 1, %0;" ::"n"(EPI_THREADS) : "memory");
-        fold_write<BN>(sP, fe, e, FG_EPI_WARPS);
+        fold_write<BN>(sP, fe, e, EPIW);
       }
     }
   }
@@ -946,15 +957,19 @@ int gemm_bf16_tn(const void* A, int M, const void* B, int N, int K, float* out, 
 
 namespace {
 
-template <int BN>
+template <int BN, int EPIW, int NST>
 int launch_fold(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int nkb, int* err, const FoldEpi& fe,
                 cudaStream_t stream) {
-  constexpr int SMEM = fg_smem_bytes<BN>();
+  constexpr int SMEM = fg_smem_bytes_st<BN, NST>();
+  constexpr int CTAS_PER_SM = EPIW == FG_EPI_WARPS ? 1 : 2;
   static_assert(SMEM <= 227 * 1024, "folding GEMM shared memory");
+  static_assert(CTAS_PER_SM * SMEM <= 228 * 1024, "folding GEMM shared memory per SM");
+  static_assert(CTAS_PER_SM * 2 * (int)tmem_cols_for(BN) <= 512, "folding GEMM TMEM per SM");
   static std::once_flag once;
   static cudaError_t attr_err = cudaSuccess;
   std::call_once(once, [] {
-    attr_err = cudaFuncSetAttribute(fold_gemm_kernel<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM);
+    attr_err = cudaFuncSetAttribute(fold_gemm_kernel<BN, EPIW, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    SMEM);
   });
   if (attr_err != cudaSuccess) return fail(CARC_CUDA_ERROR, "folding GEMM: %s", cudaGetErrorString(attr_err));
   int dev = 0, sms = 0;
@@ -963,8 +978,8 @@ int launch_fold(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int 
   const int n_tiles = N / BN;
   const int64_t tiles = (int64_t)(M / BM) * n_tiles;
   if (tiles >= (int64_t(1) << 31)) return fail(CARC_TOO_LARGE, "folding GEMM: %lld tiles", (long long)tiles);
-  const int grid = (int)std::min<int64_t>(tiles, std::max(1, sms));
-  fold_gemm_kernel<BN><<<grid, FG_THREADS, SMEM, stream>>>(ma, mb, n_tiles, (int)tiles, nkb, err, fe);
+  const int grid = (int)std::min<int64_t>(tiles, (int64_t)std::max(1, sms) * CTAS_PER_SM);
+  fold_gemm_kernel<BN, EPIW, NST><<<grid, 32 * (2 + EPIW), SMEM, stream>>>(ma, mb, n_tiles, (int)tiles, nkb, err, fe);
   CARC_CHECK_LAUNCH();
   return CARC_OK;
 }
@@ -972,7 +987,7 @@ int launch_fold(const CUtensorMap& ma, const CUtensorMap& mb, int M, int N, int 
 }  // namespace
 
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
-                      cudaStream_t stream) {
+                      cudaStream_t stream, int variant) {
   if (M <= 0 || N <= 0 || K <= 0 || M % BM != 0 || K % BK != 0 || N % 16 != 0)
     return fail(CARC_BAD_SHAPE, "tensor core GEMM: shape %d x %d x %d not tileable (M%%128, K%%64, N%%16)", M, N, K);
   if (fe.M * 4 > M || fe.N > N || (fe.col_off & 1) || fe.rows < fe.l0 * fe.l1 * fe.d * fe.nvec ||
@@ -983,12 +998,18 @@ int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const F
   CUtensorMap ma, mb;
   CARC_RETURN_IF(make_map(&ma, A, (uint64_t)K, (uint64_t)M, BM));
   CARC_RETURN_IF(make_map(&mb, B, (uint64_t)K, (uint64_t)N, (uint32_t)bn));
+  if (variant == 1 && N % 128 == 0) {
+    // two CTAs per SM: 128-column tiles, 8 fold warps, 2 stages each
+    CUtensorMap mb2;
+    CARC_RETURN_IF(make_map(&mb2, B, (uint64_t)K, (uint64_t)N, 128u));
+    return launch_fold<128, FG2_EPI_WARPS, FG2_STAGES>(ma, mb2, M, N, kb_total, err, fe, stream);
+  }
   switch (bn) {
-    case 256: return launch_fold<256>(ma, mb, M, N, kb_total, err, fe, stream);
-    case 128: return launch_fold<128>(ma, mb, M, N, kb_total, err, fe, stream);
-    case 64: return launch_fold<64>(ma, mb, M, N, kb_total, err, fe, stream);
-    case 32: return launch_fold<32>(ma, mb, M, N, kb_total, err, fe, stream);
-    default: return launch_fold<16>(ma, mb, M, N, kb_total, err, fe, stream);
+    case 256: return launch_fold<256, FG_EPI_WARPS, fg_stages<256>()>(ma, mb, M, N, kb_total, err, fe, stream);
+    case 128: return launch_fold<128, FG_EPI_WARPS, fg_stages<128>()>(ma, mb, M, N, kb_total, err, fe, stream);
+    case 64: return launch_fold<64, FG_EPI_WARPS, fg_stages<64>()>(ma, mb, M, N, kb_total, err, fe, stream);
+    case 32: return launch_fold<32, FG_EPI_WARPS, fg_stages<32>()>(ma, mb, M, N, kb_total, err, fe, stream);
+    default: return launch_fold<16, FG_EPI_WARPS, fg_stages<16>()>(ma, mb, M, N, kb_total, err, fe, stream);
   }
 }
 

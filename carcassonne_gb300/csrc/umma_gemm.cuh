@@ -92,7 +92,7 @@ int tma_map_bf16(CUtensorMap* map, const void* base, uint64_t inner, uint64_t ro
 // a persistent warp-specialised kernel (one CTA per SM, two TMEM accumulators)
 // writing W K-block-major (FoldEpi).
 int gemm_bf16_tn_fold(const void* A, int M, const void* B, int N, int K, const FoldEpi& fe, int* err,
-                      cudaStream_t stream);
+                      cudaStream_t stream, int variant = 0);
 // Deterministic FP64 reduction of split-K planes into a complex output in one
 // launch (coalesced over columns, planes spread over 8 warps per block); the
 // workspace arguments are kept for the callers' layouts and need 256 bytes.

@@ -229,6 +229,13 @@ int carc_stage3_matvec_tc(const int64_t* s0_shape, const int64_t* s1_shape, int6
  * Query workspace sizes after setting an entry. */
 int carc_tc_autotune_set(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int32_t nvec, int32_t groups,
                          int32_t ksplit);
+/* The folding-GEMM configuration of step A on the two-kernel path for one
+ * shape: 0 (default) one CTA per SM with 16 fold warps, stages and N tiles
+ * as the shape allows; 1 two CTAs per SM, each with 8 fold warps, 2 stages
+ * and 128-column N tiles (used where step A's padded N is a multiple of 128).
+ * Cleared with the rest of the cache by carc_tc_autotune_clear. */
+int carc_tc_autotune_set_fold(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d, int32_t nvec,
+                              int32_t groups, int32_t variant);
 int carc_tc_autotune_clear(void);
 int64_t carc_stage3_matvec_tc_workspace_size(const int64_t* s0_shape, const int64_t* s1_shape, int64_t d,
                                              const int32_t* terms, int32_t n_terms, int32_t nvec);
