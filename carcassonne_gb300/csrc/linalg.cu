@@ -252,15 +252,28 @@ __global__ __launch_bounds__(HEEV_THREADS) void heev_jacobi_kernel(int n, int n_
   double2* A = Aall + blockIdx.x * (int64_t)n * n;
   double2* V = Vall + blockIdx.x * (int64_t)n * n;
   extern __shared__ double rot[];  // per pair: c, s, ph.x, ph.y, p, q  (6 doubles)
-  __shared__ int rotated;
   __shared__ double off_norm, diag_norm;
   for (int i = threadIdx.x; i < n * n; i += HEEV_THREADS) V[i] = make_double2((i / n) == (i % n) ? 1.0 : 0.0, 0.0);
+  // the Hermitian part (A + A^H) / 2: the rotations are computed from the
+  // upper triangle, and any anti-Hermitian residue of the input (a product
+  // such as X^H M X rounds to a matrix that is Hermitian only to a few ulps of
+  // its largest entries) survives every unitary rotation with its Frobenius
+  // norm intact, so on a matrix whose small eigenvalues lie below that residue
+  // the off-diagonal mass would never fall to the stopping level
+  for (int idx = threadIdx.x; idx < n * n; idx += HEEV_THREADS) {
+    const int i = idx / n, j = idx % n;
+    if (i > j) continue;
+    const double2 u = A[i * n + j], l = A[j * n + i];
+    const double2 h = make_double2(0.5 * (u.x + l.x), i == j ? 0.0 : 0.5 * (u.y - l.y));
+    A[i * n + j] = h;
+    A[j * n + i] = cconj(h);
+  }
   __syncthreads();
   const int npairs = n_even / 2;
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
+    int rotated = 0;  // this thread's rotations in this sweep
     if (threadIdx.x == 0) {
-      rotated = 0;
       double on = 0.0, dn = 0.0;
       for (int i = 0; i < n; ++i)
         for (int j = 0; j < n; ++j) {
@@ -336,8 +349,9 @@ __global__ __launch_bounds__(HEEV_THREADS) void heev_jacobi_kernel(int n, int n_
       }
       __syncthreads();
     }
-    __syncthreads();
-    if (!rotated) break;
+    // one barrier both joins the threads' flags and ends the sweep, so no
+    // thread can read a flag that the next sweep has already reset
+    if (!__syncthreads_or(rotated)) break;
   }
   if (threadIdx.x == 0 && sweep >= max_sweeps) atomicExch(status, CARC_NOT_CONVERGED);
 }

@@ -99,6 +99,30 @@ def test_hermitian_jacobi_eigh(env, n):
     assert np.abs(a @ v - v * w).max() <= 1e-10 * np.abs(a).max()
 
 
+@pytest.mark.parametrize("n,rank", [(96, 24), (162, 40)])
+def test_jacobi_eigh_nearly_hermitian_rank_deficient(env, n, rank):
+    """A normalization matrix near a product state: rank-deficient, tiny, and
+    Hermitian only up to an anti-Hermitian residue of 1e-11 of its norm (a
+    rounded X^H M X).  The eigensolver works on the Hermitian part; rotations
+    driven by one triangle of the raw matrix never bring its off-diagonal
+    mass down to the stopping level."""
+    TorchData, linalg, _, _ = env
+    rng = np.random.default_rng(n + rank)
+    x = cn(rng, n, rank)
+    m = (x @ x.conj().T) * 1e-15
+    e = cn(rng, n, n)
+    e = e - e.conj().T
+    m = m + e * (1e-11 * np.linalg.norm(m) / np.linalg.norm(e))
+    h = 0.5 * (m + m.conj().T)
+    W, V = linalg.eigh_small(TorchData(m))
+    w = W.cpu().numpy()
+    ref = np.linalg.eigvalsh(h)
+    assert np.abs(w - ref).max() <= 1e-12 * np.abs(ref).max()
+    v = V.toArray()
+    assert np.abs(h @ v - v * w).max() <= 1e-11 * np.abs(h).max()
+    assert np.abs(v.conj().T @ v - np.eye(n)).max() <= 1e-12
+
+
 @pytest.mark.parametrize("n", [1, 31, 33, 100, 512])
 def test_cholesky_and_generalized_lowest(env, n):
     TorchData, linalg, _, _ = env
