@@ -416,10 +416,18 @@ def _cpu_contract_compress(system, direction, new_dimension):
     return t1 - t0, time.perf_counter() - t1
 
 
-def growth_section(cpu=True):
+def growth_section(cpu=True, heis_steps=None, cpu_step=None):
+    """Both growth runs; ``heis_steps`` runs the Heisenberg one for that many
+    absorptions (the configured run is 40; 12 by default, to keep the default
+    bench short), ``cpu_step`` puts the CPU reference's step there instead of
+    at each run's last step."""
     out = {}
     for name, spec in GROWTH.items():
-        cpu_steps = (spec["steps"] - 1,) if cpu else ()
+        if heis_steps and spec["kind"] == "heis":
+            spec = dict(spec, steps=int(heis_steps),
+                        workload="growth run, Heisenberg XXX, D=4, chi=64 (c=8), %d absorptions" % int(heis_steps))
+        last = spec["steps"] - 1
+        cpu_steps = ((min(cpu_step, last) if cpu_step is not None else last),) if cpu else ()
         out[name] = growth_run(spec, cpu_steps)
     return out
 
@@ -443,6 +451,10 @@ def parse_args():
                    help="skip the batched solves (batched block eigensolver vs the per-problem loop; sharded "
                         "over ranks under torchrun)")
     p.add_argument("--solves-count", type=int, default=256)
+    p.add_argument("--growth-heis-steps", type=int, default=None,
+                   help="absorptions of the Heisenberg growth run (the configured run is 40; default 12)")
+    p.add_argument("--growth-cpu-step", type=int, default=None,
+                   help="step of each growth run also run by the CPU reference (default: the last)")
     p.add_argument("--no-growth", dest="growth", action="store_false",
                    help="skip the growth runs' per-step time-to-energy (plain vs mixed)")
     return p.parse_args()
@@ -856,7 +868,8 @@ def main():
     cpu = cpu_reference(args, args.cpu_seconds) if world == 1 else None
     solve = solve_section() if args.solve else None
     if solve is not None and args.growth:
-        solve["growth"] = growth_section(cpu=world == 1)
+        solve["growth"] = growth_section(cpu=world == 1, heis_steps=args.growth_heis_steps,
+                                         cpu_step=args.growth_cpu_step)
     batched = None
     if args.batched and world == 1:
         from carcassonne_gb300 import batched as batched_mod
