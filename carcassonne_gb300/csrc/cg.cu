@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(kGridThreads) zcg_grid_kernel(const __grid_con
   double2* r = gsm + rpc;
   double2* pl = gsm + 2 * rpc;
   double2* gp = gsm + 3 * rpc;
+  double2* xb = gsm + 4 * rpc;  // the iterate with the smallest residual so far
   __shared__ double red[kGridWarps + 1];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int G = (int)gridDim.x, b = (int)blockIdx.x;
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(kGridThreads) zcg_grid_kernel(const __grid_con
   for (int i = tid; i < nr; i += kGridThreads) {
     const double2 ci = p.c[r0 + i];
     x[i] = make_double2(0.0, 0.0);
+    xb[i] = make_double2(0.0, 0.0);
     r[i] = ci;
     pl[i] = ci;
     p.p_glob[r0 + i] = ci;
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(kGridThreads) zcg_grid_kernel(const __grid_con
   if (tid == 0) part1[b] = v;
   bool ok = gsync();
   const double c2 = ok ? grid_total(part1, red) : 0.0;
-  double rr = c2;
+  double rr = c2, best = c2, last = c2;  // last: the recursive |r|^2 of the current x
   int it = 0, converged = (c2 == 0.0) ? 1 : 0;
   const double thresh = p.tol * p.tol * c2;
   while (ok && !converged && it < p.max_iter) {
@@ -255,11 +257,20 @@ __global__ void __launch_bounds__(kGridThreads) zcg_grid_kernel(const __grid_con
     if (!(ok = gsync())) break;
     const double rr_new = grid_total(part1, red);
     ++it;
+    last = rr_new;
+    if (rr_new < best) {
+      best = rr_new;
+      for (int i = tid; i < nr; i += kGridThreads) xb[i] = x[i];
+    }
     if (rr_new <= thresh) {
       rr = rr_new;
       converged = 1;
       break;
     }
+    // a right-hand side with a rounding-level part outside the range of a
+    // singular G: the steps along G's near-null directions grow without
+    // bound, so the iteration stops once the residual is far above its best
+    if (rr_new > 1e8 * best) break;
     const double beta = rr_new / rr;
     for (int i = tid; i < nr; i += kGridThreads) {
       pl[i] = cadd(r[i], cscale(pl[i], beta));
@@ -269,11 +280,29 @@ __global__ void __launch_bounds__(kGridThreads) zcg_grid_kernel(const __grid_con
     if (!(ok = gsync())) break;
   }
   __syncthreads();
-  for (int i = tid; i < nr; i += kGridThreads) p.x_out[r0 + i] = x[i];
+  // the returned x is the iterate with the smallest recursive residual (the
+  // current one unless the residual rose after its best), and the reported
+  // residual is the true |c - G x| / |c| of that x
+  const bool use_best = best < last;
+  for (int i = tid; i < nr; i += kGridThreads) p.x_out[r0 + i] = use_best ? xb[i] : x[i];
+  double true_rr = 0.0;
+  if (ok && c2 > 0.0 && (ok = gsync())) {
+    v = 0.0;
+    for (int i = warp; i < nr; i += kGridWarps) {
+      const double2* gi = p.G + (int64_t)(r0 + i) * n;
+      double2 s = make_double2(0.0, 0.0);
+      for (int j = lane; j < n; j += 32) cfma(s, gi[j], __ldcg(p.x_out + j));
+      s = warp_sum2(s);
+      if (lane == 0) v += cabs2(csub(p.c[r0 + i], s));
+    }
+    v = block_sum_d(v, red);
+    if (tid == 0) part0[b] = v;
+    if ((ok = gsync())) true_rr = grid_total(part0, red);
+  }
   if (b == 0 && tid == 0) {
     p.status[0] = ok ? it : -1;
     p.status[1] = ok ? converged : 0;
-    p.res[0] = !ok ? 1.0e300 : (c2 > 0.0 ? sqrt(rr / c2) : 0.0);
+    p.res[0] = !ok ? 1.0e300 : (c2 > 0.0 ? sqrt(true_rr / c2) : 0.0);
   }
 }
 
@@ -297,7 +326,7 @@ int zcg_hpsd_grid(int n, const void* Gm, const void* c, void* x, double tol, int
   if (!ws || ws_bytes < zcg_hpsd_grid_workspace(n)) return fail(CARC_BAD_ARG, "carc_zcg_hpsd_grid: workspace too small");
   const int G = cg_grid_ctas(n);
   const int rpc = (n + G - 1) / G;
-  const size_t smem = (size_t)4 * rpc * sizeof(double2);
+  const size_t smem = (size_t)5 * rpc * sizeof(double2);
   if (smem > 48 * 1024) return fail(CARC_TOO_LARGE, "carc_zcg_hpsd_grid: %d rows per CTA", rpc);
   char* w = static_cast<char*>(ws);
   CgGridParams p;

@@ -162,7 +162,69 @@ def contract_grouped(spec, a_list, b_list, out_list, entries, out_letters_shape=
     return _launch(desc, a_list, b_list, out_list, entries, alpha, accumulate)
 
 
+def _split_table(n_c, entries, limit, max_entries):
+    """Calls of at most ``limit`` distinct A, B and output slots and
+    ``max_entries`` entries covering a grouped table:
+    [(a_idx, b_idx, c_idx, local entries, accumulate_all)].  Every output
+    keeps all its entries, in their order, in one call, unless its own
+    entries need more than ``limit`` A or B slots or ``max_entries`` entries;
+    then its entries go to consecutive calls of that output alone, the later
+    ones accumulating onto the first.  Outputs without entries are still
+    written (zeroed)."""
+    by_c = {}
+    for e in entries:
+        by_c.setdefault(int(e[2]), []).append((int(e[0]), int(e[1])))
+    calls = []  # (a set, b set, outputs, global entries, accumulate)
+    cur = dict(a=set(), b=set(), c=[], e=[])
+
+    def flush():
+        if cur["c"]:
+            calls.append((cur["a"], cur["b"], cur["c"], cur["e"], False))
+        cur.update(a=set(), b=set(), c=[], e=[])
+
+    for c in range(n_c):
+        ab = by_c.get(c, [])
+        a_new, b_new = {a for a, _ in ab}, {b for _, b in ab}
+        if len(a_new) > limit or len(b_new) > limit or len(ab) > max_entries:
+            flush()
+            part, pa, pb, first = [], set(), set(), True
+            for a, b in ab:
+                if len(pa | {a}) > limit or len(pb | {b}) > limit or len(part) + 1 > max_entries:
+                    calls.append((pa, pb, [c], part, not first))
+                    part, pa, pb, first = [], set(), set(), False
+                part.append((a, b, c))
+                pa.add(a)
+                pb.add(b)
+            calls.append((pa, pb, [c], part, not first))
+            continue
+        if (len(cur["a"] | a_new) > limit or len(cur["b"] | b_new) > limit or len(cur["c"]) + 1 > limit
+                or len(cur["e"]) + len(ab) > max_entries):
+            flush()
+        cur["a"] |= a_new
+        cur["b"] |= b_new
+        cur["c"].append(c)
+        cur["e"].extend((a, b, c) for a, b in ab)
+    flush()
+    out = []
+    for a_set, b_set, c_idx, ents, acc in calls:
+        a_idx, b_idx = sorted(a_set), sorted(b_set)
+        am = {x: i for i, x in enumerate(a_idx)}
+        bm = {x: i for i, x in enumerate(b_idx)}
+        cm = {x: i for i, x in enumerate(c_idx)}
+        out.append((a_idx, b_idx, c_idx, [(am[a], bm[b], cm[c]) for a, b, c in ents], acc))
+    return out
+
+
 def _launch(desc, a_list, b_list, out_list, entries, alpha=1.0, accumulate=False):
+    limit = _lib.MAX_SLOTS
+    if len(a_list) > limit or len(b_list) > limit or len(out_list) > limit or len(entries) > _lib.MAX_ENTRIES:
+        for a_idx, b_idx, c_idx, ents, acc in _split_table(len(out_list), entries, limit, _lib.MAX_ENTRIES):
+            if not ents and not a_idx:
+                # outputs with no entry: the smallest operands keep the call valid
+                a_idx, b_idx, ents = [0], [0], []
+            _launch(desc, [a_list[i] for i in a_idx], [b_list[j] for j in b_idx], [out_list[c] for c in c_idx],
+                    ents, alpha, accumulate or acc)
+        return
     lib = _lib.load()
     device = out_list[0].device
     n_c = len(out_list)

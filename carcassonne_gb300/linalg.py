@@ -203,6 +203,34 @@ def hegv_lowest(H, N, x0=None, tol=1e-13, max_krylov=256, max_restarts=8, tensor
     return lam[0], TorchData(x), iters.value
 
 
+def hegv_lowest_projected(H, N, cut=1e-12):
+    """Lowest eigenpair of H x = l N x on the range of N, for an N whose
+    Cholesky factorisation fails (nearly singular, with rounding-level
+    negative eigenvalues).  Canonical orthogonalisation: N = V diag(w) V^H
+    (Jacobi), X = V_k diag(w_k^-1/2) over the eigenvalues w_k > cut max(w),
+    then the lowest eigenpair (l, c) of the Hermitian X^H H X and x = X c,
+    N-normalized.  The same pencil as scipy.linalg.eigh(H, N) where N is
+    definite, with N's near-null directions dropped where it is not.  Returns
+    (l, x, kept dimension); n <= 512."""
+    Ht = (H._t if isinstance(H, TorchData) else TorchData(H)._t).contiguous()
+    Nt = (N._t if isinstance(N, TorchData) else TorchData(N)._t).contiguous()
+    n = Ht.shape[0]
+    W, V = eigh_small(TorchData(Nt))
+    w = W.cpu().numpy()
+    wmax = float(np.abs(w).max()) if n else 0.0
+    k0 = int(np.searchsorted(w, cut * wmax, side="right")) if wmax > 0 else n
+    kept = n - k0
+    if kept == 0:
+        raise np.linalg.LinAlgError("hegv: the normalization matrix is zero")
+    scale = torch.from_numpy(w[k0:] ** -0.5).to(device=Ht.device, dtype=CDT)
+    X = engine.contract("ij,jk->ik", V._t[:, k0:].contiguous(), torch.diag(scale), (n, kept))
+    HX = engine.contract("ij,jk->ik", Ht, X, (n, kept))
+    C = engine.contract("ji,jk->ik", X, HX, (kept, kept), conj_a=True)
+    W2, V2 = eigh_small(TorchData(C))
+    x = engine.contract("ij,jk->ik", X, V2._t[:, :1].contiguous(), (n, 1)).reshape(-1)
+    return float(W2[0].item()), TorchData(x), kept
+
+
 def minres_projected(C, u, shift, b, maxit=60, rtol=1e-3):
     """z solving P (C - shift) P z = P b, P = I - u u^H (u unit), C dense
     Hermitian: MINRES on the device.  Returns (z, iterations)."""
@@ -221,4 +249,4 @@ def minres_projected(C, u, shift, b, maxit=60, rtol=1e-3):
 
 
 __all__ = ["svd", "unitize", "normalize_axis", "qr", "qr_economic", "eigh_small", "cholesky", "tri_inverse_lower",
-           "hegv_lowest", "minres_projected"]
+           "hegv_lowest", "hegv_lowest_projected", "minres_projected"]

@@ -14,7 +14,11 @@ mixed  : H_eff and N_eff formed on the tensor cores from split-BF16 operands
          the tensor-core eigenvector itself, with the exact H x and N x.
 
 Both return the energy, the N-normalized center and a breakdown of where the
-time went (CUDA events on the current stream).
+time went (CUDA events on the current stream).  Where N is too ill-conditioned
+for the mixed reduction, the mixed solve runs the plain one; where FP64
+Cholesky rejects N too, the pencil is solved on the range of N
+(linalg.hegv_lowest_projected).  The result's ``fallback`` key names the path
+taken ("plain" or "projected"; None when there was none).
 """
 from __future__ import annotations
 
@@ -140,7 +144,8 @@ def solve_center(H, N, x0=None, precision="plain", tol=None, newton=True):
         nrm = abs(_dot(xt.reshape(-1), Nop.apply(xt).reshape(-1))) ** 0.5
         timer.mark("eigensolve")
         return dict(energy=0.0, center=TorchData(_lin(1.0 / nrm, xt, 0.0, xt)), iterations=0,
-                    timing_ms=timer.breakdown(), lanczos_eigenvalue=0.0, rayleigh_before_correction=None)
+                    timing_ms=timer.breakdown(), lanczos_eigenvalue=0.0, rayleigh_before_correction=None,
+                    fallback=None)
     if precision == "plain":
         Hm = Hop.form_matrix()
         Nm = Nop.form_matrix()
@@ -156,9 +161,25 @@ def solve_center(H, N, x0=None, precision="plain", tol=None, newton=True):
     if precision == "mixed":
         n = Hm.shape[0]
         factors = torch.empty(2 * n * n + n, dtype=CDT, device=Hm.device)
-    lam, x, iters = linalg.hegv_lowest(TorchData(Hm), TorchData(Nm), x0=x0, tol=tol,
-                                       tensor_core=(precision == "mixed"), factors=factors,
-                                       single=(precision == "mixed"))
+    try:
+        lam, x, iters = linalg.hegv_lowest(TorchData(Hm), TorchData(Nm), x0=x0, tol=tol,
+                                           tensor_core=(precision == "mixed"), factors=factors,
+                                           single=(precision == "mixed"))
+    except np.linalg.LinAlgError:
+        if precision == "mixed":
+            # the tensor-core N (about 1e-5 relative) factored in complex64
+            # is not positive definite: N's condition number is beyond what
+            # the mixed reduction resolves, so this step is solved in FP64
+            out = solve_center(H, N, x0=x0, precision="plain")
+            out["fallback"] = "plain" if out.get("fallback") is None else out["fallback"]
+            return out
+        # FP64 Cholesky rejects N (nearly singular, rounding-level negative
+        # eigenvalues): the pencil on the range of N
+        lam, x, kept = linalg.hegv_lowest_projected(TorchData(Hm), TorchData(Nm))
+        timer.mark("eigensolve")
+        return dict(energy=float(lam), center=TorchData(x._t.reshape(Hop.in_shape)), iterations=0,
+                    timing_ms=timer.breakdown(), lanczos_eigenvalue=float(lam), rayleigh_before_correction=None,
+                    fallback="projected", kept=kept)
     timer.mark("eigensolve")
     xt = x._t
     energy = lam
@@ -175,7 +196,8 @@ def solve_center(H, N, x0=None, precision="plain", tol=None, newton=True):
         timer.mark("refine")
     out = TorchData(xt.reshape(Hop.in_shape))
     return dict(energy=float(energy), center=out, iterations=iters, timing_ms=timer.breakdown(),
-                lanczos_eigenvalue=float(lam), rayleigh_before_correction=rq0 if precision == "mixed" else None)
+                lanczos_eigenvalue=float(lam), rayleigh_before_correction=rq0 if precision == "mixed" else None,
+                fallback=None)
 
 
 __all__ = ["solve_center"]

@@ -344,15 +344,32 @@ class Stage3Operator:
         self._pack()
 
     def _pack(self):
-        """One library call per shape class of (S2_0, S2_1) pairs; the stage-2
-        tags of a boundary differ in shape only through a compressed operator axis."""
+        """One library call per shape class of (S2_0, S2_1) pairs (the stage-2
+        tags of a boundary differ in shape only through a compressed operator
+        axis), split where a class has more tags of either half or more terms
+        than one call takes; every call after the first accumulates."""
         classes = {}
         for t in self.terms:
             key = (tuple(self.s2_0[t[0]].shape), tuple(self.s2_1[t[1]].shape))
             classes.setdefault(key, []).append(t)
+        if len(self.ops) > _lib.MAX_SLOTS:
+            raise ValueError("stage 3: %d operator tags, more than the %d one call takes" %
+                             (len(self.ops), _lib.MAX_SLOTS))
+        chunks = []
+        for key, terms in classes.items():
+            cur, s0, s1 = [], set(), set()
+            for t in terms:
+                if cur and (len(s0 | {t[0]}) > _lib.MAX_SLOTS or len(s1 | {t[1]}) > _lib.MAX_SLOTS
+                            or len(cur) + 1 > _lib.MAX_ENTRIES):
+                    chunks.append((key, cur))
+                    cur, s0, s1 = [], set(), set()
+                cur.append(t)
+                s0.add(t[0])
+                s1.add(t[1])
+            chunks.append((key, cur))
         self._groups = []
         self._po, self._ko = _lib.ptr_array([t.data_ptr() for t in self.ops])
-        for (sh0, sh1), terms in classes.items():
+        for (sh0, sh1), terms in chunks:
             i0s = sorted({t[0] for t in terms})
             i1s = sorted({t[1] for t in terms})
             m0 = {v: i for i, v in enumerate(i0s)}

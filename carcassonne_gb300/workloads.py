@@ -204,6 +204,10 @@ def absorb_main(argv=None):
     p.add_argument("--precision", default="tc", choices=["tc", "fp64"], help="absorption precision")
     p.add_argument("--compress-precision", default="fp64", choices=["tc", "fp64"],
                    help="precision of the compressor's large contractions")
+    p.add_argument("--build", type=int, default=0,
+                   help="after the last step, build the center's expectation and normalization multipliers "
+                        "(stages 1-3) this many times, the last inside an NVTX range named \"build\", and print "
+                        "their wall times")
     a = p.parse_args(argv)
     from .compression import compression_precision
     system = bond_start_system(a.kind, a.D, a.seed)
@@ -239,6 +243,20 @@ def absorb_main(argv=None):
                               absorb_s=round(seconds, 6),
                               compress_s=round(compress_s, 6), side_shape=list(side.shape),
                               side_tags=len(system.sides[step % 4]))), flush=True)
+    times = []
+    for rep in range(a.build):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if rep == a.build - 1:
+            torch.cuda.nvtx.range_push("build")
+        system.formExpectationAndNormalizationMultipliers()
+        torch.cuda.synchronize()
+        times.append(round(time.perf_counter() - t0, 6))
+        if rep == a.build - 1:
+            torch.cuda.nvtx.range_pop()
+    if times:
+        print(json.dumps(dict(build_s=times, side_tags=[len(sd) for sd in system.sides],
+                              corner_tags=[len(c) for c in system.corners])), flush=True)
 
 
 if __name__ == "__main__":

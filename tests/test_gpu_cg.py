@@ -81,3 +81,26 @@ def test_grid_cg_reports_an_exhausted_budget(lib):
     G, c = _system(512, 512, 9)
     x, st, r = _run(lib, "grid", G, c, max_iter=3)
     assert st[0] == 3 and st[1] == 0 and r > 1e-10
+
+
+@pytest.mark.parametrize("name", ["grid"])
+def test_grid_cg_inconsistent_singular_system_stays_bounded(lib, name):
+    """A rank-deficient G and a right-hand side with a part of 1e-9 outside
+    its range (the rounding of formed normal equations): no x reaches the
+    tolerance, and past the least-squares residual the steps along G's
+    near-null directions would grow without bound.  The solver returns its
+    best iterate, bounded, whose true residual is the unreachable part, and
+    reports it."""
+    n, rank = 256, 40
+    G, c = _system(n, rank, 11)
+    rng = np.random.default_rng(12)
+    w, v = np.linalg.eigh(G)
+    null = v[:, : n - rank] @ (rng.standard_normal(n - rank) + 1j * rng.standard_normal(n - rank))
+    c_bad = c + 1e-9 * np.linalg.norm(c) * null / np.linalg.norm(null)
+    x, st, r = _run(lib, name, G, c_bad)
+    assert st[0] >= 0 and st[1] == 0
+    true = np.linalg.norm(G @ x - c_bad) / np.linalg.norm(c_bad)
+    assert abs(r - true) <= 1e-3 * true + 1e-14, (r, true)
+    assert 5e-10 <= r <= 1e-8, r
+    x_ls = np.linalg.pinv(G, rcond=1e-12) @ c_bad
+    assert np.linalg.norm(x) <= 1e3 * np.linalg.norm(x_ls)

@@ -112,3 +112,29 @@ def test_trajectory_operator_and_absorption(mods, name):
                 for j, t in enumerate(tags):
                     want = traj[f"{name}_{step + 1}_{kind}{idx}_{j}"]
                     assert rel(got[parse(t)], want) < 1e-10, (kind, idx, t)
+
+
+def test_grouped_table_above_the_slot_limits():
+    """A grouped FP64 table with more operands, outputs and entries than one
+    library call takes (64 slots, 512 entries) is split by the planner and
+    still gives every output its sum; an output fed by more than 64 operands
+    is accumulated over consecutive calls."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from carcassonne_gb300 import engine
+    rng = np.random.default_rng(21)
+    cplx = lambda *s: rng.standard_normal(s) + 1j * rng.standard_normal(s)
+    A = [cplx(8, 6) for _ in range(90)]
+    B = [cplx(6, 5) for _ in range(75)]
+    n_c = 100
+    entries = [(int(rng.integers(90)), int(rng.integers(75)), int(rng.integers(n_c - 1))) for _ in range(700)]
+    entries += [(i, i % 75, n_c - 1) for i in range(90)]  # the last output: 90 distinct A operands
+    outs = [torch.full((8, 5), 7.0 + 0j, dtype=torch.complex128, device="cuda") for _ in range(n_c)]
+    engine.contract_grouped("ij,jk->ik", [torch.as_tensor(a).cuda() for a in A], [torch.as_tensor(b).cuda() for b in B],
+                            outs, entries)
+    ref = [np.zeros((8, 5), complex) for _ in range(n_c)]
+    for a, b, c in entries:
+        ref[c] += A[a] @ B[b]
+    for c in range(n_c):
+        got = outs[c].cpu().numpy()
+        assert np.abs(got - ref[c]).max() <= 1e-13 * max(1.0, np.abs(ref[c]).max()), c

@@ -123,6 +123,36 @@ def test_jacobi_eigh_nearly_hermitian_rank_deficient(env, n, rank):
     assert np.abs(v.conj().T @ v - np.eye(n)).max() <= 1e-12
 
 
+@pytest.mark.parametrize("n,rank", [(64, 40), (200, 150)])
+def test_hegv_projected_on_singular_normalization(env, n, rank):
+    """N of rank < n with rounding-level negative eigenvalues: Cholesky
+    rejects it, and the projected solve returns the lowest eigenpair of the
+    pencil on N's range (canonical orthogonalisation restated in numpy)."""
+    TorchData, linalg, _, _ = env
+    rng = np.random.default_rng(n + 3 * rank)
+    x = cn(rng, n, rank)
+    nm = x @ x.conj().T
+    e = cn(rng, n, n)
+    nm = nm + 1e-14 * np.abs(nm).max() * 0.5 * (e + e.conj().T) / np.abs(e).max()
+    h = cn(rng, n, n)
+    h = h + h.conj().T
+    with pytest.raises(np.linalg.LinAlgError):
+        linalg.hegv_lowest(TorchData(h), TorchData(nm))
+    lam, xv, kept = linalg.hegv_lowest_projected(TorchData(h), TorchData(nm))
+    w, v = np.linalg.eigh(0.5 * (nm + nm.conj().T))
+    keep = w > 1e-12 * np.abs(w).max()
+    X = v[:, keep] / np.sqrt(w[keep])
+    cw = np.linalg.eigvalsh(X.conj().T @ h @ X)
+    ref, scale = cw[0], np.abs(cw).max()
+    assert kept == int(keep.sum()) == rank
+    assert abs(lam - ref) <= 1e-10 * scale
+    xa = xv.toArray()
+    assert abs((xa.conj() @ nm @ xa).real - 1.0) < 1e-9
+    # the residual vanishes on N's range
+    r = X.conj().T @ (h @ xa - lam * (nm @ xa))
+    assert np.abs(r).max() <= 1e-9 * scale
+
+
 @pytest.mark.parametrize("n", [1, 31, 33, 100, 512])
 def test_cholesky_and_generalized_lowest(env, n):
     TorchData, linalg, _, _ = env
