@@ -250,8 +250,8 @@ def solve_section():
 GROWTH = {
     "ti_h3_D2_c8": dict(workload="growth run, transverse Ising h=3, D=2, chi=64 (c=8), 20 absorptions", kind="ti",
                         D=2, seed=0, steps=20, new_dimension=8),
-    "heis_D4_c8": dict(workload="growth run, Heisenberg XXX, D=4, chi=64 (c=8), first 12 absorptions", kind="heis",
-                       D=4, seed=2, steps=12, new_dimension=8),
+    "heis_D4_c8": dict(workload="growth run, Heisenberg XXX, D=4, chi=64 (c=8), 40 absorptions", kind="heis",
+                       D=4, seed=2, steps=40, new_dimension=8, cpu_step=11),
 }
 
 
@@ -460,13 +460,16 @@ def _cpu_contract_compress(system, direction, new_dimension):
     return t1 - t0, time.perf_counter() - t1
 
 
-def growth_section(cpu=True, heis_steps=None, cpu_step=None, rescale=False):
-    """Both growth runs; ``heis_steps`` runs the Heisenberg one for that many
-    absorptions (the configured run is 40; 12 by default, to keep the default
-    bench short), ``cpu_step`` puts the CPU reference's step there instead of
-    at each run's last step, ``rescale`` divides each boundary by its largest
-    entry after every step (energies are unchanged; the scale of the grown
-    environment otherwise drifts with the number of absorptions)."""
+def growth_section(cpu=True, heis_steps=None, cpu_step=None, rescale=True):
+    """Both configured growth runs; ``heis_steps`` runs the Heisenberg one for
+    that many absorptions instead of 40, ``cpu_step`` puts the CPU reference's
+    step there instead of the run's own (the Heisenberg run's step 11, the
+    transverse-Ising run's last), ``rescale`` divides each boundary by its
+    largest entry after every step.  Energies and eigenvectors do not change
+    under it (H_eff and N_eff scale alike).  Without it the boundaries' scales
+    drift by up to tenfold per absorption, and the unscaled Heisenberg run
+    stopped partway at a step whose N_eff had no eigenvalue above 1e-12 of
+    its largest magnitude left to solve on."""
     out = {}
     for name, spec in GROWTH.items():
         if heis_steps and spec["kind"] == "heis":
@@ -475,7 +478,8 @@ def growth_section(cpu=True, heis_steps=None, cpu_step=None, rescale=False):
         if rescale:
             spec = dict(spec, rescale=True, workload=spec["workload"] + ", boundaries rescaled after each step")
         last = spec["steps"] - 1
-        cpu_steps = ((min(cpu_step, last) if cpu_step is not None else last),) if cpu else ()
+        own = spec.get("cpu_step", last)
+        cpu_steps = ((min(cpu_step if cpu_step is not None else own, last)),) if cpu else ()
         out[name] = growth_run(spec, cpu_steps)
     return out
 
@@ -500,11 +504,13 @@ def parse_args():
                         "over ranks under torchrun)")
     p.add_argument("--solves-count", type=int, default=256)
     p.add_argument("--growth-heis-steps", type=int, default=None,
-                   help="absorptions of the Heisenberg growth run (the configured run is 40; default 12)")
+                   help="absorptions of the Heisenberg growth run (default: the configured 40)")
     p.add_argument("--growth-cpu-step", type=int, default=None,
-                   help="step of each growth run also run by the CPU reference (default: the last)")
-    p.add_argument("--growth-rescale", action="store_true",
-                   help="divide every boundary by its largest entry after each growth step")
+                   help="step of each growth run also run by the CPU reference (default: the Heisenberg run's 11, the "
+                        "transverse-Ising run's last)")
+    p.add_argument("--growth-no-rescale", dest="growth_rescale", action="store_false",
+                   help="keep the growth runs' boundaries unscaled (by default each boundary is divided by its "
+                        "largest entry after every step)")
     p.add_argument("--no-growth", dest="growth", action="store_false",
                    help="skip the growth runs' per-step time-to-energy (plain vs mixed)")
     return p.parse_args()

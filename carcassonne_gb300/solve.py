@@ -15,7 +15,8 @@ mixed  : H_eff and N_eff formed on the tensor cores from split-BF16 operands
 
 Both return the energy, the N-normalized center and a breakdown of where the
 time went (CUDA events on the current stream).  Where N is too ill-conditioned
-for the mixed reduction, the mixed solve runs the plain one; where FP64
+for the mixed reduction, or out of FP32's range, the mixed solve runs the
+plain one; where FP64
 Cholesky rejects N too, the pencil is solved on the range of N
 (linalg.hegv_lowest_projected).  The result's ``fallback`` key names the path
 taken ("plain" or "projected"; None when there was none).
@@ -169,7 +170,8 @@ def solve_center(H, N, x0=None, precision="plain", tol=None, newton=True):
         if precision == "mixed":
             # the tensor-core N (about 1e-5 relative) factored in complex64
             # is not positive definite: N's condition number is beyond what
-            # the mixed reduction resolves, so this step is solved in FP64
+            # the mixed reduction resolves, or its entries lie outside FP32's
+            # range, so this step is solved in FP64
             out = solve_center(H, N, x0=x0, precision="plain")
             out["fallback"] = "plain" if out.get("fallback") is None else out["fallback"]
             return out
