@@ -394,9 +394,12 @@ int carc_zcg_hpsd(int32_t n, const void* G, const void* c, void* x, double tol, 
 /* The same iteration over a cooperative grid (rows of G spread over up to one
  * CTA per SM, three bounded grid barriers per iteration, per-CTA partial sums
  * added in CTA order: deterministic), for the FP64 rate of the whole GPU
- * rather than one SM.  status[0] = -1 and status[1] = 0 if a grid barrier
- * timed out.  workspace: device scratch of
- * carc_zcg_hpsd_grid_workspace_size(n) bytes. */
+ * rather than one SM.  It also keeps the iterate with the smallest residual
+ * and stops once the residual is 1e8 above it (a c with a part outside the
+ * range of a singular G makes the iterates grow without bound); x receives
+ * that iterate and residual its true |c - G x| / |c| (one more pass over G).
+ * status[0] = -1 and status[1] = 0 if a grid barrier timed out.  workspace:
+ * device scratch of carc_zcg_hpsd_grid_workspace_size(n) bytes. */
 int carc_zcg_hpsd_grid(int32_t n, const void* G, const void* c, void* x, double tol, int32_t max_iter, void* status,
                        void* residual, void* workspace, int64_t workspace_bytes, void* stream);
 int64_t carc_zcg_hpsd_grid_workspace_size(int32_t n);
