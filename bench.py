@@ -923,8 +923,9 @@ def main():
                             **common)
     cpu = cpu_reference(args, args.cpu_seconds) if world == 1 else None
     solve = solve_section() if args.solve else None
-    if solve is not None and args.growth:
-        solve["growth"] = growth_section(cpu=world == 1, heis_steps=args.growth_heis_steps,
+    if solve is not None and args.growth and world == 1:
+        # single-GPU workloads: under torchrun every rank would repeat them
+        solve["growth"] = growth_section(cpu=True, heis_steps=args.growth_heis_steps,
                                          cpu_step=args.growth_cpu_step, rescale=args.growth_rescale)
     batched = None
     if args.batched and world == 1:
